@@ -1,0 +1,333 @@
+"""BK5 operator-apply benchmark (GDoF/s) on one GB300, JSON-line contract.
+
+Workload: the BK5/BP5 FP64 Laplacian on the deformed unit cube, Q4 with GLL
+collocation (p = 4), 128 x 128 x 64 cells = 67,634,433 DoFs, mesh nodes moved
+by x_d += 0.05 sin(2 pi x) sin(2 pi y) sin(2 pi z), Dirichlet boundary, src
+seeded U[-1,1].  One step = one operator application vmult(dst, src) over the
+whole L-vector: dst = 0, the fused gather / D / G / D^T / scatter kernel, the
+constrained identity rows.  Inputs (src 541 MB, G 6.5 GB) are far larger than
+the 129 MB L2, so no flush is needed between steps.
+
+--impl reference times the CPU implementation of the same vmult (the oracle
+restatement, OpenMP over all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(nx=128, ny=128, nz=64, degree=4, amplitude=0.05, seed=1)
+METRIC = "BK5 GDoF/s (FP64 operator apply)"
+
+
+def algorithmic_bytes(n_dofs, n_cells, degree):
+    """src read + dst write + per quadrature point 6 FP64 metric terms and a 4-byte map entry."""
+    n3 = (degree + 1) ** 3
+    return 8 * n_dofs + 8 * n_dofs + n_cells * n3 * (48 + 4)
+
+
+def algorithmic_flops(n_cells, degree):
+    n = degree + 1
+    return n_cells * (12 * n ** 4 + 15 * n ** 3)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("MFGB_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_from_profile(arith: str):
+    """DRAM bytes per launch of the operator kernel from the committed ncu
+    summary for this workload (None if not captured)."""
+    path = os.path.join(ROOT, "profiles", f"bk5_{arith}_p4_67M.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_reference_apply_rate(prob, steps, warmup, src):
+    """Time the oracle's OpenMP vmult on the host cores; returns GDoF/s."""
+    for _ in range(warmup):
+        prob.apply(src)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        prob.apply(src)
+    dt = (time.perf_counter() - t0) / steps
+    return prob.n_dofs / dt / 1e9, dt
+
+
+def run_reference(args, rank, world):
+    """CPU implementation of the same vmult (oracle restatement; the reference's
+    deal.II CPU path cannot be built here)."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    w = WORKLOAD
+    prob = oracle.BoxProblem(w["nx"], w["ny"], w["nz"], w["degree"], amplitude=w["amplitude"])
+    src = prob.rhs(w["seed"])
+    steps = max(1, min(args.steps, 10))
+    warm = max(1, min(args.warmup, 2))
+    rate, dt = cpu_reference_apply_rate(prob, steps, warm, src)
+    cores = oracle.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "GDoF/s",
+        "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded U[-1,1] src, deformed unit-cube mesh)",
+        "config": config_dict(args, prob.n_dofs, prob.n_cells),
+        "cpu_baseline": {"value": rate, "unit": "GDoF/s", "cores": cores, "kind": "port",
+                         "sample": f"full workload, {steps} vmult on {prob.n_dofs} DoFs"},
+        "e2e": {"value": rate, "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, n_dofs, n_cells):
+    w = WORKLOAD
+    return {"workload": f"BK5 vmult p={w['degree']} {w['nx']}x{w['ny']}x{w['nz']} cells deformed "
+                        f"unit cube (a={w['amplitude']}), {n_dofs} DoFs",
+            "degree": w["degree"], "cells": [w["nx"], w["ny"], w["nz"]], "n_dofs": n_dofs,
+            "n_cells": n_cells, "arith": args.arith, "l2": "inputs larger than L2 (no flush)",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+def run_ours(args, rank, world):
+    import ctypes
+
+    import torch
+
+    import benchmarks_gb300 as mf
+    from benchmarks_gb300 import _abi
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    L = mf.lib()
+    w = WORKLOAD
+    A = mf.LaplaceOperator(mf.BoxMesh(w["nx"], w["ny"], w["nz"], degree=w["degree"],
+                                      amplitude=w["amplitude"]), arith=args.arith)
+    n, n_cells = A.m(), A.n_cells
+    arith = mf._arith(args.arith)
+    src = A.rhs_uniform(w["seed"])
+    dst = A.initialize_dof_vector()
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    op, d_dst, d_src = A.handle, ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr())
+
+    def step(ev0=None, ev1=None):
+        # vmult = dst = 0 ; cell loop (one kernel) ; constrained identity rows
+        dst.zero_()
+        if ev0 is not None:
+            ev0.record(stream)
+        _abi.check(L.mfgb_vmult_add(op, d_dst, d_src, arith, sp))
+        if ev1 is not None:
+            ev1.record(stream)
+        _abi.check(L.mfgb_copy_constrained(op, d_dst, d_src, sp))
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local).start() if rank == 0 else None
+    torch.cuda.synchronize()
+    start.record(stream)
+    for k in range(args.steps):
+        step(*ev[k])
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    total_ms = start.elapsed_time(stop)
+    kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    total_ms = max_over_ranks(total_ms, world)
+    barrier(world)
+
+    # end to end through the public vmult with pinned host buffers
+    h_src = src.cpu().pin_memory()
+    h_dst = torch.empty_like(h_src).pin_memory()
+    d_a, d_b = A.initialize_dof_vector(), A.initialize_dof_vector()
+    for _ in range(2):
+        d_a.copy_(h_src, non_blocking=True)
+        A.vmult(d_b, d_a)
+        h_dst.copy_(d_b, non_blocking=True)
+    torch.cuda.synchronize()
+    e_steps = max(3, min(args.steps, 20))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        d_a.copy_(h_src, non_blocking=True)
+        A.vmult(d_b, d_a)
+        h_dst.copy_(d_b, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e_steps, world)
+    # correctness guard on the timed result
+    assert torch.equal(h_dst.cuda(), d_b)
+
+    if rank != 0:
+        return
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    bytes_per = algorithmic_bytes(n, n_cells, w["degree"])
+    achieved = bytes_per / (kernel_ms * 1e-3) / 1e9
+    flops = algorithmic_flops(n_cells, w["degree"])
+    traffic = traffic_from_profile(args.arith)
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        from oracle import oracle
+        sample = oracle.BoxProblem(64, 64, 32, w["degree"], amplitude=w["amplitude"])
+        s_src = sample.rhs(w["seed"])
+        rate, dt = cpu_reference_apply_rate(sample, 5, 1, s_src)
+        cpu = {"value": rate, "unit": "GDoF/s", "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"5 vmult of the oracle (OpenMP) on a 64x64x32-cell p=4 mesh of the same "
+                         f"deformed cube, {sample.n_dofs} DoFs"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "GDoF/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": value / 6.83,
+        "dtype": "f64",
+        "data": "synthetic (seeded U[-1,1] src, deformed unit-cube mesh)",
+        "config": config_dict(args, n, n_cells),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": f"bk5_kernel<5,{'ArithDF' if arith else 'ArithF64'}>",
+                     "kernel_ms": kernel_ms, "bytes_per_launch": bytes_per,
+                     "flops_per_launch": flops,
+                     "fp64_equiv_tflops": flops / (kernel_ms * 1e-3) / 1e12},
+        "e2e": {"value": world * n / (e2e_ms * 1e-3) / 1e9, "unit": "GDoF/s",
+                "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--arith", choices=["df", "fp64"], default="df")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,295 @@
+"""GB300-native matrix-free BK5/BP5 Laplacian engine (host side).
+
+Python mirror of the reference's operator/solver interface for this path --
+deal.II's ``MatrixType`` concept as used by ``Portable::LaplaceOperatorBK35``
+(bakeoff_problems_dealii/include/portable_laplace_operator_bk35.h:16-95) and
+``Step64::HelmholtzOperator`` (bp5_kokkos/benchmark.cc:141-175), plus
+``SolverCG``/``ReductionControl``/``DiagonalMatrix``/``PreconditionIdentity``
+-- over the C ABI of ``libmfgb.so`` (include/mfgb.h).  Vectors are CUDA
+``torch.float64`` tensors (PyTorch is only device memory and streams here);
+every compute call goes to the CUDA library, and importing the operator
+classes without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+from . import _abi
+from ._abi import MfgbError, ARITH_FP64, ARITH_FP64_DF, lib, library_path  # noqa: F401
+
+__all__ = [
+    "BoxMesh", "LaplaceOperator", "ReductionControl", "SolverCG", "DiagonalMatrix",
+    "PreconditionIdentity", "MfgbError", "ARITH_FP64", "ARITH_FP64_DF", "lib", "library_path",
+    "bk5_evector", "bk5_lvector", "dot",
+]
+
+_ARITH = {"fp64": ARITH_FP64, "df": ARITH_FP64_DF, "fp64_df": ARITH_FP64_DF,
+          ARITH_FP64: ARITH_FP64, ARITH_FP64_DF: ARITH_FP64_DF}
+
+
+def _arith(a) -> int:
+    try:
+        return _ARITH[a]
+    except KeyError:
+        raise ValueError(f"unknown arithmetic mode {a!r}") from None
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_ptr():
+    torch = _torch()
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _check_vec(v, n, name):
+    torch = _torch()
+    if not isinstance(v, torch.Tensor) or v.dtype != torch.float64 or not v.is_cuda:
+        raise TypeError(f"{name} must be a CUDA float64 tensor")
+    if v.numel() != n or not v.is_contiguous():
+        raise ValueError(f"{name} must be contiguous with {n} entries")
+    return ctypes.c_void_p(v.data_ptr())
+
+
+@dataclass(frozen=True)
+class BoxMesh:
+    """Structured hex mesh of the unit cube (or a box): nx*ny*nz cells of
+    degree p, GLL nodes moved by x_d += a sin(2 pi x) sin(2 pi y) sin(2 pi z),
+    Dirichlet u = 0 on the boundary."""
+    nx: int
+    ny: int
+    nz: int
+    degree: int
+    amplitude: float = 0.05
+    lo: tuple = (0.0, 0.0, 0.0)
+    hi: tuple = (1.0, 1.0, 1.0)
+
+    @property
+    def n_dofs(self) -> int:
+        p = self.degree
+        return (p * self.nx + 1) * (p * self.ny + 1) * (p * self.nz + 1)
+
+    @property
+    def n_cells(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def _desc(self):
+        return _abi.BoxDesc(self.nx, self.ny, self.nz, self.degree,
+                            (ctypes.c_double * 3)(*self.lo), (ctypes.c_double * 3)(*self.hi),
+                            self.amplitude)
+
+
+class LaplaceOperator:
+    """BK5 Laplacian on Q_p hexahedra with GLL collocation (the
+    ``LaplaceOperatorBK35`` interface): ``vmult``, ``Tvmult``, ``m``, ``n``,
+    ``initialize_dof_vector``, ``compute_diagonal``,
+    ``get_matrix_diagonal_inverse``.
+
+    ``arith`` selects the arithmetic inside the kernels: ``"fp64"`` (native
+    DFMA) or ``"df"`` (FP64-accurate double-float on the FP32 pipes, the
+    default; both meet 1e-12 relative to the FP64 oracle)."""
+
+    def __init__(self, mesh: BoxMesh | None = None, *, degree=None, n_dofs=None, dof_map=None,
+                 G=None, constrained=None, arith="df"):
+        L = lib()
+        self._op = ctypes.c_void_p()
+        if mesh is not None:
+            desc = mesh._desc()
+            _abi.check(L.mfgb_operator_create_box(ctypes.byref(desc), ctypes.byref(self._op)))
+            self.mesh = mesh
+        else:
+            import numpy as np
+            dof_map = np.ascontiguousarray(dof_map, dtype=np.uint32)
+            G = np.ascontiguousarray(G, dtype=np.float64)
+            constrained = np.ascontiguousarray(
+                constrained if constrained is not None else np.zeros(0), dtype=np.int64)
+            n3 = (degree + 1) ** 3
+            n_cells = dof_map.size // n3
+            _abi.check(L.mfgb_operator_create(
+                int(degree), int(n_dofs), int(n_cells),
+                dof_map.ctypes.data_as(ctypes.c_void_p), G.ctypes.data_as(ctypes.c_void_p),
+                int(constrained.size), constrained.ctypes.data_as(ctypes.c_void_p),
+                ctypes.byref(self._op)))
+            self.mesh = None
+        nd, nc, dg, ncons = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int64()
+        _abi.check(L.mfgb_operator_info(self._op, ctypes.byref(nd), ctypes.byref(nc),
+                                        ctypes.byref(dg), ctypes.byref(ncons)))
+        self._n_dofs, self.n_cells, self.degree, self.n_constrained = (
+            nd.value, nc.value, dg.value, ncons.value)
+        self.arith = _arith(arith)
+        self._inv_diag = None
+
+    def __del__(self):
+        op = getattr(self, "_op", None)
+        if op is not None and op.value:
+            try:
+                lib().mfgb_operator_destroy(op)
+            except Exception:
+                pass
+            self._op = None
+
+    # deal.II MatrixType concept ------------------------------------------
+    def m(self) -> int:
+        return self._n_dofs
+
+    def n(self) -> int:
+        return self._n_dofs
+
+    def initialize_dof_vector(self, vec=None):
+        torch = _torch()
+        return torch.zeros(self._n_dofs, dtype=torch.float64, device="cuda")
+
+    def vmult(self, dst, src, arith=None):
+        a = self.arith if arith is None else _arith(arith)
+        _abi.check(lib().mfgb_vmult(self._op, _check_vec(dst, self._n_dofs, "dst"),
+                                    _check_vec(src, self._n_dofs, "src"), a, _stream_ptr()))
+        return dst
+
+    def Tvmult(self, dst, src, arith=None):
+        # the operator is symmetric (portable_laplace_operator_bk35.h:386-400)
+        return self.vmult(dst, src, arith)
+
+    def compute_diagonal(self):
+        d = self.initialize_dof_vector()
+        L = lib()
+        _abi.check(L.mfgb_compute_diagonal(self._op, _check_vec(d, self._n_dofs, "diag"),
+                                           _stream_ptr()))
+        inv = d.clone()
+        _abi.check(L.mfgb_invert_diagonal(self._n_dofs, _check_vec(inv, self._n_dofs, "diag"),
+                                          _stream_ptr()))
+        self._diag = d
+        self._inv_diag = DiagonalMatrix(inv)
+        return d
+
+    def get_matrix_diagonal_inverse(self):
+        if self._inv_diag is None:
+            self.compute_diagonal()
+        return self._inv_diag
+
+    def el(self, row, col):
+        if row != col:
+            raise NotImplementedError("only diagonal entries are available")
+        if self._inv_diag is None:
+            self.compute_diagonal()
+        return float(self._diag[row])
+
+    # extras --------------------------------------------------------------
+    def rhs_uniform(self, seed: int):
+        b = self.initialize_dof_vector()
+        _abi.check(lib().mfgb_rhs_uniform(self._op, ctypes.c_uint64(seed),
+                                          _check_vec(b, self._n_dofs, "b"), _stream_ptr()))
+        return b
+
+    def export(self):
+        """(dof_map, G, constrained) copied to numpy arrays."""
+        import numpy as np
+        n3 = (self.degree + 1) ** 3
+        dof_map = np.zeros(self.n_cells * n3, dtype=np.uint32)
+        G = np.zeros(self.n_cells * 6 * n3)
+        cons = np.zeros(self.n_constrained, dtype=np.int64)
+        _abi.check(lib().mfgb_operator_export(self._op, dof_map.ctypes.data_as(ctypes.c_void_p),
+                                              G.ctypes.data_as(ctypes.c_void_p),
+                                              cons.ctypes.data_as(ctypes.c_void_p)))
+        return dof_map, G, cons
+
+    @property
+    def handle(self):
+        return self._op
+
+
+class DiagonalMatrix:
+    """deal.II DiagonalMatrix: holds the vector it multiplies with."""
+
+    def __init__(self, vector):
+        self.vector = vector
+
+    def get_vector(self):
+        return self.vector
+
+    def vmult(self, dst, src):
+        dst.copy_(self.vector * src)
+        return dst
+
+
+class PreconditionIdentity:
+    def vmult(self, dst, src):
+        dst.copy_(src)
+        return dst
+
+
+class ReductionControl:
+    """deal.II ReductionControl(max_steps, tol, reduce)."""
+
+    def __init__(self, max_steps=100, tol=1e-10, reduce=1e-2):
+        self.max_steps, self.tol, self.reduce = int(max_steps), float(tol), float(reduce)
+        self._last_step = 0
+        self._initial = self._last = 0.0
+
+    def last_step(self):
+        return self._last_step
+
+    def initial_value(self):
+        return self._initial
+
+    def last_value(self):
+        return self._last
+
+
+class SolverCG:
+    """deal.II SolverCG; ``solve(A, x, b, P)`` runs on the device through
+    ``mfgb_cg_solve`` and raises ``MfgbError`` (status NOT_CONVERGED) like
+    deal.II's ``SolverControl::NoConvergence`` when max_steps is reached."""
+
+    def __init__(self, control: ReductionControl):
+        self.control = control
+
+    def solve(self, A: LaplaceOperator, x, b, preconditioner=None, arith=None):
+        ctl = _abi.CgControl(self.control.max_steps, self.control.tol, self.control.reduce,
+                             A.arith if arith is None else _arith(arith))
+        info = _abi.SolveInfo()
+        inv = None
+        if isinstance(preconditioner, DiagonalMatrix):
+            inv = _check_vec(preconditioner.vector, A.n(), "preconditioner")
+        elif preconditioner is not None and not isinstance(preconditioner, PreconditionIdentity):
+            raise TypeError("preconditioner must be PreconditionIdentity or DiagonalMatrix")
+        st = lib().mfgb_cg_solve(A.handle, _check_vec(b, A.n(), "b"), _check_vec(x, A.n(), "x"),
+                                 inv, ctypes.byref(ctl), ctypes.byref(info), _stream_ptr())
+        self.control._last_step = info.steps
+        self.control._initial = info.initial
+        self.control._last = info.last
+        _abi.check(st)
+        return x
+
+
+def bk5_evector(degree, dbasis, G, u, out, arith="fp64"):
+    """E-vector kernel seam (CEED_BK BK5::Parallel::LaplaceOperator)."""
+    n3 = (degree + 1) ** 3
+    nelmt = u.numel() // n3
+    _abi.check(lib().mfgb_bk5_evector(
+        int(degree), nelmt, ctypes.c_void_p(dbasis.data_ptr()), ctypes.c_void_p(G.data_ptr()),
+        ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(out.data_ptr()), _arith(arith),
+        _stream_ptr()))
+    return out
+
+
+def bk5_lvector(degree, dbasis, G, src, dst, dof_indices, arith="fp64"):
+    """L-vector kernel seam (BK3::Parallel::KokkosKernel_1D_Block, GLL form):
+    accumulates into dst."""
+    n3 = (degree + 1) ** 3
+    n_cells = dof_indices.numel() // n3
+    _abi.check(lib().mfgb_bk5_lvector(
+        int(degree), n_cells, ctypes.c_void_p(dbasis.data_ptr()), ctypes.c_void_p(G.data_ptr()),
+        ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(dst.data_ptr()),
+        ctypes.c_void_p(dof_indices.data_ptr()), _arith(arith), _stream_ptr()))
+    return dst
+
+
+def dot(a, b) -> float:
+    r = ctypes.c_double()
+    _abi.check(lib().mfgb_dot(a.numel(), ctypes.c_void_p(a.data_ptr()),
+                              ctypes.c_void_p(b.data_ptr()), ctypes.byref(r), _stream_ptr()))
+    return r.value

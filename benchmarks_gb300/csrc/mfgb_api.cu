@@ -1,0 +1,415 @@
+// mfgb_api.cu -- C ABI: operator set-up, vmult, kernel seams, diagonal, RHS.
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "mfgb_common.cuh"
+#include "mfgb_internal.h"
+
+namespace mfgb {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+mfgb_status cuda_status(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return MFGB_OK;
+  cudaGetLastError();  // clear sticky-free errors
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? MFGB_ERR_OUT_OF_MEMORY : MFGB_ERR_CUDA;
+}
+
+static mfgb_status dev_alloc(void **p, size_t bytes, const char *what) {
+  *p = nullptr;
+  if (bytes == 0) return MFGB_OK;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes > free_b) {
+    set_error(std::string(what) + ": needs " + std::to_string(bytes) + " bytes, " +
+              std::to_string(free_b) + " free on the device");
+    return MFGB_ERR_OUT_OF_MEMORY;
+  }
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_status(e, what);
+  }
+  return MFGB_OK;
+}
+
+mfgb_status ensure_df(mfgb_operator *op) {
+  if (op->d_Gdf) return MFGB_OK;
+  const int64_t ng = op->n_cells * 6 * (int64_t)op->n * op->n * op->n;
+  mfgb_status st = dev_alloc((void **)&op->d_Gdf, sizeof(float2) * ng, "G (double-float)");
+  if (st) return st;
+  st = cuda_status(g_to_df(ng, op->d_G, op->d_Gdf, nullptr), "G -> double-float");
+  if (st) return st;
+  return cuda_status(cudaDeviceSynchronize(), "G -> double-float");
+}
+
+mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int arith,
+                       double *partials, int *grid, cudaStream_t s, const int *done) {
+  const bool full = partials == nullptr;
+  mfgb_status st;
+  if (full && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
+                                "vmult: dst = 0")))
+    return st;
+  cudaError_t e;
+  if (arith == MFGB_ARITH_FP64) {
+    e = bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s, done);
+  } else if (arith == MFGB_ARITH_FP64_DF) {
+    if ((st = ensure_df(op))) return st;
+    e = bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s, done);
+  } else {
+    set_error("vmult: unknown arith mode");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if ((st = cuda_status(e, "vmult: bk5 kernel"))) return st;
+  if (full)
+    return cuda_status(copy_constrained(op->n_constrained, op->d_constrained, src, dst, s),
+                       "vmult: constrained rows");
+  return MFGB_OK;
+}
+
+static void free_operator(mfgb_operator *op) {
+  if (!op) return;
+  cudaFree(op->d_map);
+  cudaFree(op->d_G);
+  cudaFree(op->d_Gdf);
+  cudaFree(op->d_G32);
+  cudaFree(op->d_constrained);
+  cudaFree(op->d_partials);
+  delete op;
+}
+
+static void init_basis(mfgb_operator *op, int degree) {
+  op->degree = degree;
+  op->n = degree + 1;
+  gll_nodes(op->n, op->gll_x, op->gll_w);
+  derivative_matrix(op->n, op->gll_x, op->D);
+}
+
+}  // namespace mfgb
+
+using namespace mfgb;
+
+extern "C" {
+
+const char *mfgb_status_string(mfgb_status s) {
+  switch (s) {
+    case MFGB_OK: return "ok";
+    case MFGB_ERR_INVALID_ARG: return "invalid argument";
+    case MFGB_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case MFGB_ERR_NOT_CONVERGED: return "not converged";
+    case MFGB_ERR_TIMEOUT: return "timeout";
+    case MFGB_ERR_NONFINITE: return "non-finite value";
+    case MFGB_ERR_CUDA: return "CUDA error";
+    case MFGB_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char *mfgb_last_error(void) { return g_last_error.c_str(); }
+
+int mfgb_version(void) { return 1; }
+
+mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **out) {
+  if (!box || !out) {
+    set_error("mfgb_operator_create_box: null argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  if (box->degree < 1 || box->degree > 8 || box->nx < 1 || box->ny < 1 || box->nz < 1 ||
+      !(box->hi[0] > box->lo[0]) || !(box->hi[1] > box->lo[1]) || !(box->hi[2] > box->lo[2])) {
+    set_error("mfgb_operator_create_box: degree must be 1..8 and the box non-empty");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  const int64_t p = box->degree;
+  const int64_t Nx = p * box->nx + 1, Ny = p * box->ny + 1, Nz = p * box->nz + 1;
+  const int64_t n_dofs = Nx * Ny * Nz;
+  if (n_dofs >= (int64_t)MFGB_INVALID_DOF) {
+    set_error("mfgb_operator_create_box: more DoFs than a 32-bit map can index");
+    return MFGB_ERR_UNSUPPORTED;
+  }
+  mfgb_operator *op = new mfgb_operator();
+  init_basis(op, box->degree);
+  op->is_box = true;
+  op->box = *box;
+  op->n_dofs = n_dofs;
+  op->n_cells = (int64_t)box->nx * box->ny * box->nz;
+  const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  // constrained list: every boundary DoF, ascending
+  std::vector<int64_t> cons;
+  cons.reserve(2 * (Nx * Ny + Ny * Nz + Nx * Nz));
+  for (int64_t gz = 0; gz < Nz; ++gz)
+    for (int64_t gy = 0; gy < Ny; ++gy) {
+      const bool face = gz == 0 || gz == Nz - 1 || gy == 0 || gy == Ny - 1;
+      if (face) {
+        for (int64_t gx = 0; gx < Nx; ++gx) cons.push_back(gx + Nx * (gy + Ny * gz));
+      } else {
+        cons.push_back(Nx * (gy + Ny * gz));
+        if (Nx > 1) cons.push_back(Nx - 1 + Nx * (gy + Ny * gz));
+      }
+    }
+  op->n_constrained = (int64_t)cons.size();
+  mfgb_status st;
+  if ((st = dev_alloc((void **)&op->d_map, sizeof(uint32_t) * op->n_cells * n3, "dof map")) ||
+      (st = dev_alloc((void **)&op->d_G, sizeof(double) * op->n_cells * 6 * n3, "G")) ||
+      (st = dev_alloc((void **)&op->d_constrained, sizeof(int64_t) * cons.size(), "constraints"))) {
+    free_operator(op);
+    return st;
+  }
+  if ((st = cuda_status(cudaMemcpy(op->d_constrained, cons.data(), sizeof(int64_t) * cons.size(),
+                                   cudaMemcpyHostToDevice),
+                        "constraints copy")) ||
+      (st = cuda_status(box_map(*box, op->d_map, nullptr), "box map")) ||
+      (st = cuda_status(box_geometry(*box, op->gll_x, op->gll_w, op->D, op->d_G, nullptr),
+                        "box geometry")) ||
+      (st = cuda_status(cudaDeviceSynchronize(), "box set-up"))) {
+    free_operator(op);
+    return st;
+  }
+  *out = op;
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_operator_create(int degree, int64_t n_dofs, int64_t n_cells,
+                                 const uint32_t *h_dof_map, const double *h_G,
+                                 int64_t n_constrained, const int64_t *h_constrained,
+                                 mfgb_operator **out) {
+  if (!out || degree < 1 || degree > 8 || n_dofs < 0 || n_cells < 0 || n_constrained < 0 ||
+      (n_cells > 0 && (!h_dof_map || !h_G)) || (n_constrained > 0 && !h_constrained) ||
+      n_dofs >= (int64_t)MFGB_INVALID_DOF) {
+    set_error("mfgb_operator_create: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  const int64_t n3 = (int64_t)(degree + 1) * (degree + 1) * (degree + 1);
+  for (int64_t t = 0; t < n_cells * n3; ++t)
+    if (h_dof_map[t] != MFGB_INVALID_DOF && (int64_t)h_dof_map[t] >= n_dofs) {
+      set_error("mfgb_operator_create: dof map entry out of range");
+      return MFGB_ERR_INVALID_ARG;
+    }
+  for (int64_t c = 0; c < n_constrained; ++c)
+    if (h_constrained[c] < 0 || h_constrained[c] >= n_dofs) {
+      set_error("mfgb_operator_create: constrained index out of range");
+      return MFGB_ERR_INVALID_ARG;
+    }
+  mfgb_operator *op = new mfgb_operator();
+  init_basis(op, degree);
+  op->n_dofs = n_dofs;
+  op->n_cells = n_cells;
+  op->n_constrained = n_constrained;
+  mfgb_status st;
+  if ((st = dev_alloc((void **)&op->d_map, sizeof(uint32_t) * n_cells * n3, "dof map")) ||
+      (st = dev_alloc((void **)&op->d_G, sizeof(double) * n_cells * 6 * n3, "G")) ||
+      (st = dev_alloc((void **)&op->d_constrained, sizeof(int64_t) * n_constrained,
+                      "constraints"))) {
+    free_operator(op);
+    return st;
+  }
+  if ((n_cells > 0 &&
+       ((st = cuda_status(cudaMemcpy(op->d_map, h_dof_map, sizeof(uint32_t) * n_cells * n3,
+                                     cudaMemcpyHostToDevice),
+                          "map copy")) ||
+        (st = cuda_status(cudaMemcpy(op->d_G, h_G, sizeof(double) * n_cells * 6 * n3,
+                                     cudaMemcpyHostToDevice),
+                          "G copy")))) ||
+      (n_constrained > 0 &&
+       (st = cuda_status(cudaMemcpy(op->d_constrained, h_constrained,
+                                    sizeof(int64_t) * n_constrained, cudaMemcpyHostToDevice),
+                         "constraints copy")))) {
+    free_operator(op);
+    return st;
+  }
+  *out = op;
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_operator_destroy(mfgb_operator *op) {
+  free_operator(op);
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_operator_info(const mfgb_operator *op, int64_t *n_dofs, int64_t *n_cells,
+                               int *degree, int64_t *n_constrained) {
+  if (!op) {
+    set_error("mfgb_operator_info: null operator");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if (n_dofs) *n_dofs = op->n_dofs;
+  if (n_cells) *n_cells = op->n_cells;
+  if (degree) *degree = op->degree;
+  if (n_constrained) *n_constrained = op->n_constrained;
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_operator_export(const mfgb_operator *op, uint32_t *h_dof_map, double *h_G,
+                                 int64_t *h_constrained) {
+  if (!op) {
+    set_error("mfgb_operator_export: null operator");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  mfgb_status st;
+  if (h_dof_map && op->n_cells > 0 &&
+      (st = cuda_status(cudaMemcpy(h_dof_map, op->d_map, sizeof(uint32_t) * op->n_cells * n3,
+                                   cudaMemcpyDeviceToHost),
+                        "export map")))
+    return st;
+  if (h_G && op->n_cells > 0 &&
+      (st = cuda_status(cudaMemcpy(h_G, op->d_G, sizeof(double) * op->n_cells * 6 * n3,
+                                   cudaMemcpyDeviceToHost),
+                        "export G")))
+    return st;
+  if (h_constrained && op->n_constrained > 0 &&
+      (st = cuda_status(cudaMemcpy(h_constrained, op->d_constrained,
+                                   sizeof(int64_t) * op->n_constrained, cudaMemcpyDeviceToHost),
+                        "export constraints")))
+    return st;
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_vmult(const mfgb_operator *op, double *d_dst, const double *d_src, int arith,
+                       void *stream) {
+  if (!op || (op->n_dofs > 0 && (!d_dst || !d_src)) || d_dst == d_src) {
+    set_error("mfgb_vmult: invalid argument (dst and src must be distinct device vectors)");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return vmult_impl(const_cast<mfgb_operator *>(op), d_dst, d_src, arith, nullptr, nullptr,
+                    (cudaStream_t)stream);
+}
+
+mfgb_status mfgb_vmult_add(const mfgb_operator *op, double *d_dst, const double *d_src, int arith,
+                           void *stream) {
+  if (!op || (op->n_dofs > 0 && (!d_dst || !d_src)) || d_dst == d_src) {
+    set_error("mfgb_vmult_add: invalid argument (dst and src must be distinct device vectors)");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  mfgb_operator *o = const_cast<mfgb_operator *>(op);
+  cudaError_t e;
+  mfgb_status st;
+  if (arith == MFGB_ARITH_FP64) {
+    e = bk5_f64(o->n, o->n_cells, o->d_map, o->d_G, d_src, d_dst, o->D, nullptr, nullptr, s);
+  } else if (arith == MFGB_ARITH_FP64_DF) {
+    if ((st = ensure_df(o))) return st;
+    e = bk5_df(o->n, o->n_cells, o->d_map, o->d_Gdf, d_src, d_dst, o->D, nullptr, nullptr, s);
+  } else {
+    set_error("mfgb_vmult_add: unknown arith mode");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return cuda_status(e, "mfgb_vmult_add");
+}
+
+mfgb_status mfgb_copy_constrained(const mfgb_operator *op, double *d_dst, const double *d_src,
+                                  void *stream) {
+  if (!op || (op->n_constrained > 0 && (!d_dst || !d_src))) {
+    set_error("mfgb_copy_constrained: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return cuda_status(copy_constrained(op->n_constrained, op->d_constrained, d_src, d_dst,
+                                      (cudaStream_t)stream),
+                     "mfgb_copy_constrained");
+}
+
+static bool read_basis(int degree, const double *d_dbasis, double *D, cudaStream_t s) {
+  const int n = degree + 1;
+  if (cudaMemcpyAsync(D, d_dbasis, sizeof(double) * n * n, cudaMemcpyDeviceToHost, s) !=
+      cudaSuccess)
+    return false;
+  return cudaStreamSynchronize(s) == cudaSuccess;
+}
+
+mfgb_status mfgb_bk5_lvector(int degree, int64_t n_cells, const double *d_dbasis,
+                             const double *d_G, const double *d_src, double *d_dst,
+                             const uint32_t *d_dof_indices, int arith, void *stream) {
+  if (degree < 1 || degree > 8 || n_cells < 0 ||
+      (n_cells > 0 && (!d_dbasis || !d_G || !d_src || !d_dst || !d_dof_indices))) {
+    set_error("mfgb_bk5_lvector: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if (n_cells == 0) return MFGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  double D[81];
+  if (!read_basis(degree, d_dbasis, D, s)) return cuda_status(cudaGetLastError(), "read dbasis");
+  cudaError_t e;
+  if (arith == MFGB_ARITH_FP64)
+    e = bk5_f64(degree + 1, n_cells, d_dof_indices, d_G, d_src, d_dst, D, nullptr, nullptr, s);
+  else if (arith == MFGB_ARITH_FP64_DF)
+    e = bk5_df_g64(degree + 1, n_cells, d_dof_indices, d_G, d_src, d_dst, D, s);
+  else {
+    set_error("mfgb_bk5_lvector: unknown arith");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return cuda_status(e, "mfgb_bk5_lvector");
+}
+
+mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, const double *d_G,
+                             const double *d_in, double *d_out, int arith, void *stream) {
+  if (degree < 1 || degree > 8 || nelmt < 0 ||
+      (nelmt > 0 && (!d_dbasis || !d_G || !d_in || !d_out))) {
+    set_error("mfgb_bk5_evector: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if (nelmt == 0) return MFGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  double D[81];
+  if (!read_basis(degree, d_dbasis, D, s)) return cuda_status(cudaGetLastError(), "read dbasis");
+  cudaError_t e;
+  if (arith == MFGB_ARITH_FP64)
+    e = bk5_f64(degree + 1, nelmt, nullptr, d_G, d_in, d_out, D, nullptr, nullptr, s);
+  else if (arith == MFGB_ARITH_FP64_DF)
+    e = bk5_df_g64(degree + 1, nelmt, nullptr, d_G, d_in, d_out, D, s);
+  else {
+    set_error("mfgb_bk5_evector: unknown arith");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return cuda_status(e, "mfgb_bk5_evector");
+}
+
+mfgb_status mfgb_compute_diagonal(const mfgb_operator *op, double *d_diag, void *stream) {
+  if (!op || (op->n_dofs > 0 && !d_diag)) {
+    set_error("mfgb_compute_diagonal: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  mfgb_status st;
+  if ((st = cuda_status(cudaMemsetAsync(d_diag, 0, sizeof(double) * op->n_dofs, s), "diag = 0")) ||
+      (st = cuda_status(diagonal_f64(op->n, op->n_cells, op->d_map, op->d_G, op->D, d_diag, s),
+                        "diagonal kernel")))
+    return st;
+  return cuda_status(set_constrained(op->n_constrained, op->d_constrained, d_diag, 1.0, s),
+                     "diagonal constrained rows");
+}
+
+mfgb_status mfgb_invert_diagonal(int64_t n, double *d_diag, void *stream) {
+  if (n < 0 || (n > 0 && !d_diag)) {
+    set_error("mfgb_invert_diagonal: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return cuda_status(invert_diagonal(n, d_diag, (cudaStream_t)stream), "invert diagonal");
+}
+
+mfgb_status mfgb_rhs_uniform(const mfgb_operator *op, uint64_t seed, double *d_b, void *stream) {
+  if (!op || (op->n_dofs > 0 && !d_b)) {
+    set_error("mfgb_rhs_uniform: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  std::vector<double> b(op->n_dofs);
+  std::mt19937_64 gen(seed);
+  for (int64_t i = 0; i < op->n_dofs; ++i)
+    b[i] = 2.0 * ((double)(gen() >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+  cudaStream_t s = (cudaStream_t)stream;
+  mfgb_status st;
+  if ((st = cuda_status(cudaMemcpyAsync(d_b, b.data(), sizeof(double) * op->n_dofs,
+                                        cudaMemcpyHostToDevice, s),
+                        "rhs copy")) ||
+      (st = cuda_status(set_constrained(op->n_constrained, op->d_constrained, d_b, 0.0, s),
+                        "rhs constrained")))
+    return st;
+  return cuda_status(cudaStreamSynchronize(s), "rhs sync");
+}
+
+}  // extern "C"

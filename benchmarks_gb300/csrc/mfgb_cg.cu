@@ -1,0 +1,383 @@
+// mfgb_cg.cu -- conjugate gradients on the BK5 operator.
+//
+// Semantics of deal.II SolverCG with ReductionControl as used by the reference
+// (bp5_kokkos/benchmark.cc:355-378; bakeoff_problems_dealii/tests/
+// scaling_bp35_kokkos_kernel/program.cc:263-287): r0 = b - A x0,
+// tol_eff = max(tol, reduce * |r0|), success as soon as |r_k| <= tol_eff,
+// failure when k reaches max_steps.  Preconditioner: identity or the inverse
+// diagonal (DiagonalMatrix).
+//
+// GB300 layout of one iteration (all on the device, no host round trip):
+//   1. bk5 apply  v += A p, with per-CTA partials of sum_e p_e.(A_e p_e)
+//   2. constrained rows v_c = p_c, partial sum p_c^2
+//   3. update     alpha = rz / pAp; x += alpha p; r -= alpha v;
+//                 partials of r.r and r.z (z = Dinv r, never stored)
+//   4. direction  |r| test -> done flag; beta; p = z + beta p; v = 0
+// Each kernel returns at once when the done flag is set, so a CUDA graph of
+// K iterations can be replayed until the host sees the flag.  All reductions
+// are two-stage with a fixed order (deterministic).
+#include <cmath>
+#include <vector>
+
+#include "mfgb_common.cuh"
+#include "mfgb_internal.h"
+
+namespace mfgb {
+
+struct CgScalars {
+  double rz[2];     // r.z of the current direction, by iteration parity
+  double res[2];    // residual norm, by parity
+  int its[2];       // completed iterations, by parity
+  double tol_eff;
+  int max_steps;
+  int done;         // 0 running, 1 converged, 2 failed
+  int final_its;
+  double final_res;
+};
+
+constexpr int VEC_THREADS = 256;
+constexpr int VEC_BLOCKS = 152 * 8;
+
+template <int T>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < T / 32; ++i) s += sh[i];
+  return s;  // valid in thread 0
+}
+
+// every CTA sums the same partials in the same order -> identical result
+__device__ __forceinline__ double sum_partials(const double *__restrict__ p, int n, int stride,
+                                               double *sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v += p[(size_t)i * stride];
+  double s = block_sum<VEC_THREADS>(v, sh);
+  __syncthreads();
+  if (threadIdx.x == 0) sh[32] = s;
+  __syncthreads();
+  return sh[32];
+}
+
+__global__ void __launch_bounds__(VEC_THREADS)
+    cg_constrained_kernel(int64_t nc, const int64_t *__restrict__ c, const double *__restrict__ p,
+                          double *__restrict__ v, double *__restrict__ partial,
+                          const CgScalars *__restrict__ sc) {
+  if (sc->done) return;
+  __shared__ double sh[40];
+  double acc = 0.0;
+  for (int64_t t = threadIdx.x; t < nc; t += blockDim.x) {
+    const double pv = p[c[t]];
+    v[c[t]] = pv;
+    acc += pv * pv;
+  }
+  const double s = block_sum<VEC_THREADS>(acc, sh);
+  if (threadIdx.x == 0) *partial = s;
+}
+
+__global__ void __launch_bounds__(VEC_THREADS)
+    cg_update_kernel(int64_t n, double *__restrict__ x, double *__restrict__ r,
+                     const double *__restrict__ p, const double *__restrict__ v,
+                     const double *__restrict__ dinv, const double *__restrict__ pap_partials,
+                     int n_pap, double *__restrict__ out_partials, CgScalars *__restrict__ sc,
+                     int parity) {
+  if (sc->done) return;
+  __shared__ double sh[40];
+  const double pap = sum_partials(pap_partials, n_pap, 1, sh);
+  const double alpha = sc->rz[parity] / pap;
+  double rr = 0.0, rz = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double pt = p[t];
+    x[t] = __fma_rn(alpha, pt, x[t]);
+    const double rt = __fma_rn(-alpha, v[t], r[t]);
+    r[t] = rt;
+    const double zt = dinv ? dinv[t] * rt : rt;
+    rr = __fma_rn(rt, rt, rr);
+    rz = __fma_rn(rt, zt, rz);
+  }
+  const double srr = block_sum<VEC_THREADS>(rr, sh);
+  __syncthreads();
+  const double srz = block_sum<VEC_THREADS>(rz, sh);
+  if (threadIdx.x == 0) {
+    out_partials[2 * blockIdx.x] = srr;
+    out_partials[2 * blockIdx.x + 1] = srz;
+  }
+}
+
+__global__ void __launch_bounds__(VEC_THREADS)
+    cg_direction_kernel(int64_t n, const double *__restrict__ r, double *__restrict__ p,
+                        double *__restrict__ v, const double *__restrict__ dinv,
+                        const double *__restrict__ partials, int n_part,
+                        CgScalars *__restrict__ sc, int parity) {
+  if (sc->done) return;
+  __shared__ double sh[40];
+  const double rr = sum_partials(partials, n_part, 2, sh);
+  const double rz_new = sum_partials(partials + 1, n_part, 2, sh);
+  const double res = sqrt(rr);
+  const int it = sc->its[parity] + 1;
+  const bool converged = res <= sc->tol_eff;
+  const bool failed = !converged && (it >= sc->max_steps || isnan(res));
+  if (converged || failed) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      sc->final_its = it;
+      sc->final_res = res;
+      sc->done = converged ? 1 : 2;
+    }
+    return;
+  }
+  const double beta = rz_new / sc->rz[parity];
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double rt = r[t];
+    const double zt = dinv ? dinv[t] * rt : rt;
+    p[t] = __fma_rn(beta, p[t], zt);
+    v[t] = 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->rz[parity ^ 1] = rz_new;
+    sc->its[parity ^ 1] = it;
+    sc->res[parity ^ 1] = res;
+  }
+}
+
+// r = b - v; z = Dinv r; p = z; partials of r.r and r.z
+__global__ void __launch_bounds__(VEC_THREADS)
+    cg_init_kernel(int64_t n, const double *__restrict__ b, const double *__restrict__ v,
+                   double *__restrict__ r, double *__restrict__ p, const double *__restrict__ dinv,
+                   double *__restrict__ out_partials) {
+  __shared__ double sh[40];
+  double rr = 0.0, rz = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double rt = b[t] - v[t];
+    r[t] = rt;
+    const double zt = dinv ? dinv[t] * rt : rt;
+    p[t] = zt;
+    rr = __fma_rn(rt, rt, rr);
+    rz = __fma_rn(rt, zt, rz);
+  }
+  const double srr = block_sum<VEC_THREADS>(rr, sh);
+  __syncthreads();
+  const double srz = block_sum<VEC_THREADS>(rz, sh);
+  if (threadIdx.x == 0) {
+    out_partials[2 * blockIdx.x] = srr;
+    out_partials[2 * blockIdx.x + 1] = srz;
+  }
+}
+
+__global__ void __launch_bounds__(VEC_THREADS)
+    dot_kernel(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
+               double *__restrict__ partials) {
+  __shared__ double sh[40];
+  double s = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    s = __fma_rn(a[t], b[t], s);
+  const double bs = block_sum<VEC_THREADS>(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+}
+
+__global__ void finish_sum_kernel(const double *__restrict__ partials, int n, int stride,
+                                  double *__restrict__ out) {
+  __shared__ double sh[40];
+  const double s = sum_partials(partials, n, stride, sh);
+  if (threadIdx.x == 0) *out = s;
+}
+
+}  // namespace mfgb
+
+using namespace mfgb;
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+mfgb_status alloc(DevBuf &b, size_t bytes) {
+  const cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    set_error("cudaMalloc failed (out of device memory)");
+    return MFGB_ERR_OUT_OF_MEMORY;
+  }
+  return cuda_status(e, "cudaMalloc");
+}
+
+}  // namespace
+
+extern "C" mfgb_status mfgb_dot(int64_t n, const double *d_a, const double *d_b, double *h_result,
+                                void *stream) {
+  if (n < 0 || (n > 0 && (!d_a || !d_b)) || !h_result) {
+    set_error("mfgb_dot: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  DevBuf part;
+  mfgb_status st = alloc(part, sizeof(double) * (VEC_BLOCKS + 1));
+  if (st) return st;
+  double *pp = (double *)part.p;
+  dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_a, d_b, pp);
+  finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(pp, VEC_BLOCKS, 1, pp + VEC_BLOCKS);
+  st = cuda_status(cudaMemcpyAsync(h_result, pp + VEC_BLOCKS, sizeof(double),
+                                   cudaMemcpyDeviceToHost, s),
+                   "dot copy");
+  if (st) return st;
+  return cuda_status(cudaStreamSynchronize(s), "dot sync");
+}
+
+extern "C" mfgb_status mfgb_cg_solve(const mfgb_operator *cop, const double *d_b, double *d_x,
+                                     const double *d_inv_diag, const mfgb_cg_control *ctl,
+                                     mfgb_solve_info *info, void *stream) {
+  if (!cop || !d_b || !d_x || !ctl || !info || ctl->max_steps < 0) {
+    set_error("mfgb_cg_solve: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if (ctl->arith != MFGB_ARITH_FP64 && ctl->arith != MFGB_ARITH_FP64_DF) {
+    set_error("mfgb_cg_solve: unknown arith");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  mfgb_operator *op = const_cast<mfgb_operator *>(cop);
+  const int64_t n = op->n_dofs;
+  cudaStream_t user = (cudaStream_t)stream;
+  mfgb_status st;
+  if (ctl->arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+
+  // work vectors: r, p, v, partials, scalars
+  DevBuf br, bp, bv, bpart, bsc;
+  if ((st = alloc(br, sizeof(double) * n)) || (st = alloc(bp, sizeof(double) * n)) ||
+      (st = alloc(bv, sizeof(double) * n)))
+    return st;
+  double *r = (double *)br.p, *p = (double *)bp.p, *v = (double *)bv.p;
+  const double *dinv = d_inv_diag;
+  constexpr int PAP_CAP = 152 * 64 + 1;
+  if ((st = alloc(bpart, sizeof(double) * (PAP_CAP + 2 * VEC_BLOCKS + 8)))) return st;
+  double *pap_part = (double *)bpart.p;
+  double *vec_part = pap_part + PAP_CAP;
+  if ((st = alloc(bsc, sizeof(CgScalars)))) return st;
+  CgScalars *sc = (CgScalars *)bsc.p;
+
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_status(cudaErrorUnknown, "stream create");
+  }
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  cudaEvent_t ev;
+  cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  cudaEventRecord(ev, user);
+  cudaStreamWaitEvent(s, ev, 0);
+  cudaEventDestroy(ev);
+
+  // r0 = b - A x0, p0 = z0
+  if ((st = vmult_impl(op, v, d_x, ctl->arith, nullptr, nullptr, s))) return st;
+  cg_init_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_b, v, r, p, dinv, vec_part);
+  finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(vec_part, VEC_BLOCKS, 2, vec_part + 2 * VEC_BLOCKS);
+  finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(vec_part + 1, VEC_BLOCKS, 2,
+                                              vec_part + 2 * VEC_BLOCKS + 1);
+  double h2[2];
+  if ((st = cuda_status(cudaMemcpyAsync(h2, vec_part + 2 * VEC_BLOCKS, 2 * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s),
+                        "cg init copy")))
+    return st;
+  if ((st = cuda_status(cudaStreamSynchronize(s), "cg init"))) return st;
+  const double res0 = std::sqrt(h2[0]);
+  info->initial = res0;
+  info->last = res0;
+  info->steps = 0;
+  info->converged = 0;
+  const double tol_eff = std::fmax(ctl->tol, ctl->reduce * res0);
+  if (res0 <= tol_eff) {
+    info->converged = 1;
+    return MFGB_OK;
+  }
+  if (std::isnan(res0)) {
+    set_error("mfgb_cg_solve: initial residual is NaN");
+    return MFGB_ERR_NONFINITE;
+  }
+  if (ctl->max_steps == 0) return MFGB_ERR_NOT_CONVERGED;
+
+  CgScalars hsc{};
+  hsc.rz[0] = h2[1];
+  hsc.res[0] = res0;
+  hsc.its[0] = 0;
+  hsc.tol_eff = tol_eff;
+  hsc.max_steps = ctl->max_steps;
+  hsc.done = 0;
+  if ((st = cuda_status(cudaMemcpyAsync(sc, &hsc, sizeof(hsc), cudaMemcpyHostToDevice, s),
+                        "cg scalars")))
+    return st;
+  if ((st = cuda_status(cudaMemsetAsync(v, 0, sizeof(double) * n, s), "v = 0"))) return st;
+
+  // capture K iterations into a graph (parity alternates, K even)
+  const int K = 16;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if ((st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                        "begin capture")))
+    return st;
+  mfgb_status cap_st = MFGB_OK;
+  for (int k = 0; k < K && cap_st == MFGB_OK; ++k) {
+    const int parity = k & 1;
+    int grid = 0;
+    cap_st = vmult_impl(op, v, p, ctl->arith, pap_part, &grid, s, &sc->done);
+    if (cap_st) break;
+    if (grid + 1 > PAP_CAP) {
+      set_error("mfgb_cg_solve: partials buffer too small");
+      cap_st = MFGB_ERR_UNSUPPORTED;
+      break;
+    }
+    cg_constrained_kernel<<<1, VEC_THREADS, 0, s>>>(op->n_constrained, op->d_constrained, p, v,
+                                                     pap_part + grid, sc);
+    cg_update_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_x, r, p, v, dinv, pap_part, grid + 1,
+                                                        vec_part, sc, parity);
+    cg_direction_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, r, p, v, dinv, vec_part, VEC_BLOCKS,
+                                                           sc, parity);
+  }
+  const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (cap_st) {
+    if (graph) cudaGraphDestroy(graph);
+    return cap_st;
+  }
+  if ((st = cuda_status(ce, "end capture"))) return st;
+  if ((st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate"))) {
+    cudaGraphDestroy(graph);
+    return st;
+  }
+  CgScalars out{};
+  for (;;) {
+    cudaError_t e = cudaGraphLaunch(exec, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&out, sc, sizeof(out), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      return cuda_status(e, "cg iterations");
+    }
+    if (out.done) break;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  info->steps = out.final_its;
+  info->last = out.final_res;
+  info->converged = out.done == 1;
+  if (out.done == 1) return MFGB_OK;
+  if (std::isnan(out.final_res)) {
+    set_error("mfgb_cg_solve: residual became NaN");
+    return MFGB_ERR_NONFINITE;
+  }
+  set_error("mfgb_cg_solve: max_steps reached");
+  return MFGB_ERR_NOT_CONVERGED;
+}

@@ -1,0 +1,165 @@
+// mfgb_common.cuh -- shared device/host helpers for the GB300 BK5/BP5 engine.
+//
+// Arithmetic policies used by the templated operator kernels:
+//   ArithF64  native FP64 (DFMA; GB300 runs FP64 at ~1/58 of its FP32 rate)
+//   ArithF32  native FP32
+//   ArithDF   "double-float": every value is an unevaluated pair hi + lo of
+//             floats (about 2^-47 relative precision), computed on the FP32
+//             pipes with error-free transformations: TwoProduct by FMA and
+//             Knuth's TwoSum (accumulation as in Ogita, Rump & Oishi,
+//             "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).
+//             Conversions to and from double use integer bit operations only,
+//             so no FP64-pipe conversion instruction is issued.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define MFGB_INVALID_DOF 0xFFFFFFFFu
+
+namespace mfgb {
+
+// ---------------------------------------------------------------- df type --
+struct df {
+  float hi, lo;
+};
+
+// double -> (hi, lo) with integer ops: hi = x truncated to 24 significant
+// bits, lo = the remaining 29 mantissa bits rounded to float.  |x| < 2^-126
+// flushes to zero (below any value this engine carries); |x| >= 2^128 is
+// outside the float exponent range and is returned as (+-inf, 0).
+__device__ __forceinline__ df df_from_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const unsigned sign = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7FFu);
+  df r;
+  if (e <= 896) { r.hi = 0.f; r.lo = 0.f; return r; }
+  if (e >= 1151) { r.hi = __uint_as_float(sign | 0x7F800000u); r.lo = 0.f; return r; }
+  const unsigned hm = ((hw & 0xFFFFFu) << 3) | (lw >> 29);
+  r.hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | hm);
+  const unsigned rem = lw & 0x1FFFFFFFu;
+  if (rem == 0u || e < 949) {
+    r.lo = 0.f;
+  } else {
+    const unsigned fb = __float_as_uint(__uint2float_rn(rem));
+    r.lo = __uint_as_float(sign | (fb + ((unsigned)(e - 1075) << 23)));
+  }
+  return r;
+}
+
+// exact float -> double widening by integer ops (subnormal floats -> 0)
+__device__ __forceinline__ double double_from_float_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xFFu;
+  if (ex == 0u) return 0.0;
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(ex + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+__device__ __forceinline__ double df_to_double(df a) {
+  return double_from_float_exact(a.hi) + double_from_float_exact(a.lo);
+}
+
+// Knuth TwoSum: s + t == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &t) {
+  s = __fadd_rn(a, b);
+  const float z = __fsub_rn(s, a);
+  t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+}
+
+// lazy double-float accumulator: value = s + c
+struct dfacc {
+  float s, c;
+};
+
+__device__ __forceinline__ void dfacc_zero(dfacc &a) { a.s = 0.f; a.c = 0.f; }
+
+// a += x * y   (x, y double-float)
+__device__ __forceinline__ void dfacc_fma(dfacc &a, df x, df y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  const float e = __fmaf_rn(x.hi, y.hi, -p);
+  float s, t;
+  two_sum(a.s, p, s, t);
+  a.s = s;
+  float c = __fadd_rn(a.c, __fadd_rn(t, e));
+  c = __fmaf_rn(x.hi, y.lo, c);
+  c = __fmaf_rn(x.lo, y.hi, c);
+  a.c = c;
+}
+
+__device__ __forceinline__ df dfacc_finish(const dfacc &a) {
+  df r;
+  float t;
+  two_sum(a.s, a.c, r.hi, t);
+  r.lo = t;
+  return r;
+}
+
+// ----------------------------------------------------- arithmetic policies --
+// Every policy defines:
+//   V       value type carried through the contractions
+//   Acc     accumulator type
+//   GType   storage type of one geometric-factor component
+//   VecT    L-vector element type
+struct ArithF64 {
+  using V = double;
+  using Acc = double;
+  using GType = double;
+  using VecT = double;
+  static __device__ __forceinline__ void zero(Acc &a) { a = 0.0; }
+  static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fma_rn(x, y, a); }
+  static __device__ __forceinline__ V finish(const Acc &a) { return a; }
+  static __device__ __forceinline__ V load_vec(VecT x) { return x; }
+  static __device__ __forceinline__ VecT store_vec(V x) { return x; }
+  static __device__ __forceinline__ V load_g(GType g) { return g; }
+  static __device__ __forceinline__ V zero_v() { return 0.0; }
+  static __device__ __forceinline__ double to_double(V x) { return x; }
+};
+
+struct ArithF32 {
+  using V = float;
+  using Acc = float;
+  using GType = float;
+  using VecT = float;
+  static __device__ __forceinline__ void zero(Acc &a) { a = 0.f; }
+  static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fmaf_rn(x, y, a); }
+  static __device__ __forceinline__ V finish(const Acc &a) { return a; }
+  static __device__ __forceinline__ V load_vec(VecT x) { return x; }
+  static __device__ __forceinline__ VecT store_vec(V x) { return x; }
+  static __device__ __forceinline__ V load_g(GType g) { return g; }
+  static __device__ __forceinline__ V zero_v() { return 0.f; }
+  static __device__ __forceinline__ double to_double(V x) { return (double)x; }
+};
+
+struct ArithDF {
+  using V = df;
+  using Acc = dfacc;
+  using GType = float2;  // (hi, lo)
+  using VecT = double;
+  static __device__ __forceinline__ void zero(Acc &a) { dfacc_zero(a); }
+  static __device__ __forceinline__ void fma(Acc &a, V x, V y) { dfacc_fma(a, x, y); }
+  static __device__ __forceinline__ V finish(const Acc &a) { return dfacc_finish(a); }
+  static __device__ __forceinline__ V load_vec(VecT x) { return df_from_double(x); }
+  static __device__ __forceinline__ VecT store_vec(V x) { return df_to_double(x); }
+  static __device__ __forceinline__ V load_g(GType g) { df r; r.hi = g.x; r.lo = g.y; return r; }
+  static __device__ __forceinline__ V zero_v() { df r; r.hi = 0.f; r.lo = 0.f; return r; }
+  static __device__ __forceinline__ double to_double(V x) { return df_to_double(x); }
+};
+
+// ArithDF reading FP64 geometric factors (the kernel seams, where the caller
+// supplies G in double): each component is split to (hi, lo) on load.
+struct ArithDFG64 : ArithDF {
+  using GType = double;
+  static __device__ __forceinline__ V load_g(GType g) { return df_from_double(g); }
+};
+
+// 1D derivative matrix D[point*N + basis] passed by value (kernel parameter
+// space, i.e. the constant bank), in the value type of the policy.
+template <int N, class A>
+struct Basis {
+  typename A::V D[N * N];
+};
+
+}  // namespace mfgb

@@ -1,0 +1,48 @@
+// mfgb_dispatch.cuh -- runtime degree dispatch for the BK5 kernels.
+#pragma once
+#include "mfgb_launch.cuh"
+
+namespace mfgb {
+
+template <class A> struct BasisValue;
+template <> struct BasisValue<ArithF64> {
+  static double from(double d) { return d; }
+};
+template <> struct BasisValue<ArithF32> {
+  static float from(double d) { return (float)d; }
+};
+template <> struct BasisValue<ArithDF> {
+  static df from(double d) {
+    df r;
+    r.hi = (float)d;
+    r.lo = (float)(d - (double)r.hi);
+    return r;
+  }
+};
+template <> struct BasisValue<ArithDFG64> : BasisValue<ArithDF> {};
+
+template <int N, class A, bool EVEC, bool EN>
+cudaError_t bk5_with_basis(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
+                           const typename A::VecT *src, typename A::VecT *dst, const double *D64,
+                           double *partials, int *grid, cudaStream_t s, const int *done) {
+  Basis<N, A> b;
+  for (int q = 0; q < N * N; ++q) b.D[q] = BasisValue<A>::from(D64[q]);
+  return bk5_launch<N, A, EVEC, EN>(n_cells, map, G, src, dst, b, partials, grid, s, done);
+}
+
+template <class A, bool EVEC, bool EN>
+cudaError_t bk5_dispatch(int N, int64_t n_cells, const uint32_t *map, const typename A::GType *G,
+                         const typename A::VecT *src, typename A::VecT *dst, const double *D64,
+                         double *partials, int *grid, cudaStream_t s,
+                         const int *done = nullptr) {
+  switch (N) {
+#define MFGB_CASE(NN) \
+  case NN: return bk5_with_basis<NN, A, EVEC, EN>(n_cells, map, G, src, dst, D64, partials, grid, s, done);
+    MFGB_CASE(2) MFGB_CASE(3) MFGB_CASE(4) MFGB_CASE(5) MFGB_CASE(6) MFGB_CASE(7) MFGB_CASE(8)
+    MFGB_CASE(9)
+#undef MFGB_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace mfgb

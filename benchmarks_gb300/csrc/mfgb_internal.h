@@ -1,0 +1,72 @@
+// mfgb_internal.h -- host-side internals shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+
+#include "mfgb.h"
+
+struct mfgb_operator {
+  int degree = 0;
+  int n = 0;  // points per direction
+  int64_t n_dofs = 0, n_cells = 0, n_constrained = 0;
+  uint32_t *d_map = nullptr;      // [n_cells][n^3]
+  double *d_G = nullptr;          // [n_cells][6][n^3]
+  float2 *d_Gdf = nullptr;        // same, double-float pairs (built on demand)
+  float *d_G32 = nullptr;         // same, FP32 (built on demand)
+  int64_t *d_constrained = nullptr;
+  double D[81] = {0};             // derivative matrix D[q*n + b]
+  double gll_x[9] = {0}, gll_w[9] = {0};
+  bool is_box = false;
+  mfgb_box_desc box{};
+  // workspace for reductions (per-CTA partials)
+  double *d_partials = nullptr;
+  int partials_cap = 0;
+};
+
+namespace mfgb {
+
+void set_error(const std::string &msg);
+mfgb_status cuda_status(cudaError_t e, const char *what);
+
+// 1D bases (host, FP64)
+void gll_nodes(int n, double *x, double *w);
+double lagrange_derivative(int n, const double *nodes, int j, double x);
+double lagrange_value(int n, const double *nodes, int j, double x);
+void derivative_matrix(int n, const double *nodes, double *D);
+
+// BK5 kernels (map == nullptr selects E-vector mode where supported)
+cudaError_t bk5_f64(int N, int64_t n_cells, const uint32_t *map, const double *G, const double *src,
+                    double *dst, const double *D, double *partials, int *grid, cudaStream_t s,
+                    const int *done = nullptr);
+cudaError_t bk5_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const double *src,
+                   double *dst, const double *D, double *partials, int *grid, cudaStream_t s,
+                    const int *done = nullptr);
+cudaError_t bk5_df_g64(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                       const double *src, double *dst, const double *D, cudaStream_t s);
+cudaError_t bk5_f32(int N, int64_t n_cells, const uint32_t *map, const float *G, const float *src,
+                    float *dst, const double *D, double *partials, int *grid, cudaStream_t s,
+                    const int *done = nullptr);
+
+// set-up kernels (mfgb_setup.cu)
+cudaError_t box_map(const mfgb_box_desc &b, uint32_t *d_map, cudaStream_t s);
+cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
+                         const double *D, double *d_G, cudaStream_t s);
+cudaError_t g_to_df(int64_t n, const double *G, float2 *Gdf, cudaStream_t s);
+cudaError_t g_to_f32(int64_t n, const double *G, float *G32, cudaStream_t s);
+cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                         const double *D, double *diag, cudaStream_t s);
+cudaError_t set_constrained(int64_t n_constrained, const int64_t *constrained, double *v,
+                            double value, cudaStream_t s);
+cudaError_t copy_constrained(int64_t n_constrained, const int64_t *constrained, const double *src,
+                             double *dst, cudaStream_t s);
+cudaError_t invert_diagonal(int64_t n, double *d, cudaStream_t s);
+
+// operator helpers (mfgb_api.cu)
+mfgb_status ensure_df(mfgb_operator *op);
+mfgb_status ensure_partials(mfgb_operator *op, int n);
+// vmult with optional energy partials (p.Ap) for the solver
+mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int arith,
+                       double *partials, int *grid, cudaStream_t s, const int *done = nullptr);
+
+}  // namespace mfgb

@@ -1,0 +1,300 @@
+// mfgb_setup.cu -- bases, structured-box set-up kernels, diagonal, constraints.
+#include <cmath>
+
+#include "mfgb_common.cuh"
+#include "mfgb_internal.h"
+
+namespace mfgb {
+
+// ------------------------------------------------------------------ bases --
+static void legendre_pair(int N, double x, double *pm1, double *pN) {
+  double p0 = 1.0, p1 = x;
+  if (N == 0) { *pm1 = 0.0; *pN = 1.0; return; }
+  for (int k = 2; k <= N; ++k) {
+    const double pk = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+    p0 = p1;
+    p1 = pk;
+  }
+  *pm1 = p0;
+  *pN = p1;
+}
+
+// Gauss-Lobatto-Legendre points: Newton on x P_N - P_{N-1} from the
+// Chebyshev-Gauss-Lobatto points, w = 2 / (N (N+1) P_N^2); symmetrised.
+void gll_nodes(int n, double *x, double *w) {
+  if (n == 1) { x[0] = 0.0; w[0] = 2.0; return; }
+  const int N = n - 1;
+  for (int i = 0; i < n; ++i) {
+    double xi = -std::cos(M_PI * i / N);
+    for (int it = 0; it < 200; ++it) {
+      double pm1, pN;
+      legendre_pair(N, xi, &pm1, &pN);
+      const double dx = (xi * pN - pm1) / ((N + 1.0) * pN);
+      xi -= dx;
+      if (std::fabs(dx) < 1e-17) break;
+    }
+    double pm1, pN;
+    legendre_pair(N, xi, &pm1, &pN);
+    x[i] = xi;
+    w[i] = 2.0 / (N * (N + 1.0) * pN * pN);
+  }
+  for (int i = 0; i < n / 2; ++i) {
+    const double v = 0.5 * (x[N - i] - x[i]);
+    const double ww = 0.5 * (w[N - i] + w[i]);
+    x[i] = -v; x[N - i] = v;
+    w[i] = ww; w[N - i] = ww;
+  }
+  if (n % 2) x[n / 2] = 0.0;
+  x[0] = -1.0;
+  x[N] = 1.0;
+}
+
+// Lagrange basis on arbitrary nodes, in the form of
+// sum_factorization/include/math/lagrange_basis.hpp:29-65.
+double lagrange_value(int n, const double *nodes, int j, double x) {
+  double num = 1.0, den = 1.0;
+  for (int m = 0; m < n; ++m) {
+    if (m == j) continue;
+    num *= (x - nodes[m]);
+    den *= (nodes[j] - nodes[m]);
+  }
+  return num / den;
+}
+
+double lagrange_derivative(int n, const double *nodes, int j, double x) {
+  double sum = 0.0;
+  for (int i = 0; i < n; ++i) {
+    if (i == j) continue;
+    double prod = 1.0;
+    for (int m = 0; m < n; ++m)
+      if (m != i && m != j) prod *= (x - nodes[m]) / (nodes[j] - nodes[m]);
+    sum += (1.0 / (nodes[j] - nodes[i])) * prod;
+  }
+  return sum;
+}
+
+void derivative_matrix(int n, const double *nodes, double *D) {
+  for (int q = 0; q < n; ++q)
+    for (int b = 0; b < n; ++b) D[q * n + b] = lagrange_derivative(n, nodes, b, nodes[q]);
+}
+
+// -------------------------------------------------------------- box mesh --
+__global__ void box_map_kernel(mfgb_box_desc b, uint32_t *__restrict__ map) {
+  const int p = b.degree, n = p + 1, n3 = n * n * n;
+  const int64_t Nx = (int64_t)p * b.nx + 1, Ny = (int64_t)p * b.ny + 1, Nz = (int64_t)p * b.nz + 1;
+  const int64_t total = (int64_t)b.nx * b.ny * b.nz * n3;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = t / n3;
+    const int l = (int)(t - e * n3);
+    const int i = l / (n * n), j = (l / n) % n, k = l % n;
+    const int64_t cx = e % b.nx, cy = (e / b.nx) % b.ny, cz = e / ((int64_t)b.nx * b.ny);
+    const int64_t gx = cx * p + k, gy = cy * p + j, gz = cz * p + i;
+    const bool bnd = gx == 0 || gx == Nx - 1 || gy == 0 || gy == Ny - 1 || gz == 0 || gz == Nz - 1;
+    map[t] = bnd ? MFGB_INVALID_DOF : (uint32_t)(gx + Nx * (gy + Ny * gz));
+  }
+}
+
+cudaError_t box_map(const mfgb_box_desc &b, uint32_t *d_map, cudaStream_t s) {
+  box_map_kernel<<<152 * 16, 256, 0, s>>>(b, d_map);
+  return cudaGetLastError();
+}
+
+struct GeomParams {
+  double x[9], w[9], D[81];
+};
+
+// One CTA per cell: node coordinates (GLL points of the cell, deformed) in
+// shared memory, then J = dx/dxi by the derivative matrix, and
+// G = |det J| w_i w_j w_k Jinv Jinv^T at every GLL point.
+__global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__restrict__ G) {
+  __shared__ double xyz[729 * 3];
+  const int n = b.degree + 1, n3 = n * n * n;
+  const int64_t e = blockIdx.x;
+  const int64_t cx = e % b.nx, cy = (e / b.nx) % b.ny, cz = e / ((int64_t)b.nx * b.ny);
+  const double hx = (b.hi[0] - b.lo[0]) / b.nx, hy = (b.hi[1] - b.lo[1]) / b.ny,
+               hz = (b.hi[2] - b.lo[2]) / b.nz;
+  const double two_pi = 2.0 * M_PI;
+  for (int l = threadIdx.x; l < n3; l += blockDim.x) {
+    const int i = l / (n * n), j = (l / n) % n, k = l % n;
+    const double X = b.lo[0] + ((double)cx + 0.5 * (gp.x[k] + 1.0)) * hx;
+    const double Y = b.lo[1] + ((double)cy + 0.5 * (gp.x[j] + 1.0)) * hy;
+    const double Z = b.lo[2] + ((double)cz + 0.5 * (gp.x[i] + 1.0)) * hz;
+    const double s = b.amplitude * sin(two_pi * X) * sin(two_pi * Y) * sin(two_pi * Z);
+    xyz[3 * l + 0] = X + s;
+    xyz[3 * l + 1] = Y + s;
+    xyz[3 * l + 2] = Z + s;
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < n3; l += blockDim.x) {
+    const int i = l / (n * n), j = (l / n) % n, k = l % n;
+    double J[3][3];
+    for (int d = 0; d < 3; ++d) {
+      double jr = 0, js = 0, jt = 0;
+      for (int m = 0; m < n; ++m) {
+        jr += gp.D[i * n + m] * xyz[3 * (m * n * n + j * n + k) + d];
+        js += gp.D[j * n + m] * xyz[3 * (i * n * n + m * n + k) + d];
+        jt += gp.D[k * n + m] * xyz[3 * (i * n * n + j * n + m) + d];
+      }
+      J[d][0] = jr; J[d][1] = js; J[d][2] = jt;
+    }
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    double Ji[3][3];
+    Ji[0][0] = c00 / det;
+    Ji[1][0] = c01 / det;
+    Ji[2][0] = c02 / det;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    const double jxw = fabs(det) * gp.w[i] * gp.w[j] * gp.w[k];
+    double *Gc = G + e * 6 * n3 + l;
+    int c = 0;
+    for (int a = 0; a < 3; ++a)
+      for (int bb = a; bb < 3; ++bb) {
+        double s = 0;
+        for (int d = 0; d < 3; ++d) s += Ji[a][d] * Ji[bb][d];
+        Gc[c * n3] = jxw * s;
+        ++c;
+      }
+  }
+}
+
+cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
+                         const double *D, double *d_G, cudaStream_t s) {
+  GeomParams gp;
+  const int n = b.degree + 1;
+  for (int i = 0; i < 9; ++i) { gp.x[i] = i < n ? gll_x[i] : 0.0; gp.w[i] = i < n ? gll_w[i] : 0.0; }
+  for (int i = 0; i < 81; ++i) gp.D[i] = i < n * n ? D[i] : 0.0;
+  const int64_t n_cells = (int64_t)b.nx * b.ny * b.nz;
+  if (n_cells == 0) return cudaSuccess;
+  const int threads = ((n * n * n + 31) / 32) * 32;
+  box_geometry_kernel<<<(unsigned)n_cells, threads > 256 ? 256 : threads, 0, s>>>(b, gp, d_G);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------- G conversions --
+__global__ void g_to_df_kernel(int64_t n, const double *__restrict__ G, float2 *__restrict__ out) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double g = G[t];
+    const float hi = (float)g;
+    out[t] = make_float2(hi, (float)(g - (double)hi));
+  }
+}
+
+__global__ void g_to_f32_kernel(int64_t n, const double *__restrict__ G, float *__restrict__ out) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = (float)G[t];
+}
+
+cudaError_t g_to_df(int64_t n, const double *G, float2 *Gdf, cudaStream_t s) {
+  g_to_df_kernel<<<152 * 16, 256, 0, s>>>(n, G, Gdf);
+  return cudaGetLastError();
+}
+
+cudaError_t g_to_f32(int64_t n, const double *G, float *G32, cudaStream_t s) {
+  g_to_f32_kernel<<<152 * 16, 256, 0, s>>>(n, G, G32);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- diagonal --
+// A[l,l] of one cell, l = (i,j,k): for GLL collocation the basis gradient
+// d_r phi_l at point (a,b,c) is D[a][i] delta_bj delta_ck, so
+//   A_e[l,l] = sum_a Grr(a,j,k) D[a][i]^2 + sum_b Gss(i,b,k) D[b][j]^2
+//            + sum_c Gtt(i,j,c) D[c][k]^2
+//            + 2 (Grs D[i][i] D[j][j] + Grt D[i][i] D[k][k] + Gst D[j][j] D[k][k])(i,j,k).
+struct DiagParams {
+  double D[81];
+};
+
+__global__ void diagonal_kernel(int n, int64_t n_cells, const uint32_t *__restrict__ map,
+                                const double *__restrict__ G, DiagParams dp,
+                                double *__restrict__ diag) {
+  const int n3 = n * n * n;
+  const int64_t total = n_cells * n3;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t dof = map[t];
+    if (dof == MFGB_INVALID_DOF) continue;
+    const int64_t e = t / n3;
+    const int q = (int)(t - e * n3);
+    const int i = q / (n * n), j = (q / n) % n, k = q % n;
+    const double *Ge = G + e * 6 * n3;
+    double d = 0.0;
+    for (int a = 0; a < n; ++a) {
+      const double di = dp.D[a * n + i], dj = dp.D[a * n + j], dk = dp.D[a * n + k];
+      d += Ge[0 * n3 + a * n * n + j * n + k] * di * di;
+      d += Ge[3 * n3 + i * n * n + a * n + k] * dj * dj;
+      d += Ge[5 * n3 + i * n * n + j * n + a] * dk * dk;
+    }
+    const double Dii = dp.D[i * n + i], Djj = dp.D[j * n + j], Dkk = dp.D[k * n + k];
+    d += 2.0 * Ge[1 * n3 + q] * Dii * Djj;
+    d += 2.0 * Ge[2 * n3 + q] * Dii * Dkk;
+    d += 2.0 * Ge[4 * n3 + q] * Djj * Dkk;
+    atomicAdd(diag + dof, d);
+  }
+}
+
+cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                         const double *D, double *diag, cudaStream_t s) {
+  DiagParams dp;
+  for (int i = 0; i < 81; ++i) dp.D[i] = i < N * N ? D[i] : 0.0;
+  diagonal_kernel<<<152 * 16, 256, 0, s>>>(N, n_cells, map, G, dp, diag);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- constraints --
+__global__ void set_constrained_kernel(int64_t nc, const int64_t *__restrict__ c, double *v,
+                                       double value) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nc;
+       t += (int64_t)gridDim.x * blockDim.x)
+    v[c[t]] = value;
+}
+
+__global__ void copy_constrained_kernel(int64_t nc, const int64_t *__restrict__ c,
+                                        const double *__restrict__ src, double *dst) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nc;
+       t += (int64_t)gridDim.x * blockDim.x)
+    dst[c[t]] = src[c[t]];
+}
+
+__global__ void invert_diagonal_kernel(int64_t n, double *d) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double v = d[t];
+    d[t] = v > 0.0 ? 1.0 / v : 1.0;
+  }
+}
+
+static unsigned grid_for(int64_t n) {
+  const int64_t g = (n + 255) / 256;
+  return (unsigned)(g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g));
+}
+
+cudaError_t set_constrained(int64_t nc, const int64_t *c, double *v, double value, cudaStream_t s) {
+  if (nc == 0) return cudaSuccess;
+  set_constrained_kernel<<<grid_for(nc), 256, 0, s>>>(nc, c, v, value);
+  return cudaGetLastError();
+}
+
+cudaError_t copy_constrained(int64_t nc, const int64_t *c, const double *src, double *dst,
+                             cudaStream_t s) {
+  if (nc == 0) return cudaSuccess;
+  copy_constrained_kernel<<<grid_for(nc), 256, 0, s>>>(nc, c, src, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t invert_diagonal(int64_t n, double *d, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  invert_diagonal_kernel<<<grid_for(n), 256, 0, s>>>(n, d);
+  return cudaGetLastError();
+}
+
+}  // namespace mfgb

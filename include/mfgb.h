@@ -1,0 +1,159 @@
+/*
+ * mfgb.h -- C ABI of the GB300-native matrix-free BK5/BP5 Laplacian engine
+ * (libmfgb.so).
+ *
+ * Plain pointers and sizes only.  Vector and array arguments named `d_*` are
+ * device pointers owned by the caller; `h_*` are host pointers.  `stream` is a
+ * cudaStream_t passed as void* (NULL = legacy default stream).  Every call
+ * returns an mfgb_status and never exits or aborts; the text of the last error
+ * of the calling thread is available from mfgb_last_error().
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the dealii-X/benchmarks project root).
+ */
+#ifndef MFGB_H
+#define MFGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int mfgb_status;
+enum {
+  MFGB_OK = 0,
+  MFGB_ERR_INVALID_ARG = 1,
+  MFGB_ERR_OUT_OF_MEMORY = 2,
+  MFGB_ERR_NOT_CONVERGED = 3,
+  MFGB_ERR_TIMEOUT = 4,
+  MFGB_ERR_NONFINITE = 5,
+  MFGB_ERR_CUDA = 6,
+  MFGB_ERR_UNSUPPORTED = 7
+};
+
+/* Arithmetic used inside the operator kernels (vectors stay FP64). */
+enum {
+  MFGB_ARITH_FP64 = 0,    /* native FP64 (DFMA) */
+  MFGB_ARITH_FP64_DF = 1  /* FP64-accurate double-float on the FP32 pipes */
+};
+
+#define MFGB_INVALID_DOF_INDEX 0xFFFFFFFFu
+
+typedef struct mfgb_operator mfgb_operator;
+
+/* Structured box mesh: nx*ny*nz hex cells of degree p with GLL nodes,
+   every geometry node moved by x_d += amplitude*sin(2 pi x)sin(2 pi y)sin(2 pi z),
+   Dirichlet u = 0 on the whole boundary, lexicographic DoF numbering (x fastest). */
+typedef struct {
+  int nx, ny, nz;
+  int degree;
+  double lo[3], hi[3];
+  double amplitude;
+} mfgb_box_desc;
+
+typedef struct {
+  int max_steps;    /* ReductionControl max_steps */
+  double tol;       /* absolute tolerance */
+  double reduce;    /* relative reduction of the initial residual */
+  int arith;        /* MFGB_ARITH_* used for the operator inside the solve */
+} mfgb_cg_control;
+
+typedef struct {
+  int steps;        /* last_step() */
+  double initial;   /* initial_value() */
+  double last;      /* last_value() */
+  int converged;    /* 1 if the reduction criterion was met */
+} mfgb_solve_info;
+
+const char *mfgb_status_string(mfgb_status s);
+const char *mfgb_last_error(void);
+int mfgb_version(void);
+
+/* ---- operator set-up ---------------------------------------------------
+ * Replaces the LaplaceOperatorBK35 constructor
+ * (bakeoff_problems_dealii/include/portable_laplace_operator_bk35.h:97-121):
+ * dof map with invalid entries for constrained DoFs (:294-384) and the
+ * geometric factors G[cell][6][q] (:229-292), built on the device. */
+mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **op);
+
+/* Same, from caller-provided host arrays (the deal.II set-up path):
+   h_dof_map[cell*(p+1)^3 + l] (0xFFFFFFFF = constrained), h_G[cell][6][(p+1)^3]
+   in the order rr, rs, rt, ss, st, tt, and the list of constrained DoFs. */
+mfgb_status mfgb_operator_create(int degree, int64_t n_dofs, int64_t n_cells,
+                                 const uint32_t *h_dof_map, const double *h_G,
+                                 int64_t n_constrained, const int64_t *h_constrained,
+                                 mfgb_operator **op);
+
+mfgb_status mfgb_operator_destroy(mfgb_operator *op);
+
+/* m() / n() and sizes (portable_laplace_operator_bk35.h:418-430) */
+mfgb_status mfgb_operator_info(const mfgb_operator *op, int64_t *n_dofs, int64_t *n_cells,
+                               int *degree, int64_t *n_constrained);
+
+/* Copies the operator's map, geometric factors and constraint list to host
+   arrays (any pointer may be NULL). */
+mfgb_status mfgb_operator_export(const mfgb_operator *op, uint32_t *h_dof_map, double *h_G,
+                                 int64_t *h_constrained);
+
+/* ---- operator application ----------------------------------------------
+ * vmult / Tvmult (portable_laplace_operator_bk35.h:123-167, :386-400):
+ * dst = 0; dst += sum_cells P^T A_e P src (masked gather, atomic scatter);
+ * dst[c] = src[c] on constrained DoFs (copy_constrained_values). */
+mfgb_status mfgb_vmult(const mfgb_operator *op, double *d_dst, const double *d_src, int arith,
+                       void *stream);
+
+/* The two parts of vmult, for callers that schedule them (the deal.II cell
+   loop, portable_laplace_operator_bk35.h:140-162, and copy_constrained_values,
+   :166): d_dst += sum_cells P^T A_e P d_src (one kernel launch), and
+   d_dst[c] = d_src[c] on the constrained DoFs. */
+mfgb_status mfgb_vmult_add(const mfgb_operator *op, double *d_dst, const double *d_src, int arith,
+                           void *stream);
+mfgb_status mfgb_copy_constrained(const mfgb_operator *op, double *d_dst, const double *d_src,
+                                  void *stream);
+
+/* Kernel seam of BK3::Parallel::KokkosKernel_1D_Block
+   (bakeoff_problems_dealii/include/bk3_kokkos_kernel.h:32-43) in the
+   GLL-collocated form: accumulates sum_cells P^T A_e P src into d_dst (no
+   zeroing, no constrained copy).  d_dbasis[q*(p+1)+b] = l_b'(x_q); d_G as above. */
+mfgb_status mfgb_bk5_lvector(int degree, int64_t n_cells, const double *d_dbasis,
+                             const double *d_G, const double *d_src, double *d_dst,
+                             const uint32_t *d_dof_indices, int arith, void *stream);
+
+/* E-vector kernel seam of BK5::Parallel::LaplaceOperator<T,nq>
+   (CEED_BK/include/kernels/BK5/templated_cuda_kernels.cuh:11-14):
+   out_e = D^T G_e D in_e for every element, d_G[e][6][(p+1)^3]. */
+mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, const double *d_G,
+                             const double *d_in, double *d_out, int arith, void *stream);
+
+/* ---- diagonal -------------------------------------------------------------
+ * compute_diagonal (bp5_kokkos/benchmark.cc:218-251): exact diagonal of the
+ * operator (1 on constrained rows), then d -> (d > 0 ? 1/d : 1). */
+mfgb_status mfgb_compute_diagonal(const mfgb_operator *op, double *d_diag, void *stream);
+mfgb_status mfgb_invert_diagonal(int64_t n, double *d_diag, void *stream);
+
+/* ---- right-hand side ------------------------------------------------------
+ * b_i = 2*((x_i >> 11) * 2^-53) - 1 with x_i the i-th output of
+ * mt19937_64(seed), i in DoF order; 0 on constrained DoFs. */
+mfgb_status mfgb_rhs_uniform(const mfgb_operator *op, uint64_t seed, double *d_b, void *stream);
+
+/* ---- conjugate gradients ---------------------------------------------------
+ * SolverCG + ReductionControl (bp5_kokkos/benchmark.cc:355-378;
+ * bakeoff_problems_dealii/tests/scaling_bp35_kokkos_kernel/program.cc:263-287).
+ * d_x holds the initial guess on entry.  d_inv_diag is the preconditioner:
+ * NULL = PreconditionIdentity, else DiagonalMatrix with that (inverse
+ * diagonal) vector.  Returns MFGB_ERR_NOT_CONVERGED (with *info filled) when
+ * max_steps is reached. */
+mfgb_status mfgb_cg_solve(const mfgb_operator *op, const double *d_b, double *d_x,
+                          const double *d_inv_diag, const mfgb_cg_control *ctl,
+                          mfgb_solve_info *info, void *stream);
+
+/* ---- vector kernels used by the solver (exposed for tests) -------------- */
+/* result[0] = sum a_i b_i (deterministic two-stage reduction) */
+mfgb_status mfgb_dot(int64_t n, const double *d_a, const double *d_b, double *h_result,
+                     void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,515 @@
+/*
+ * mf_oracle.c -- CPU ORACLE (test infrastructure only) for the BK5/BP5
+ * matrix-free Laplacian.  See mf_oracle.h for conventions.  Only tests/,
+ * the smoke check and bench.py's CPU-baseline leg load this code.
+ *
+ * Reference files followed (paths relative to dealii-X/benchmarks):
+ *   sum_factorization/include/math/lagrange_basis.hpp:9-70     Lagrange basis
+ *   CEED_BK/include/kernels/BK5/templated_cuda_kernels.cuh:50-122 BK5 E-vector
+ *   bakeoff_problems_dealii/include/bk3_kokkos_kernel.h:129-151  gather + mask
+ *   bakeoff_problems_dealii/include/bk3_kokkos_kernel.h:406-426  atomic scatter
+ *   bakeoff_problems_dealii/include/portable_laplace_operator_bk35.h:123-167
+ *       vmult: dst = 0, cell loop, copy_constrained_values
+ *   bakeoff_problems_dealii/include/portable_laplace_operator_bk35.h:229-292
+ *       G = JxW * Jinv Jinv^T (index order as in the deal.II-kernel variant
+ *       portable_laplace_operator.h:227-255: grad_phys = Jinv^T grad_ref)
+ *   bp5_kokkos/benchmark.cc:218-251  diagonal + inverse with the d<=0 guard
+ *   bp5_kokkos/benchmark.cc:355-378, scaling_bp35_kokkos_kernel/program.cc:
+ *       263-287  SolverCG + ReductionControl (deal.II, third party, >= 9.7.0;
+ *       the published conjugate-gradient algorithm is restated here)
+ */
+#include "mf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* 1D bases                                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* Legendre P_{N-1}(x) and P_N(x) by the three-term recurrence. */
+static void legendre_pair(int N, double x, double *pm1, double *pN) {
+  double p0 = 1.0, p1 = x;
+  if (N == 0) { *pm1 = 0.0; *pN = 1.0; return; }
+  for (int k = 2; k <= N; ++k) {
+    double pk = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+    p0 = p1;
+    p1 = pk;
+  }
+  *pm1 = p0;
+  *pN = p1;
+}
+
+/* Gauss-Lobatto-Legendre nodes/weights on [-1,1], ascending.  Newton's
+   method on x P_N(x) - P_{N-1}(x) (whose interior zeros are those of P_N'),
+   started at the Chebyshev-Gauss-Lobatto points; w = 2 / (N (N+1) P_N^2).
+   (Published method: Canuto et al., "Spectral Methods", sec. 2.3; the
+   iteration as in G. von Winckel's lglnodes.)  Symmetrised afterwards. */
+void orc_gll(int n, double *x, double *w) {
+  if (n == 1) { x[0] = 0.0; w[0] = 2.0; return; }
+  const int N = n - 1;
+  for (int i = 0; i < n; ++i) {
+    double xi = -cos(M_PI * i / N);
+    for (int it = 0; it < 200; ++it) {
+      double pm1, pN;
+      legendre_pair(N, xi, &pm1, &pN);
+      double dx = (xi * pN - pm1) / ((N + 1.0) * pN);
+      xi -= dx;
+      if (fabs(dx) < 1e-17) break;
+    }
+    double pm1, pN;
+    legendre_pair(N, xi, &pm1, &pN);
+    x[i] = xi;
+    w[i] = 2.0 / (N * (N + 1.0) * pN * pN);
+  }
+  for (int i = 0; i < n / 2; ++i) {
+    double v = 0.5 * (x[N - i] - x[i]);
+    double ww = 0.5 * (w[N - i] + w[i]);
+    x[i] = -v; x[N - i] = v;
+    w[i] = ww; w[N - i] = ww;
+  }
+  if (n % 2) x[n / 2] = 0.0;
+  x[0] = -1.0; x[N] = 1.0;
+}
+
+/* Gauss-Legendre nodes/weights on [-1,1], ascending (Newton on P_n). */
+void orc_gauss(int n, double *x, double *w) {
+  for (int i = 0; i < n; ++i) {
+    double xi = -cos(M_PI * (i + 0.75) / (n + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 200; ++it) {
+      double pm1, pn;
+      legendre_pair(n, xi, &pm1, &pn);
+      dp = n * (xi * pn - pm1) / (xi * xi - 1.0);
+      double dx = pn / dp;
+      xi -= dx;
+      if (fabs(dx) < 1e-17) break;
+    }
+    double pm1, pn;
+    legendre_pair(n, xi, &pm1, &pn);
+    dp = n * (xi * pn - pm1) / (xi * xi - 1.0);
+    x[i] = xi;
+    w[i] = 2.0 / ((1.0 - xi * xi) * dp * dp);
+  }
+  for (int i = 0; i < n / 2; ++i) {
+    double v = 0.5 * (x[n - 1 - i] - x[i]);
+    double ww = 0.5 * (w[n - 1 - i] + w[i]);
+    x[i] = -v; x[n - 1 - i] = v;
+    w[i] = ww; w[n - 1 - i] = ww;
+  }
+  if (n % 2) x[n / 2] = 0.0;
+}
+
+/* l_j(x) = prod_{m != j} (x - x_m) / prod_{m != j} (x_j - x_m)
+   (sum_factorization/include/math/lagrange_basis.hpp:10-42) */
+double orc_lagrange_value(int n, const double *nodes, int j, double x) {
+  double num = 1.0, den = 1.0;
+  for (int m = 0; m < n; ++m) {
+    if (m == j) continue;
+    num *= (x - nodes[m]);
+    den *= (nodes[j] - nodes[m]);
+  }
+  return num / den;
+}
+
+/* l_j'(x) = sum_{i != j} 1/(x_j - x_i) prod_{m != i,j} (x - x_m)/(x_j - x_m)
+   (sum_factorization/include/math/lagrange_basis.hpp:44-65) */
+double orc_lagrange_derivative(int n, const double *nodes, int j, double x) {
+  double sum = 0.0;
+  for (int i = 0; i < n; ++i) {
+    if (i == j) continue;
+    double prod = 1.0;
+    for (int m = 0; m < n; ++m)
+      if (m != i && m != j) prod *= (x - nodes[m]) / (nodes[j] - nodes[m]);
+    sum += (1.0 / (nodes[j] - nodes[i])) * prod;
+  }
+  return sum;
+}
+
+/* D[point*n + basis] = l_basis'(x_point)  (CEED_BK dbasis layout,
+   CEED_BK/include/kernels/BK5/templated_cuda_kernels.cuh:55-58,85-86) */
+void orc_derivative_matrix(int n, const double *nodes, double *D) {
+  for (int q = 0; q < n; ++q)
+    for (int b = 0; b < n; ++b) D[q * n + b] = orc_lagrange_derivative(n, nodes, b, nodes[q]);
+}
+
+/* B[t*n_from + f] = l_f(pts_to[t]) */
+void orc_interpolation_matrix(int n_from, const double *nodes_from, int n_to,
+                              const double *pts_to, double *B) {
+  for (int t = 0; t < n_to; ++t)
+    for (int f = 0; f < n_from; ++f)
+      B[t * n_from + f] = orc_lagrange_value(n_from, nodes_from, f, pts_to[t]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* structured box mesh                                                       */
+/* ------------------------------------------------------------------------ */
+
+int64_t orc_box_n_dofs(const orc_box *b) {
+  const int64_t p = b->degree;
+  return (p * b->nx + 1) * (p * b->ny + 1) * (p * b->nz + 1);
+}
+
+int64_t orc_box_n_cells(const orc_box *b) {
+  return (int64_t)b->nx * b->ny * b->nz;
+}
+
+void orc_box_cell_nodes(const orc_box *b, int64_t cell, double *xyz) {
+  const int n = b->degree + 1;
+  double xg[16], wg[16];
+  orc_gll(n, xg, wg);
+  const int64_t cx = cell % b->nx, cy = (cell / b->nx) % b->ny, cz = cell / ((int64_t)b->nx * b->ny);
+  const double hx = (b->hi[0] - b->lo[0]) / b->nx;
+  const double hy = (b->hi[1] - b->lo[1]) / b->ny;
+  const double hz = (b->hi[2] - b->lo[2]) / b->nz;
+  const double two_pi = 2.0 * M_PI;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < n; ++k) {
+        const double X = b->lo[0] + ((double)cx + 0.5 * (xg[k] + 1.0)) * hx;
+        const double Y = b->lo[1] + ((double)cy + 0.5 * (xg[j] + 1.0)) * hy;
+        const double Z = b->lo[2] + ((double)cz + 0.5 * (xg[i] + 1.0)) * hz;
+        const double s = b->amplitude * sin(two_pi * X) * sin(two_pi * Y) * sin(two_pi * Z);
+        double *o = xyz + 3 * (i * n * n + j * n + k);
+        o[0] = X + s;
+        o[1] = Y + s;
+        o[2] = Z + s;
+      }
+}
+
+int64_t orc_box_dof_map(const orc_box *b, uint32_t *map, int64_t *constrained) {
+  const int p = b->degree, n = p + 1;
+  const int64_t Nx = (int64_t)p * b->nx + 1, Ny = (int64_t)p * b->ny + 1, Nz = (int64_t)p * b->nz + 1;
+  const int64_t n_cells = orc_box_n_cells(b);
+  if (map) {
+    for (int64_t e = 0; e < n_cells; ++e) {
+      const int64_t cx = e % b->nx, cy = (e / b->nx) % b->ny, cz = e / ((int64_t)b->nx * b->ny);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+          for (int k = 0; k < n; ++k) {
+            const int64_t gx = cx * p + k, gy = cy * p + j, gz = cz * p + i;
+            const int bnd = gx == 0 || gx == Nx - 1 || gy == 0 || gy == Ny - 1 || gz == 0 || gz == Nz - 1;
+            map[e * n * n * n + i * n * n + j * n + k] =
+                bnd ? ORC_INVALID_DOF : (uint32_t)(gx + Nx * (gy + Ny * gz));
+          }
+    }
+  }
+  int64_t nc = 0;
+  for (int64_t gz = 0; gz < Nz; ++gz)
+    for (int64_t gy = 0; gy < Ny; ++gy)
+      for (int64_t gx = 0; gx < Nx; ++gx) {
+        const int bnd = gx == 0 || gx == Nx - 1 || gy == 0 || gy == Ny - 1 || gz == 0 || gz == Nz - 1;
+        if (bnd) {
+          if (constrained) constrained[nc] = gx + Nx * (gy + Ny * gz);
+          ++nc;
+        }
+      }
+  return nc;
+}
+
+/* G_ab = JxW sum_d Jinv[a][d] Jinv[b][d], J[d][a] = dx_d/dxi_a, JxW = |det J| w.
+   Returns 1 if the cell is degenerate or folded (det changes sign / is 0). */
+int orc_cell_geometry(int n, const double *D, const double *w, const double *xyz, double *Gc) {
+  const int nq = n * n * n;
+  int bad = 0, sign0 = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < n; ++k) {
+        double J[3][3];
+        for (int d = 0; d < 3; ++d) {
+          double jr = 0, js = 0, jt = 0;
+          for (int m = 0; m < n; ++m) {
+            jr += D[i * n + m] * xyz[3 * (m * n * n + j * n + k) + d];
+            js += D[j * n + m] * xyz[3 * (i * n * n + m * n + k) + d];
+            jt += D[k * n + m] * xyz[3 * (i * n * n + j * n + m) + d];
+          }
+          J[d][0] = jr; J[d][1] = js; J[d][2] = jt;
+        }
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const int sg = det > 0 ? 1 : (det < 0 ? -1 : 0);
+        if (sg == 0) bad = 1;
+        if (sign0 == 0) sign0 = sg; else if (sg != sign0) bad = 1;
+        /* Jinv[a][d] = cofactor(d,a) / det */
+        double Ji[3][3];
+        Ji[0][0] = c00 / det;
+        Ji[1][0] = c01 / det;
+        Ji[2][0] = c02 / det;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        const double jxw = fabs(det) * w[i] * w[j] * w[k];
+        const int q = i * n * n + j * n + k;
+        int c = 0;
+        for (int a = 0; a < 3; ++a)
+          for (int bb = a; bb < 3; ++bb) {
+            double s = 0;
+            for (int d = 0; d < 3; ++d) s += Ji[a][d] * Ji[bb][d];
+            Gc[c * nq + q] = jxw * s;
+            ++c;
+          }
+      }
+  return bad;
+}
+
+int64_t orc_box_geometry(const orc_box *b, double *G) {
+  const int n = b->degree + 1, nq = n * n * n;
+  double xg[16], wg[16], D[256];
+  orc_gll(n, xg, wg);
+  orc_derivative_matrix(n, xg, D);
+  const int64_t n_cells = orc_box_n_cells(b);
+  int64_t bad = 0;
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *xyz = (double *)malloc(sizeof(double) * 3 * nq);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < n_cells; ++e) {
+      orc_box_cell_nodes(b, e, xyz);
+      bad += orc_cell_geometry(n, D, wg, xyz, G + e * 6 * nq);
+    }
+    free(xyz);
+  }
+  return bad;
+}
+
+/* ------------------------------------------------------------------------ */
+/* operator                                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* One element: out = D^T G D in  (CEED_BK/include/kernels/BK5/
+   templated_cuda_kernels.cuh:50-122, with G[6][n^3] read per component). */
+static void bk5_element(int n, const double *D, const double *G, const double *u, double *out,
+                        double *vr, double *vs, double *vt) {
+  const int nq = n * n * n;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < n; ++k) {
+        const int q = i * n * n + j * n + k;
+        double qr = 0, qs = 0, qt = 0;
+        for (int m = 0; m < n; ++m) {
+          qr += D[i * n + m] * u[m * n * n + j * n + k];
+          qs += D[j * n + m] * u[i * n * n + m * n + k];
+          qt += D[k * n + m] * u[i * n * n + j * n + m];
+        }
+        const double grr = G[0 * nq + q], grs = G[1 * nq + q], grt = G[2 * nq + q];
+        const double gss = G[3 * nq + q], gst = G[4 * nq + q], gtt = G[5 * nq + q];
+        vr[q] = grr * qr + grs * qs + grt * qt;
+        vs[q] = grs * qr + gss * qs + gst * qt;
+        vt[q] = grt * qr + gst * qs + gtt * qt;
+      }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < n; ++k) {
+        double t = 0;
+        for (int m = 0; m < n; ++m) t += D[m * n + i] * vr[m * n * n + j * n + k];
+        for (int m = 0; m < n; ++m) t += D[m * n + j] * vs[i * n * n + m * n + k];
+        for (int m = 0; m < n; ++m) t += D[m * n + k] * vt[i * n * n + j * n + m];
+        out[i * n * n + j * n + k] = t;
+      }
+}
+
+void orc_bk5_evector(int n, int64_t nelmt, const double *D, const double *G,
+                     const double *in, double *out) {
+  const int nq = n * n * n;
+#pragma omp parallel
+  {
+    double *scratch = (double *)malloc(sizeof(double) * 3 * nq);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < nelmt; ++e)
+      bk5_element(n, D, G + e * 6 * nq, in + e * nq, out + e * nq, scratch, scratch + nq,
+                  scratch + 2 * nq);
+    free(scratch);
+  }
+}
+
+void orc_bk5_apply(int n, int64_t n_cells, const uint32_t *map, const double *D,
+                   const double *G, int64_t n_dofs, int64_t n_constrained,
+                   const int64_t *constrained, const double *src, double *dst) {
+  const int nq = n * n * n;
+  memset(dst, 0, sizeof(double) * n_dofs);
+#pragma omp parallel
+  {
+    double *scratch = (double *)malloc(sizeof(double) * 5 * nq);
+    double *u = scratch, *y = scratch + nq;
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < n_cells; ++e) {
+      const uint32_t *me = map + e * nq;
+      for (int l = 0; l < nq; ++l) u[l] = me[l] == ORC_INVALID_DOF ? 0.0 : src[me[l]];
+      bk5_element(n, D, G + e * 6 * nq, u, y, scratch + 2 * nq, scratch + 3 * nq, scratch + 4 * nq);
+      for (int l = 0; l < nq; ++l)
+        if (me[l] != ORC_INVALID_DOF) {
+#pragma omp atomic
+          dst[me[l]] += y[l];
+        }
+    }
+    free(scratch);
+  }
+  for (int64_t c = 0; c < n_constrained; ++c) dst[constrained[c]] = src[constrained[c]];
+}
+
+void orc_bk5_diagonal(int n, int64_t n_cells, const uint32_t *map, const double *D,
+                      const double *G, int64_t n_dofs, int64_t n_constrained,
+                      const int64_t *constrained, double *diag) {
+  const int nq = n * n * n;
+  memset(diag, 0, sizeof(double) * n_dofs);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < n_cells; ++e) {
+    const uint32_t *me = map + e * nq;
+    const double *Ge = G + e * 6 * nq;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        for (int k = 0; k < n; ++k) {
+          const int q = i * n * n + j * n + k;
+          if (me[q] == ORC_INVALID_DOF) continue;
+          double d = 0;
+          for (int a = 0; a < n; ++a) d += Ge[0 * nq + a * n * n + j * n + k] * D[a * n + i] * D[a * n + i];
+          for (int a = 0; a < n; ++a) d += Ge[3 * nq + i * n * n + a * n + k] * D[a * n + j] * D[a * n + j];
+          for (int a = 0; a < n; ++a) d += Ge[5 * nq + i * n * n + j * n + a] * D[a * n + k] * D[a * n + k];
+          d += 2.0 * Ge[1 * nq + q] * D[i * n + i] * D[j * n + j];
+          d += 2.0 * Ge[2 * nq + q] * D[i * n + i] * D[k * n + k];
+          d += 2.0 * Ge[4 * nq + q] * D[j * n + j] * D[k * n + k];
+#pragma omp atomic
+          diag[me[q]] += d;
+        }
+  }
+  for (int64_t c = 0; c < n_constrained; ++c) diag[constrained[c]] = 1.0;
+}
+
+/* bp5_kokkos/benchmark.cc:240-250 */
+void orc_invert_diagonal(int64_t n, double *d) {
+  for (int64_t i = 0; i < n; ++i) d[i] = d[i] > 0 ? 1.0 / d[i] : 1.0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* MT19937-64 (Matsumoto & Nishimura, 2000/2004 published algorithm)        */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  uint64_t mt[312];
+  int idx;
+} mt64;
+
+static void mt64_seed(mt64 *s, uint64_t seed) {
+  s->mt[0] = seed;
+  for (int i = 1; i < 312; ++i)
+    s->mt[i] = 6364136223846793005ULL * (s->mt[i - 1] ^ (s->mt[i - 1] >> 62)) + (uint64_t)i;
+  s->idx = 312;
+}
+
+static uint64_t mt64_next(mt64 *s) {
+  const uint64_t UM = 0xFFFFFFFF80000000ULL, LM = 0x7FFFFFFFULL;
+  if (s->idx >= 312) {
+    for (int i = 0; i < 312; ++i) {
+      uint64_t x = (s->mt[i] & UM) | (s->mt[(i + 1) % 312] & LM);
+      uint64_t xa = x >> 1;
+      if (x & 1ULL) xa ^= 0xB5026F5AA96619E9ULL;
+      s->mt[i] = s->mt[(i + 156) % 312] ^ xa;
+    }
+    s->idx = 0;
+  }
+  uint64_t y = s->mt[s->idx++];
+  y ^= (y >> 29) & 0x5555555555555555ULL;
+  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+  y ^= (y >> 43);
+  return y;
+}
+
+uint64_t orc_mt19937_64_nth(uint64_t seed, int64_t nth) {
+  mt64 s;
+  mt64_seed(&s, seed);
+  uint64_t v = 0;
+  for (int64_t i = 0; i < nth; ++i) v = mt64_next(&s);
+  return v;
+}
+
+/* b_i = 2 * ((x >> 11) * 2^-53) - 1 for every DoF in index order, then 0 on
+   the constrained DoFs. */
+void orc_rhs_uniform(uint64_t seed, int64_t n_dofs, int64_t n_constrained,
+                     const int64_t *constrained, double *b) {
+  mt64 s;
+  mt64_seed(&s, seed);
+  for (int64_t i = 0; i < n_dofs; ++i) {
+    const double u = (double)(mt64_next(&s) >> 11) * (1.0 / 9007199254740992.0);
+    b[i] = 2.0 * u - 1.0;
+  }
+  for (int64_t c = 0; c < n_constrained; ++c) b[constrained[c]] = 0.0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* conjugate gradients (deal.II SolverCG + ReductionControl semantics)       */
+/* ------------------------------------------------------------------------ */
+static double dot(int64_t n, const double *a, const double *b) {
+  double s = 0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+orc_solve_info orc_cg_solve(int n, int64_t n_cells, const uint32_t *map, const double *D,
+                            const double *G, int64_t N, int64_t n_constrained,
+                            const int64_t *constrained, const double *diag_inv,
+                            const double *b, double *x, orc_reduction_control ctl) {
+  orc_solve_info info = {0, 0.0, 0.0, 0};
+  double *r = (double *)malloc(sizeof(double) * N);
+  double *z = (double *)malloc(sizeof(double) * N);
+  double *p = (double *)malloc(sizeof(double) * N);
+  double *v = (double *)malloc(sizeof(double) * N);
+
+  /* r = b - A x */
+  orc_bk5_apply(n, n_cells, map, D, G, N, n_constrained, constrained, x, v);
+  for (int64_t i = 0; i < N; ++i) r[i] = b[i] - v[i];
+  double res = sqrt(dot(N, r, r));
+  info.initial = res;
+  info.last = res;
+  /* ReductionControl::check at step 0: tol_eff = max(tol, reduce * r0) */
+  const double tol_eff = fmax(ctl.tol, ctl.reduce * res);
+  if (res <= tol_eff) { info.converged = 1; goto done; }
+  if (isnan(res)) goto done;
+
+  for (int64_t i = 0; i < N; ++i) z[i] = diag_inv ? diag_inv[i] * r[i] : r[i];
+  memcpy(p, z, sizeof(double) * N);
+  double rz = dot(N, r, z);
+
+  for (int it = 1;; ++it) {
+    orc_bk5_apply(n, n_cells, map, D, G, N, n_constrained, constrained, p, v);
+    const double alpha = rz / dot(N, p, v);
+    for (int64_t i = 0; i < N; ++i) {
+      x[i] += alpha * p[i];
+      r[i] -= alpha * v[i];
+    }
+    res = sqrt(dot(N, r, r));
+    info.steps = it;
+    info.last = res;
+    if (res <= tol_eff) { info.converged = 1; break; }
+    if (it >= ctl.max_steps || isnan(res)) break;
+    for (int64_t i = 0; i < N; ++i) z[i] = diag_inv ? diag_inv[i] * r[i] : r[i];
+    const double rz_new = dot(N, r, z);
+    const double beta = rz_new / rz;
+    rz = rz_new;
+    for (int64_t i = 0; i < N; ++i) p[i] = z[i] + beta * p[i];
+  }
+done:
+  free(r); free(z); free(p); free(v);
+  return info;
+}

@@ -1,0 +1,62 @@
+"""The C ABI library loads and exports every entry point include/mfgb.h declares
+(no compute call: runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(mfgb_\w+)\s*\(", text, re.M))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def libmfgb():
+    from benchmarks_gb300 import build
+    if not os.path.exists(build.LIB):
+        build.build()
+    return ctypes.CDLL(build.LIB)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for need in ("mfgb_vmult", "mfgb_bk5_lvector", "mfgb_bk5_evector", "mfgb_cg_solve",
+                 "mfgb_compute_diagonal", "mfgb_operator_create_box"):
+        assert need in syms
+
+
+def test_library_exports_every_declared_symbol(libmfgb):
+    missing = [s for s in declared_symbols() if not hasattr(libmfgb, s)]
+    assert not missing, missing
+
+
+def test_status_strings(libmfgb):
+    libmfgb.mfgb_status_string.restype = ctypes.c_char_p
+    assert libmfgb.mfgb_status_string(0) == b"ok"
+    assert libmfgb.mfgb_status_string(2) == b"out of device memory"
+    libmfgb.mfgb_version.restype = ctypes.c_int
+    assert libmfgb.mfgb_version() >= 1
+
+
+def test_invalid_arguments_are_rejected_without_gpu(libmfgb):
+    """Argument validation happens before any CUDA call."""
+    import benchmarks_gb300 as mf
+    from benchmarks_gb300 import _abi
+    L = mf.lib()
+    op = ctypes.c_void_p()
+    bad = _abi.BoxDesc(2, 2, 2, 9, (ctypes.c_double * 3)(0, 0, 0), (ctypes.c_double * 3)(1, 1, 1), 0.0)
+    assert L.mfgb_operator_create_box(ctypes.byref(bad), ctypes.byref(op)) == _abi.ERR_INVALID_ARG
+    assert b"degree" in L.mfgb_last_error()
+    assert L.mfgb_bk5_evector(0, 1, None, None, None, None, 0, None) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_vmult(None, None, None, 0, None) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_cg_solve(None, None, None, None, None, None, None) == _abi.ERR_INVALID_ARG
+    with pytest.raises(ValueError):
+        mf._arith("fp16")
