@@ -71,6 +71,8 @@ def lib():
         "mfgb_rhs_uniform": ([P, ctypes.c_uint64, P, P], I32),
         "mfgb_cg_solve": ([P, P, P, P, ctypes.POINTER(CgControl), ctypes.POINTER(SolveInfo), P],
                           I32),
+        "mfgb_cg_solve_noalloc": ([P, P, P, P, ctypes.POINTER(CgControl),
+                                   ctypes.POINTER(SolveInfo), P], I32),
         "mfgb_dot": ([I64, P, P, ctypes.POINTER(D), P], I32),
     }
     for name, (args, res) in sigs.items():

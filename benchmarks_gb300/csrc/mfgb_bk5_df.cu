@@ -15,4 +15,10 @@ cudaError_t bk5_df_g64(int N, int64_t n_cells, const uint32_t *map, const double
     return bk5_dispatch<ArithDFG64, true, false>(N, n_cells, map, G, src, dst, D, nullptr, nullptr, s);
   return bk5_dispatch<ArithDFG64, false, false>(N, n_cells, map, G, src, dst, D, nullptr, nullptr, s);
 }
+cudaError_t bk5_df_g64_energy(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                              const double *src, double *dst, const double *D, double *partials,
+                              int *grid, cudaStream_t s, const int *done) {
+  return bk5_dispatch<ArithDFG64, false, true>(N, n_cells, map, G, src, dst, D, partials, grid, s,
+                                               done);
+}
 }  // namespace mfgb

@@ -381,3 +381,193 @@ extern "C" mfgb_status mfgb_cg_solve(const mfgb_operator *cop, const double *d_b
   set_error("mfgb_cg_solve: max_steps reached");
   return MFGB_ERR_NOT_CONVERGED;
 }
+
+// ---------------------------------------------------------------------------
+// Conjugate gradients without any device allocation.
+//
+// For callers that must not allocate device memory while solving: code that
+// runs under an external memory budget or a pool it does not own (a host
+// application whose allocator reserved the device, a solver called from inside
+// another library's time step), and code paths where a cudaMalloc could block
+// or fail at a bad moment.  The work vectors, the reduction partials and the
+// device scalars live in one file-scope __device__ array, sized for at most
+// MFGB_CG_NOALLOC_MAX_DOFS unknowns (about 25 MB).  Every GPU that loads this
+// library keeps that array until the process exits.  Every call shares it and
+// it keeps the previous call's contents, so everything the solve reads is
+// initialised by the solve itself; calls whose work overlaps on the GPU (two
+// streams, two host threads on one device) race on it and must be serialised
+// by the caller.  The first call on a device looks up the array's device
+// address (cudaGetSymbolAddress, once per device); make that first call before
+// any stream capture.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace mfgb {
+
+constexpr int64_t NOALLOC_PAP_CAP = 152 * 64 + 1;
+constexpr int64_t NOALLOC_VEC_PART = 2 * VEC_BLOCKS + 8;
+constexpr int64_t NOALLOC_SCALARS = 32;  // doubles reserved for CgScalars
+static_assert(sizeof(CgScalars) <= NOALLOC_SCALARS * sizeof(double), "scalar slot too small");
+constexpr int64_t NOALLOC_DOUBLES =
+    3 * (int64_t)MFGB_CG_NOALLOC_MAX_DOFS + NOALLOC_PAP_CAP + NOALLOC_VEC_PART + NOALLOC_SCALARS;
+
+static __device__ __align__(256) double g_cg_noalloc_scratch[NOALLOC_DOUBLES];
+
+static std::mutex g_noalloc_mutex;
+static double *g_noalloc_ptr[64] = {nullptr};
+
+// device address of the scratch array on the current device (looked up once)
+static mfgb_status noalloc_scratch(double **out) {
+  int dev = 0;
+  mfgb_status st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+  if (st) return st;
+  if (dev < 0 || dev >= 64) {
+    set_error("mfgb_cg_solve_noalloc: device ordinal above 63");
+    return MFGB_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    st = cuda_status(cudaGetSymbolAddress(&p, g_cg_noalloc_scratch), "cudaGetSymbolAddress");
+    if (st) return st;
+    g_noalloc_ptr[dev] = (double *)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MFGB_OK;
+}
+
+// vmult (partials == nullptr) or accumulate-with-energy, never allocating:
+// double-float arithmetic uses the operator's split copy of G when an earlier
+// call created it, and otherwise splits the FP64 geometric factors on load.
+static mfgb_status noalloc_apply(const mfgb_operator *op, double *dst, const double *src, int arith,
+                                 double *partials, int *grid, cudaStream_t s, const int *done) {
+  mfgb_status st;
+  if (!partials && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
+                                     "dst = 0")))
+    return st;
+  cudaError_t e;
+  if (arith == MFGB_ARITH_FP64)
+    e = bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s, done);
+  else if (op->d_Gdf)
+    e = bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s, done);
+  else if (partials)
+    e = bk5_df_g64_energy(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid,
+                          s, done);
+  else
+    e = bk5_df_g64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, s);
+  if ((st = cuda_status(e, "bk5 kernel"))) return st;
+  if (!partials)
+    return cuda_status(copy_constrained(op->n_constrained, op->d_constrained, src, dst, s),
+                       "constrained rows");
+  return MFGB_OK;
+}
+
+}  // namespace mfgb
+
+extern "C" mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const double *d_b,
+                                             double *d_x, const double *d_inv_diag,
+                                             const mfgb_cg_control *ctl, mfgb_solve_info *info,
+                                             void *stream) {
+  if (!op || !d_b || !d_x || !ctl || !info || ctl->max_steps < 0) {
+    set_error("mfgb_cg_solve_noalloc: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if (ctl->arith != MFGB_ARITH_FP64 && ctl->arith != MFGB_ARITH_FP64_DF) {
+    set_error("mfgb_cg_solve_noalloc: unknown arith");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  const int64_t n = op->n_dofs;
+  if (n > (int64_t)MFGB_CG_NOALLOC_MAX_DOFS) {
+    set_error("mfgb_cg_solve_noalloc: " + std::to_string(n) + " DoFs exceed the fixed scratch of " +
+              std::to_string((long long)MFGB_CG_NOALLOC_MAX_DOFS) +
+              " DoFs; use mfgb_cg_solve for larger problems");
+    return MFGB_ERR_UNSUPPORTED;
+  }
+  double *scratch = nullptr;
+  mfgb_status st = noalloc_scratch(&scratch);
+  if (st) return st;
+  double *r = scratch;
+  double *p = r + MFGB_CG_NOALLOC_MAX_DOFS;
+  double *v = p + MFGB_CG_NOALLOC_MAX_DOFS;
+  double *pap_part = v + MFGB_CG_NOALLOC_MAX_DOFS;
+  double *vec_part = pap_part + NOALLOC_PAP_CAP;
+  CgScalars *sc = (CgScalars *)(vec_part + NOALLOC_VEC_PART);
+  cudaStream_t s = (cudaStream_t)stream;
+  const double *dinv = d_inv_diag;
+
+  // r0 = b - A x0, p0 = z0
+  if ((st = noalloc_apply(op, v, d_x, ctl->arith, nullptr, nullptr, s, nullptr))) return st;
+  cg_init_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_b, v, r, p, dinv, vec_part);
+  finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(vec_part, VEC_BLOCKS, 2, vec_part + 2 * VEC_BLOCKS);
+  finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(vec_part + 1, VEC_BLOCKS, 2,
+                                              vec_part + 2 * VEC_BLOCKS + 1);
+  double h2[2];
+  if ((st = cuda_status(cudaMemcpyAsync(h2, vec_part + 2 * VEC_BLOCKS, 2 * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s),
+                        "cg init copy")) ||
+      (st = cuda_status(cudaStreamSynchronize(s), "cg init")))
+    return st;
+  const double res0 = std::sqrt(h2[0]);
+  info->initial = res0;
+  info->last = res0;
+  info->steps = 0;
+  info->converged = 0;
+  const double tol_eff = std::fmax(ctl->tol, ctl->reduce * res0);
+  if (res0 <= tol_eff) {
+    info->converged = 1;
+    return MFGB_OK;
+  }
+  if (std::isnan(res0)) {
+    set_error("mfgb_cg_solve_noalloc: initial residual is NaN");
+    return MFGB_ERR_NONFINITE;
+  }
+  if (ctl->max_steps == 0) return MFGB_ERR_NOT_CONVERGED;
+
+  CgScalars hsc{};
+  hsc.rz[0] = h2[1];
+  hsc.res[0] = res0;
+  hsc.its[0] = 0;
+  hsc.tol_eff = tol_eff;
+  hsc.max_steps = ctl->max_steps;
+  hsc.done = 0;
+  if ((st = cuda_status(cudaMemcpyAsync(sc, &hsc, sizeof(hsc), cudaMemcpyHostToDevice, s),
+                        "cg scalars")) ||
+      (st = cuda_status(cudaMemsetAsync(v, 0, sizeof(double) * n, s), "v = 0")))
+    return st;
+
+  const int K = 16;  // iterations between host checks of the done flag
+  CgScalars out{};
+  for (;;) {
+    for (int k = 0; k < K; ++k) {
+      const int parity = k & 1;
+      int grid = 0;
+      if ((st = noalloc_apply(op, v, p, ctl->arith, pap_part, &grid, s, &sc->done))) return st;
+      if (grid + 1 > NOALLOC_PAP_CAP) {
+        set_error("mfgb_cg_solve_noalloc: partials slot too small");
+        return MFGB_ERR_UNSUPPORTED;
+      }
+      cg_constrained_kernel<<<1, VEC_THREADS, 0, s>>>(op->n_constrained, op->d_constrained, p, v,
+                                                       pap_part + grid, sc);
+      cg_update_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_x, r, p, v, dinv, pap_part,
+                                                          grid + 1, vec_part, sc, parity);
+      cg_direction_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, r, p, v, dinv, vec_part,
+                                                             VEC_BLOCKS, sc, parity);
+    }
+    if ((st = cuda_status(cudaGetLastError(), "cg iterations")) ||
+        (st = cuda_status(cudaMemcpyAsync(&out, sc, sizeof(out), cudaMemcpyDeviceToHost, s),
+                          "cg scalars copy")) ||
+        (st = cuda_status(cudaStreamSynchronize(s), "cg iterations")))
+      return st;
+    if (out.done) break;
+  }
+  info->steps = out.final_its;
+  info->last = out.final_res;
+  info->converged = out.done == 1;
+  if (out.done == 1) return MFGB_OK;
+  if (std::isnan(out.final_res)) {
+    set_error("mfgb_cg_solve_noalloc: residual became NaN");
+    return MFGB_ERR_NONFINITE;
+  }
+  set_error("mfgb_cg_solve_noalloc: max_steps reached");
+  return MFGB_ERR_NOT_CONVERGED;
+}

@@ -148,6 +148,22 @@ mfgb_status mfgb_cg_solve(const mfgb_operator *op, const double *d_b, double *d_
                           const double *d_inv_diag, const mfgb_cg_control *ctl,
                           mfgb_solve_info *info, void *stream);
 
+/* Same solve without allocating any device memory (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc during a solve -- an
+ * application whose own allocator owns the device memory, or a solver called
+ * from inside another library's time loop -- the work vectors, reduction
+ * partials and scalars live in a fixed file-scope device array sized for at
+ * most MFGB_CG_NOALLOC_MAX_DOFS unknowns (about 25 MB, held on every GPU that
+ * loads the library until the process exits).  Larger operators are rejected
+ * with MFGB_ERR_UNSUPPORTED.  All calls share that array: calls whose work
+ * overlaps on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture. */
+#define MFGB_CG_NOALLOC_MAX_DOFS 1048576
+mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const double *d_b, double *d_x,
+                                  const double *d_inv_diag, const mfgb_cg_control *ctl,
+                                  mfgb_solve_info *info, void *stream);
+
 /* ---- vector kernels used by the solver (exposed for tests) -------------- */
 /* result[0] = sum a_i b_i (deterministic two-stage reduction) */
 mfgb_status mfgb_dot(int64_t n, const double *d_a, const double *d_b, double *h_result,
