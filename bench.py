@@ -136,6 +136,8 @@ class ClockSampler:
 def traffic_from_profile(arith: str):
     """DRAM bytes per launch of the operator kernel from the committed ncu
     summary for this workload (None if not captured)."""
+    if not is_headline():
+        return None
     path = os.path.join(ROOT, "profiles", f"bk5_{arith}_p4_67M.md")
     try:
         with open(path) as f:
@@ -184,12 +186,17 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def is_headline():
+    return (WORKLOAD["nx"], WORKLOAD["ny"], WORKLOAD["nz"], WORKLOAD["degree"]) == (128, 128, 64, 4)
+
+
 def config_dict(args, n_dofs, n_cells):
     w = WORKLOAD
     return {"workload": f"BK5 vmult p={w['degree']} {w['nx']}x{w['ny']}x{w['nz']} cells deformed "
                         f"unit cube (a={w['amplitude']}), {n_dofs} DoFs",
             "degree": w["degree"], "cells": [w["nx"], w["ny"], w["nz"]], "n_dofs": n_dofs,
-            "n_cells": n_cells, "arith": args.arith, "l2": "inputs larger than L2 (no flush)",
+            "n_cells": n_cells, "arith": args.arith, "shape": getattr(args, "shape", "auto"),
+            "l2": "inputs larger than L2 (no flush)",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
 
@@ -205,6 +212,9 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(local)
     L = mf.lib()
     w = WORKLOAD
+    if args.shape != "auto":
+        _abi.check(L.mfgb_set_kernel_shape(mf._arith(args.arith), w["degree"],
+                                           {"column": 0, "point": 1, "tma": 2}[args.shape]))
     A = mf.LaplaceOperator(mf.BoxMesh(w["nx"], w["ny"], w["nz"], degree=w["degree"],
                                       amplitude=w["amplitude"]), arith=args.arith)
     n, n_cells = A.m(), A.n_cells
@@ -246,6 +256,9 @@ def run_ours(args, rank, world):
     barrier(world)
 
     # end to end through the public vmult with pinned host buffers
+    e2e_ms = float("nan")
+    if args.no_e2e:
+        return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk)
     h_src = src.cpu().pin_memory()
     h_dst = torch.empty_like(h_src).pin_memory()
     d_a, d_b = A.initialize_dof_vector(), A.initialize_dof_vector()
@@ -266,7 +279,11 @@ def run_ours(args, rank, world):
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e_steps, world)
     # correctness guard on the timed result
     assert torch.equal(h_dst.cuda(), d_b)
+    return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk)
 
+
+def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk):
+    w = WORKLOAD
     if rank != 0:
         return
     ms_per_step = total_ms / args.steps
@@ -279,23 +296,25 @@ def run_ours(args, rank, world):
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         from oracle import oracle
-        sample = oracle.BoxProblem(64, 64, 32, w["degree"], amplitude=w["amplitude"])
+        sample = oracle.BoxProblem(max(1, w["nx"] // 2), max(1, w["ny"] // 2), max(1, w["nz"] // 2),
+                                   w["degree"], amplitude=w["amplitude"])
         s_src = sample.rhs(w["seed"])
         rate, dt = cpu_reference_apply_rate(sample, 5, 1, s_src)
         cpu = {"value": rate, "unit": "GDoF/s", "cores": oracle.num_threads(), "kind": "port",
-               "sample": f"5 vmult of the oracle (OpenMP) on a 64x64x32-cell p=4 mesh of the same "
-                         f"deformed cube, {sample.n_dofs} DoFs"}
+               "sample": f"5 vmult of the oracle (OpenMP) on a {sample.nx}x{sample.ny}x{sample.nz}-"
+                         f"cell p={w['degree']} mesh of the same deformed cube, "
+                         f"{sample.n_dofs} DoFs"}
     line = {
         "metric": METRIC, "value": value, "unit": "GDoF/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": value / 6.83,
+        "vs_baseline": value / 6.83 if is_headline() else None,
         "dtype": "f64",
         "data": "synthetic (seeded U[-1,1] src, deformed unit-cube mesh)",
         "config": config_dict(args, n, n_cells),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": f"bk5_kernel<5,{'ArithDF' if arith else 'ArithF64'}>",
+                     "kernel": f"bk5_kernel<{w['degree'] + 1},{'ArithDF' if arith else 'ArithF64'}>",
                      "kernel_ms": kernel_ms, "bytes_per_launch": bytes_per,
                      "flops_per_launch": flops,
                      "fp64_equiv_tflops": flops / (kernel_ms * 1e-3) / 1e12},
@@ -318,7 +337,17 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--arith", choices=["df", "fp64"], default="df")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
+    ap.add_argument("--cells", type=int, nargs=3, default=None,
+                    help="override the mesh (cells per direction) for sweeps and profiling")
+    ap.add_argument("--degree", type=int, default=None, help="override the degree p")
+    ap.add_argument("--shape", choices=["auto", "column", "point", "tma"], default="auto",
+                    help="operator kernel thread layout (default: the library's table)")
     args = ap.parse_args()
+    if args.cells:
+        WORKLOAD.update(nx=args.cells[0], ny=args.cells[1], nz=args.cells[2])
+    if args.degree:
+        WORKLOAD.update(degree=args.degree)
     rank, world = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)

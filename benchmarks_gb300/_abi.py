@@ -9,7 +9,7 @@ _LIB = None
 
 OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_NOT_CONVERGED = 0, 1, 2, 3
 ERR_TIMEOUT, ERR_NONFINITE, ERR_CUDA, ERR_UNSUPPORTED = 4, 5, 6, 7
-ARITH_FP64, ARITH_FP64_DF = 0, 1
+ARITH_FP64, ARITH_FP64_DF, ARITH_FP32 = 0, 1, 2
 INVALID_DOF = 0xFFFFFFFF
 
 
@@ -56,6 +56,9 @@ def lib():
         "mfgb_status_string": ([I32], ctypes.c_char_p),
         "mfgb_last_error": ([], ctypes.c_char_p),
         "mfgb_version": ([], I32),
+        "mfgb_set_kernel_shape": ([I32, I32, I32], I32),
+        "mfgb_get_kernel_shape": ([I32, I32, ctypes.POINTER(I32)], I32),
+        "mfgb_check_device_errors": ([P], I32),
         "mfgb_operator_create_box": ([ctypes.POINTER(BoxDesc), PP], I32),
         "mfgb_operator_create": ([I32, I64, I64, P, P, I64, P, PP], I32),
         "mfgb_operator_destroy": ([P], I32),

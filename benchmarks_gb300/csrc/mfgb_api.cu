@@ -72,6 +72,37 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
   return MFGB_OK;
 }
 
+// kernel shape per (arithmetic class, N): 0 column, 1 point-per-thread,
+// 2 column with TMA-prefetched geometric factors
+static int g_shape[3][10] = {
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0},  // FP64
+    {2, 2, 2, 2, 2, 2, 2, 2, 2, 2},  // double-float
+    {2, 2, 2, 2, 2, 2, 2, 2, 2, 2},  // FP32
+};
+
+// device-side error word (a TMA wait that ran out of time), one per device
+static __device__ int g_device_error;
+static int *g_device_error_ptr[64] = {nullptr};
+
+int *device_error_flag() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!g_device_error_ptr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    g_device_error_ptr[dev] = (int *)p;
+  }
+  return g_device_error_ptr[dev];
+}
+
+int kernel_shape(int arith_class, int N) {
+  if (arith_class < 0 || arith_class > 2 || N < 0 || N > 9) return 0;
+  return g_shape[arith_class][N];
+}
+
 static void free_operator(mfgb_operator *op) {
   if (!op) return;
   cudaFree(op->d_map);
@@ -113,6 +144,45 @@ const char *mfgb_status_string(mfgb_status s) {
 const char *mfgb_last_error(void) { return g_last_error.c_str(); }
 
 int mfgb_version(void) { return 1; }
+
+mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape) {
+  if (arith < 0 || arith > 2 || degree < 1 || degree > 8 || shape < 0 || shape > 2) {
+    set_error("mfgb_set_kernel_shape: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  g_shape[arith][degree + 1] = shape;
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_check_device_errors(void *stream) {
+  int *flag = device_error_flag();
+  if (!flag) {
+    set_error("mfgb_check_device_errors: no device error word");
+    return MFGB_ERR_CUDA;
+  }
+  int h = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  mfgb_status st;
+  if ((st = cuda_status(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s),
+                        "read device error word")) ||
+      (st = cuda_status(cudaMemsetAsync(flag, 0, sizeof(int), s), "clear device error word")) ||
+      (st = cuda_status(cudaStreamSynchronize(s), "device error word")))
+    return st;
+  if (h) {
+    set_error("a kernel's bulk-copy wait exceeded its time limit; results are invalid");
+    return MFGB_ERR_TIMEOUT;
+  }
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_get_kernel_shape(int arith, int degree, int *shape) {
+  if (arith < 0 || arith > 2 || degree < 1 || degree > 8 || !shape) {
+    set_error("mfgb_get_kernel_shape: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  *shape = g_shape[arith][degree + 1];
+  return MFGB_OK;
+}
 
 mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **out) {
   if (!box || !out) {

@@ -143,3 +143,298 @@ __global__ void __launch_bounds__(E * N * N)
 }
 
 }  // namespace mfgb
+
+namespace mfgb {
+
+// Point-per-thread variant: thread (e, i, j, k) owns one quadrature point of
+// element e.  Registers stay low (the element tiles live in shared memory), so
+// many more warps are resident to hide the gather / G latency; used for the
+// double-float arithmetic whose FP32-pipe work per point is large.
+template <int N, int E, class A, bool EVEC, bool WITH_ENERGY>
+__global__ void __launch_bounds__(E * N * N * N)
+    bk5_pt_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                  const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+                  typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
+                  double *__restrict__ energy_partials, const int *__restrict__ done_flag) {
+  if (done_flag != nullptr && *done_flag) return;  // solver already finished
+  using V = typename A::V;
+  using Acc = typename A::Acc;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  __shared__ V s_D[N2];
+  __shared__ V s_u[E * N3];
+  __shared__ V s_vr[E * N3];
+  __shared__ V s_vs[E * N3];
+  __shared__ V s_vt[E * N3];
+
+  const int tid = threadIdx.x;
+  const int el = tid / N3;
+  const int q = tid - el * N3;
+  const int i = q / N2;
+  const int j = (q / N) % N;
+  const int k = q % N;
+  for (int t = tid; t < N2; t += blockDim.x) s_D[t] = basis.D[t];
+  const V *su = s_u + el * N3;
+  const V *svr = s_vr + el * N3;
+  const V *svs = s_vs + el * N3;
+  const V *svt = s_vt + el * N3;
+
+  double energy = 0.0;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  for (int64_t batch = blockIdx.x; batch < n_batches; batch += gridDim.x) {
+    const int64_t cell = batch * E + el;
+    const bool valid = cell < n_cells;
+    uint32_t idx = MFGB_INVALID_DOF;
+    typename A::VecT raw = 0;
+    if (EVEC) {
+      if (valid) raw = src[cell * N3 + q];
+    } else {
+      idx = valid ? __ldg(map + cell * N3 + q) : MFGB_INVALID_DOF;
+      if (idx != MFGB_INVALID_DOF) raw = __ldg(src + idx);
+    }
+    // geometric factors of this point (issued early, consumed after the gradient)
+    const typename A::GType *Gc = G + (valid ? cell : 0) * 6 * N3 + q;
+    const typename A::GType g0 = __ldg(Gc + 0 * N3), g1 = __ldg(Gc + 1 * N3),
+                            g2 = __ldg(Gc + 2 * N3), g3 = __ldg(Gc + 3 * N3),
+                            g4 = __ldg(Gc + 4 * N3), g5 = __ldg(Gc + 5 * N3);
+    s_u[tid] = A::load_vec(raw);
+    __syncthreads();
+
+    Acc ar, as, at;
+    A::zero(ar);
+    A::zero(as);
+    A::zero(at);
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      A::fma(ar, s_D[i * N + m], su[m * N2 + j * N + k]);
+      A::fma(as, s_D[j * N + m], su[i * N2 + m * N + k]);
+      A::fma(at, s_D[k * N + m], su[i * N2 + j * N + m]);
+    }
+    const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+    const V grr = A::load_g(g0), grs = A::load_g(g1), grt = A::load_g(g2);
+    const V gss = A::load_g(g3), gst = A::load_g(g4), gtt = A::load_g(g5);
+    Acc br, bs, bt;
+    A::zero(br);
+    A::zero(bs);
+    A::zero(bt);
+    A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+    A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+    A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+    s_vr[tid] = A::finish(br);
+    s_vs[tid] = A::finish(bs);
+    s_vt[tid] = A::finish(bt);
+    __syncthreads();
+
+    Acc cr, cs, ct;
+    A::zero(cr);
+    A::zero(cs);
+    A::zero(ct);
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      A::fma(cr, s_D[m * N + i], svr[m * N2 + j * N + k]);
+      A::fma(cs, s_D[m * N + j], svs[i * N2 + m * N + k]);
+      A::fma(ct, s_D[m * N + k], svt[i * N2 + j * N + m]);
+    }
+    A::merge(cr, cs);  // y = cr + cs + ct
+    A::merge(cr, ct);
+    const V y = A::finish(cr);
+    if (EVEC) {
+      if (valid) dst[cell * N3 + q] = A::store_vec(y);
+    } else if (idx != MFGB_INVALID_DOF) {
+      const typename A::VecT yv = A::store_vec(y);
+      atomicAdd(dst + idx, yv);
+      if (WITH_ENERGY) energy = __fma_rn((double)raw, (double)yv, energy);
+    }
+    __syncthreads();  // s_u / s_v* are rewritten by the next batch
+  }
+
+  if (WITH_ENERGY) {
+    __shared__ double s_red[E * N3];
+    s_red[tid] = energy;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int t = 0; t < E * N3; ++t) s += s_red[t];
+      energy_partials[blockIdx.x] = s;
+    }
+  }
+}
+
+}  // namespace mfgb
+
+#include "mfgb_tma.cuh"
+
+namespace mfgb {
+
+template <int N, int E, class A>
+struct TmaLayout {
+  static constexpr int N3 = N * N * N;
+  static constexpr size_t g_bytes = sizeof(typename A::GType) * E * 6 * N3;
+  static constexpr size_t map_bytes = ((size_t)E * N3 * 4 + 15) / 16 * 16;
+  static constexpr size_t work_bytes = 3 * sizeof(typename A::V) * E * N3;
+  static constexpr size_t total = g_bytes + map_bytes + work_bytes + 16;
+  static constexpr bool map_tma = (E * N3 * 4) % 16 == 0;
+};
+
+// Column kernel with the next batch's geometric factors (and dof map, when its
+// tile is 16-byte sized) prefetched into shared memory by one bulk TMA copy
+// per batch, issued as soon as the current batch has consumed its tiles; the
+// copy lands while the CTA integrates and scatters.  L-vector mode only.
+// err_flag (may be null) records a TMA wait that exceeded its time limit.
+template <int N, int E, class A, bool WITH_ENERGY>
+__global__ void __launch_bounds__(E * N * N)
+    bk5_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                   const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+                   typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
+                   double *__restrict__ energy_partials, const int *__restrict__ done_flag,
+                   int *__restrict__ err_flag) {
+  if (done_flag != nullptr && *done_flag) return;
+  using V = typename A::V;
+  using Acc = typename A::Acc;
+  using GT = typename A::GType;
+  using L = TmaLayout<N, E, A>;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  extern __shared__ __align__(128) unsigned char smem[];
+  GT *sG = reinterpret_cast<GT *>(smem);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *s_u = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
+  V *s_vs = s_u + E * N3;
+  V *s_vt = s_vs + E * N3;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+
+  const int tid = threadIdx.x;
+  const int el = tid / N2;
+  const int jk = tid - el * N2;
+  const int j = jk / N;
+  const int k = jk - j * N;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  int64_t batch = blockIdx.x;
+  if (batch >= n_batches) return;  // uniform across the CTA
+
+  V Dj[N], Dk[N], Dtj[N], Dtk[N];
+#pragma unroll
+  for (int m = 0; m < N; ++m) {
+    Dj[m] = basis.D[j * N + m];
+    Dk[m] = basis.D[k * N + m];
+    Dtj[m] = basis.D[m * N + j];
+    Dtk[m] = basis.D[m * N + k];
+  }
+
+  auto issue = [&](int64_t b) {  // one thread
+    const int64_t c0 = b * E;
+    const int cells = (int)min((int64_t)E, n_cells - c0);
+    const uint32_t gb = (uint32_t)(sizeof(GT) * cells * 6 * N3);
+    const bool mt = L::map_tma && ((cells * N3 * 4) % 16 == 0);
+    const uint32_t mb = mt ? (uint32_t)(cells * N3 * 4) : 0u;
+    mbar_arrive_expect_tx(mbar, gb + mb);
+    bulk_g2s(sG, G + c0 * 6 * N3, gb, mbar);
+    if (mt) bulk_g2s(sMap, map + c0 * N3, mb, mbar);
+  };
+
+  if (tid == 0) {
+    mbar_init(mbar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) issue(batch);
+  uint32_t phase = 0;
+  double energy = 0.0;
+
+  for (; batch < n_batches; batch += gridDim.x) {
+    const int64_t c0 = batch * E;
+    const int cells = (int)min((int64_t)E, n_cells - c0);
+    const bool mt = L::map_tma && ((cells * N3 * 4) % 16 == 0);
+    const bool valid = el < cells;
+    const int64_t cell = c0 + el;
+    const bool landed = mbar_wait(mbar, phase);
+    if (__syncthreads_or(!landed)) {
+      if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+      mbar_wait(mbar, phase);  // bounded second wait for the copy still in flight
+      return;
+    }
+    phase ^= 1u;
+
+    V u[N];
+    uint32_t idx[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      idx[i] = valid ? (mt ? sMap[el * N3 + i * N2 + jk] : __ldg(map + cell * N3 + i * N2 + jk))
+                     : MFGB_INVALID_DOF;
+      u[i] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(__ldg(src + idx[i])) : A::zero_v();
+      s_u[el * N3 + i * N2 + jk] = u[i];
+    }
+    __syncthreads();
+
+    V vr[N];
+    const GT *Gc = sG + el * 6 * N3 + jk;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc ar, as, at;
+      A::zero(ar);
+      A::zero(as);
+      A::zero(at);
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        A::fma(ar, basis.D[i * N + m], u[m]);
+        A::fma(as, Dj[m], s_u[el * N3 + i * N2 + m * N + k]);
+        A::fma(at, Dk[m], s_u[el * N3 + i * N2 + j * N + m]);
+      }
+      const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+      V grr = A::zero_v(), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+      if (valid) {
+        grr = A::load_g(Gc[0 * N3 + i * N2]);
+        grs = A::load_g(Gc[1 * N3 + i * N2]);
+        grt = A::load_g(Gc[2 * N3 + i * N2]);
+        gss = A::load_g(Gc[3 * N3 + i * N2]);
+        gst = A::load_g(Gc[4 * N3 + i * N2]);
+        gtt = A::load_g(Gc[5 * N3 + i * N2]);
+      }
+      Acc br, bs, bt;
+      A::zero(br);
+      A::zero(bs);
+      A::zero(bt);
+      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      vr[i] = A::finish(br);
+      s_vs[el * N3 + i * N2 + jk] = A::finish(bs);
+      s_vt[el * N3 + i * N2 + jk] = A::finish(bt);
+    }
+    __syncthreads();  // this batch's G and map tiles are consumed
+    if (tid == 0 && batch + gridDim.x < n_batches) {
+      fence_proxy_async_smem();
+      issue(batch + gridDim.x);
+    }
+
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        A::fma(a, basis.D[m * N + i], vr[m]);
+        A::fma(a, Dtj[m], s_vs[el * N3 + i * N2 + m * N + k]);
+        A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
+      }
+      const V y = A::finish(a);
+      if (idx[i] != MFGB_INVALID_DOF) {
+        const typename A::VecT yv = A::store_vec(y);
+        atomicAdd(dst + idx[i], yv);
+        if (WITH_ENERGY) energy = __fma_rn((double)__ldg(src + idx[i]), (double)yv, energy);
+      }
+    }
+    __syncthreads();
+  }
+
+  if (WITH_ENERGY) {
+    double *s_red = reinterpret_cast<double *>(s_u);  // work arrays are free now
+    s_red[tid] = energy;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int t = 0; t < E * N * N; ++t) s += s_red[t];
+      energy_partials[blockIdx.x] = s;
+    }
+  }
+}
+
+}  // namespace mfgb

@@ -89,6 +89,14 @@ __device__ __forceinline__ void dfacc_fma(dfacc &a, df x, df y) {
   a.c = c;
 }
 
+// a += b  (two lazy accumulators)
+__device__ __forceinline__ void dfacc_merge(dfacc &a, const dfacc &b) {
+  float s, t;
+  two_sum(a.s, b.s, s, t);
+  a.s = s;
+  a.c = __fadd_rn(a.c, __fadd_rn(b.c, t));
+}
+
 __device__ __forceinline__ df dfacc_finish(const dfacc &a) {
   df r;
   float t;
@@ -110,6 +118,7 @@ struct ArithF64 {
   using VecT = double;
   static __device__ __forceinline__ void zero(Acc &a) { a = 0.0; }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fma_rn(x, y, a); }
+  static __device__ __forceinline__ void merge(Acc &a, const Acc &b) { a = __dadd_rn(a, b); }
   static __device__ __forceinline__ V finish(const Acc &a) { return a; }
   static __device__ __forceinline__ V load_vec(VecT x) { return x; }
   static __device__ __forceinline__ VecT store_vec(V x) { return x; }
@@ -125,6 +134,7 @@ struct ArithF32 {
   using VecT = float;
   static __device__ __forceinline__ void zero(Acc &a) { a = 0.f; }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fmaf_rn(x, y, a); }
+  static __device__ __forceinline__ void merge(Acc &a, const Acc &b) { a = __fadd_rn(a, b); }
   static __device__ __forceinline__ V finish(const Acc &a) { return a; }
   static __device__ __forceinline__ V load_vec(VecT x) { return x; }
   static __device__ __forceinline__ VecT store_vec(V x) { return x; }
@@ -140,6 +150,7 @@ struct ArithDF {
   using VecT = double;
   static __device__ __forceinline__ void zero(Acc &a) { dfacc_zero(a); }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { dfacc_fma(a, x, y); }
+  static __device__ __forceinline__ void merge(Acc &a, const Acc &b) { dfacc_merge(a, b); }
   static __device__ __forceinline__ V finish(const Acc &a) { return dfacc_finish(a); }
   static __device__ __forceinline__ V load_vec(VecT x) { return df_from_double(x); }
   static __device__ __forceinline__ VecT store_vec(V x) { return df_to_double(x); }

@@ -16,6 +16,29 @@ template <> struct ElemsPerCta<7> { static constexpr int value = 4; };
 template <> struct ElemsPerCta<8> { static constexpr int value = 2; };
 template <> struct ElemsPerCta<9> { static constexpr int value = 2; };
 
+// point-per-thread kernel: elements per CTA (CTA = E * N^3 threads)
+template <int N> struct ElemsPerCtaPt;
+template <> struct ElemsPerCtaPt<2> { static constexpr int value = 32; };
+template <> struct ElemsPerCtaPt<3> { static constexpr int value = 8; };
+template <> struct ElemsPerCtaPt<4> { static constexpr int value = 4; };
+template <> struct ElemsPerCtaPt<5> { static constexpr int value = 2; };
+template <> struct ElemsPerCtaPt<6> { static constexpr int value = 2; };
+template <> struct ElemsPerCtaPt<7> { static constexpr int value = 1; };
+template <> struct ElemsPerCtaPt<8> { static constexpr int value = 1; };
+template <> struct ElemsPerCtaPt<9> { static constexpr int value = 1; };
+
+// Kernel shape: 0 = column (thread owns an i-column), 1 = point-per-thread,
+// 2 = column with TMA-prefetched geometric factors.  Default per
+// (arithmetic, N); overridable at run time (autotuner).
+enum { SHAPE_COLUMN = 0, SHAPE_POINT = 1, SHAPE_TMA = 2 };
+int kernel_shape(int arith_class, int N);  // mfgb_api.cu
+int *device_error_flag();                  // mfgb_api.cu
+
+template <class A> struct ArithClass { static constexpr int value = 0; };  // FP64
+template <> struct ArithClass<ArithDF> { static constexpr int value = 1; };
+template <> struct ArithClass<ArithDFG64> { static constexpr int value = 1; };
+template <> struct ArithClass<ArithF32> { static constexpr int value = 2; };
+
 inline int num_sms() {
   static int sms = -1;
   if (sms < 0) {
@@ -26,18 +49,40 @@ inline int num_sms() {
   return sms;
 }
 
+// CTAs per SM of one kernel instantiation (queried once)
+template <class K>
+int ctas_per_sm(K kernel, int threads, size_t smem) {
+  int ps = 0;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, kernel, threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    ps = 0;
+  }
+  return ps;
+}
+
 // grid for a persistent launch: all resident CTAs, capped by the work
 template <int N, class A, bool EVEC, bool EN>
-int bk5_grid(int64_t n_cells) {
-  constexpr int E = ElemsPerCta<N>::value;
-  static int per_sm = -1;
-  if (per_sm < 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bk5_kernel<N, E, A, EVEC, EN>,
-                                                      E * N * N, 0) != cudaSuccess || per_sm < 1)
-      per_sm = 1;
+int bk5_grid(int64_t n_cells, int shape) {
+  static int per_sm[3] = {-1, -1, -1};
+  int &ps = per_sm[shape];
+  int E;
+  if (shape == SHAPE_POINT) {
+    E = ElemsPerCtaPt<N>::value;
+    if (ps < 0) ps = ctas_per_sm(bk5_pt_kernel<N, ElemsPerCtaPt<N>::value, A, EVEC, EN>, E * N * N * N, 0);
+  } else if (shape == SHAPE_TMA) {
+    constexpr int ET = ElemsPerCta<N>::value;
+    E = ET;
+    if (ps < 0)
+      ps = ctas_per_sm(bk5_tma_kernel<N, ET, A, EN>, ET * N * N, TmaLayout<N, ET, A>::total);
+  } else {
+    E = ElemsPerCta<N>::value;
+    if (ps < 0) ps = ctas_per_sm(bk5_kernel<N, ElemsPerCta<N>::value, A, EVEC, EN>, E * N * N, 0);
   }
+  if (ps < 1) ps = 1;
   const int64_t n_batches = (n_cells + E - 1) / E;
-  const int64_t full = (int64_t)per_sm * num_sms();
+  const int64_t full = (int64_t)ps * num_sms();
   return (int)std::max<int64_t>(1, std::min<int64_t>(n_batches, full));
 }
 
@@ -46,12 +91,30 @@ cudaError_t bk5_launch(int64_t n_cells, const uint32_t *map, const typename A::G
                        const typename A::VecT *src, typename A::VecT *dst,
                        const Basis<N, A> &basis, double *partials, int *grid_used,
                        cudaStream_t stream, const int *done_flag = nullptr) {
-  constexpr int E = ElemsPerCta<N>::value;
-  const int grid = bk5_grid<N, A, EVEC, EN>(n_cells);
+  int shape = kernel_shape(ArithClass<A>::value, N);
+  // bulk copies need 16-byte aligned tiles: E-vector mode and caller arrays
+  // that are not 16-byte aligned use the plain column kernel
+  if (shape == SHAPE_TMA &&
+      (EVEC || ((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(map)) & 15u)))
+    shape = SHAPE_COLUMN;
+  const int grid = bk5_grid<N, A, EVEC, EN>(n_cells, shape);
   if (grid_used) *grid_used = grid;
   if (n_cells <= 0) return cudaSuccess;
-  bk5_kernel<N, E, A, EVEC, EN><<<grid, E * N * N, 0, stream>>>(n_cells, map, G, src, dst, basis,
-                                                                 partials, done_flag);
+  if (shape == SHAPE_POINT) {
+    constexpr int E = ElemsPerCtaPt<N>::value;
+    bk5_pt_kernel<N, E, A, EVEC, EN><<<grid, E * N * N * N, 0, stream>>>(
+        n_cells, map, G, src, dst, basis, partials, done_flag);
+  } else if (shape == SHAPE_TMA) {
+    if constexpr (!EVEC) {
+      constexpr int E = ElemsPerCta<N>::value;
+      bk5_tma_kernel<N, E, A, EN><<<grid, E * N * N, TmaLayout<N, E, A>::total, stream>>>(
+          n_cells, map, G, src, dst, basis, partials, done_flag, device_error_flag());
+    }
+  } else {
+    constexpr int E = ElemsPerCta<N>::value;
+    bk5_kernel<N, E, A, EVEC, EN><<<grid, E * N * N, 0, stream>>>(n_cells, map, G, src, dst,
+                                                                   basis, partials, done_flag);
+  }
   return cudaGetLastError();
 }
 

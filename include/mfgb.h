@@ -35,7 +35,8 @@ enum {
 /* Arithmetic used inside the operator kernels (vectors stay FP64). */
 enum {
   MFGB_ARITH_FP64 = 0,    /* native FP64 (DFMA) */
-  MFGB_ARITH_FP64_DF = 1  /* FP64-accurate double-float on the FP32 pipes */
+  MFGB_ARITH_FP64_DF = 1, /* FP64-accurate double-float on the FP32 pipes */
+  MFGB_ARITH_FP32 = 2     /* FP32 operator on FP32 vectors (multigrid levels) */
 };
 
 #define MFGB_INVALID_DOF_INDEX 0xFFFFFFFFu
@@ -65,6 +66,19 @@ typedef struct {
   double last;      /* last_value() */
   int converged;    /* 1 if the reduction criterion was met */
 } mfgb_solve_info;
+
+/* Thread layout of the operator kernel for (arith, degree): 0 = one thread per
+   (j,k) column of an element, 1 = one thread per quadrature point, 2 = columns
+   with the geometric factors prefetched by bulk TMA copies.  The
+   library starts from a built-in table; the autotuner overrides it.  No
+   counterpart in the reference (its launch shape is a compile-time choice,
+   CEED_BK/src/BK5/templated_cuda_benchmark.cc:114-124). */
+mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape);
+mfgb_status mfgb_get_kernel_shape(int arith, int degree, int *shape);
+
+/* Reads and clears the device error word: MFGB_ERR_TIMEOUT if a kernel gave
+   up on a bulk-copy wait since the last check (its results are invalid). */
+mfgb_status mfgb_check_device_errors(void *stream);
 
 const char *mfgb_status_string(mfgb_status s);
 const char *mfgb_last_error(void);

@@ -188,3 +188,39 @@ def test_full_size_properties(mf):
     assert mf.dot(u, Audf) > 0
     del A
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2])
+@pytest.mark.parametrize("arith", ["fp64", "df"])
+@pytest.mark.parametrize("p", [1, 2, 4, 5, 7, 8])
+def test_every_kernel_shape_matches_oracle(mf, orc, shape, arith, p):
+    """Each thread layout (column, point, column + TMA prefetch) for each
+    arithmetic, on a mesh whose cell count leaves a partial last batch."""
+    import ctypes
+    from benchmarks_gb300 import _abi
+    L = mf.lib()
+    a = mf._arith(arith)
+    old = ctypes.c_int()
+    _abi.check(L.mfgb_get_kernel_shape(a, p, ctypes.byref(old)))
+    try:
+        _abi.check(L.mfgb_set_kernel_shape(a, p, shape))
+        cells = (3, 5, 3)  # 45 cells: not a multiple of any batch size
+        A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.1))
+        ref = orc.BoxProblem(*cells, p, amplitude=0.1)
+        src = np.random.default_rng(3).uniform(-1, 1, ref.n_dofs)
+        y = A.initialize_dof_vector()
+        A.vmult(y, to_dev(src), arith=arith)
+        assert rel(y.cpu().numpy(), ref.apply(src)) <= TOL
+        # the energy (p.Ap) variant used by CG: iterate after 6 steps (before
+        # convergence, so the comparison is not at a rounding-level residual)
+        b = A.rhs_uniform(4)
+        x = A.initialize_dof_vector()
+        ctl = mf.ReductionControl(6, 1e-300, 1e-14)
+        with pytest.raises(mf.MfgbError):
+            mf.SolverCG(ctl).solve(A, x, b, arith=arith)
+        x_ref, info = ref.cg(ref.rhs(4), reduce=1e-14, max_steps=6)
+        assert ctl.last_step() == info["steps"] == 6
+        assert rel(x.cpu().numpy(), x_ref) <= 1e-10
+        _abi.check(L.mfgb_check_device_errors(None))
+    finally:
+        _abi.check(L.mfgb_set_kernel_shape(a, p, old.value))
