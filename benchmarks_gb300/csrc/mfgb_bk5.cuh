@@ -275,13 +275,20 @@ struct TmaLayout {
   static constexpr bool map_tma = (E * N3 * 4) % 16 == 0;
 };
 
-// Column kernel with the next batch's geometric factors (and dof map, when its
-// tile is 16-byte sized) prefetched into shared memory by one bulk TMA copy
-// per batch, issued as soon as the current batch has consumed its tiles; the
-// copy lands while the CTA integrates and scatters.  L-vector mode only.
+// Column kernel with bulk-TMA prefetch.  Per batch b of E cells:
+//   barrier A   wait for G(b) (mbarrier 0); the u(b) gather was prefetched
+//               into registers during batch b-1
+//   write s_u, barrier B, then TMA of map(b+next) (mbarrier 1)
+//   gradient + metric (reads s_u, G(b) from shared memory), barrier C,
+//   then TMA of G(b+next)
+//   wait for map(b+next), prefetch u(b+next) = src[map] into registers,
+//   integrate + atomic scatter of batch b
+// Shared memory holds one G tile, one map tile and the three work arrays.
 // err_flag (may be null) records a TMA wait that exceeded its time limit.
+template <int N> struct TmaMinBlocks { static constexpr int value = N <= 6 ? 2 : 1; };
+
 template <int N, int E, class A, bool WITH_ENERGY>
-__global__ void __launch_bounds__(E * N * N)
+__global__ void __launch_bounds__(E * N * N, TmaMinBlocks<N>::value)
     bk5_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
                    const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
                    typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
@@ -291,6 +298,7 @@ __global__ void __launch_bounds__(E * N * N)
   using V = typename A::V;
   using Acc = typename A::Acc;
   using GT = typename A::GType;
+  using VT = typename A::VecT;
   using L = TmaLayout<N, E, A>;
   constexpr int N2 = N * N, N3 = N * N * N;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -300,6 +308,7 @@ __global__ void __launch_bounds__(E * N * N)
   V *s_vs = s_u + E * N3;
   V *s_vt = s_vs + E * N3;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+  uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
 
   const int tid = threadIdx.x;
   const int el = tid / N2;
@@ -319,51 +328,77 @@ __global__ void __launch_bounds__(E * N * N)
     Dtk[m] = basis.D[m * N + k];
   }
 
-  auto issue = [&](int64_t b) {  // one thread
-    const int64_t c0 = b * E;
-    const int cells = (int)min((int64_t)E, n_cells - c0);
-    const uint32_t gb = (uint32_t)(sizeof(GT) * cells * 6 * N3);
-    const bool mt = L::map_tma && ((cells * N3 * 4) % 16 == 0);
-    const uint32_t mb = mt ? (uint32_t)(cells * N3 * 4) : 0u;
-    mbar_arrive_expect_tx(mbar, gb + mb);
-    bulk_g2s(sG, G + c0 * 6 * N3, gb, mbar);
-    if (mt) bulk_g2s(sMap, map + c0 * N3, mb, mbar);
+  auto cells_of = [&](int64_t b) { return (int)min((int64_t)E, n_cells - b * E); };
+  auto map_by_tma = [&](int cells) { return L::map_tma && ((cells * N3 * 4) % 16 == 0); };
+  auto issue_g = [&](int64_t b) {  // one thread
+    const uint32_t gb = (uint32_t)(sizeof(GT) * cells_of(b) * 6 * N3);
+    mbar_arrive_expect_tx(mbar_g, gb);
+    bulk_g2s(sG, G + b * E * 6 * N3, gb, mbar_g);
+  };
+  auto issue_map = [&](int64_t b) {  // one thread; completes the phase either way
+    const int cells = cells_of(b);
+    const uint32_t mb = map_by_tma(cells) ? (uint32_t)(cells * N3 * 4) : 0u;
+    mbar_arrive_expect_tx(mbar_m, mb);
+    if (mb) bulk_g2s(sMap, map + b * E * N3, mb, mbar_m);
+  };
+  // gather of one batch into registers (idx from the map tile or global)
+  auto gather = [&](int64_t b, uint32_t *idx, VT *raw) {
+    const int cells = cells_of(b);
+    const bool valid = el < cells;
+    const bool mt = map_by_tma(cells);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      idx[i] = valid ? (mt ? sMap[el * N3 + i * N2 + jk] : __ldg(map + (b * E + el) * N3 + i * N2 + jk))
+                     : MFGB_INVALID_DOF;
+      raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + idx[i]) : VT(0);
+    }
+  };
+  auto fail = [&](uint32_t pg, uint32_t pm) {
+    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
+    mbar_wait(mbar_m, pm);
   };
 
   if (tid == 0) {
-    mbar_init(mbar, 1);
+    mbar_init(mbar_g, 1);
+    mbar_init(mbar_m, 1);
     fence_mbar_init();
   }
   __syncthreads();
-  if (tid == 0) issue(batch);
-  uint32_t phase = 0;
+  if (tid == 0) {
+    issue_g(batch);
+    issue_map(batch);
+  }
+  uint32_t ph_g = 0, ph_m = 0;
+  uint32_t idx[N];
+  VT raw[N];
+  {
+    const bool ok = mbar_wait(mbar_m, ph_m);
+    if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
+    ph_m ^= 1u;
+    gather(batch, idx, raw);
+  }
   double energy = 0.0;
 
   for (; batch < n_batches; batch += gridDim.x) {
-    const int64_t c0 = batch * E;
-    const int cells = (int)min((int64_t)E, n_cells - c0);
-    const bool mt = L::map_tma && ((cells * N3 * 4) % 16 == 0);
-    const bool valid = el < cells;
-    const int64_t cell = c0 + el;
-    const bool landed = mbar_wait(mbar, phase);
-    if (__syncthreads_or(!landed)) {
-      if (tid == 0 && err_flag) atomicExch(err_flag, 1);
-      mbar_wait(mbar, phase);  // bounded second wait for the copy still in flight
-      return;
-    }
-    phase ^= 1u;
-
+    const int64_t next = batch + gridDim.x;
+    const bool has_next = next < n_batches;
+    const bool okg = mbar_wait(mbar_g, ph_g);
+    if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
+    ph_g ^= 1u;
     V u[N];
-    uint32_t idx[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      idx[i] = valid ? (mt ? sMap[el * N3 + i * N2 + jk] : __ldg(map + cell * N3 + i * N2 + jk))
-                     : MFGB_INVALID_DOF;
-      u[i] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(__ldg(src + idx[i])) : A::zero_v();
+      u[i] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(raw[i]) : A::zero_v();
       s_u[el * N3 + i * N2 + jk] = u[i];
     }
-    __syncthreads();
+    __syncthreads();  // barrier B: s_u ready; the map tile is free
+    if (tid == 0 && has_next) {
+      fence_proxy_async_smem();
+      issue_map(next);
+    }
 
+    const bool valid = el < cells_of(batch);
     V vr[N];
     const GT *Gc = sG + el * 6 * N3 + jk;
 #pragma unroll
@@ -399,10 +434,29 @@ __global__ void __launch_bounds__(E * N * N)
       s_vs[el * N3 + i * N2 + jk] = A::finish(bs);
       s_vt[el * N3 + i * N2 + jk] = A::finish(bt);
     }
-    __syncthreads();  // this batch's G and map tiles are consumed
-    if (tid == 0 && batch + gridDim.x < n_batches) {
+    __syncthreads();  // barrier C: G tile consumed, s_vs / s_vt ready
+    if (tid == 0 && has_next) {
       fence_proxy_async_smem();
-      issue(batch + gridDim.x);
+      issue_g(next);
+    }
+
+    // this batch's scatter targets; then prefetch the next batch's gather
+    uint32_t cur[N];
+    VT cur_raw[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      cur[i] = idx[i];
+      cur_raw[i] = raw[i];
+    }
+    if (has_next) {
+      const bool okm = mbar_wait(mbar_m, ph_m);
+      if (!okm) {  // per-thread: fall back to the global map (always valid)
+        if (err_flag) atomicExch(err_flag, 1);
+      }
+      ph_m ^= 1u;
+      if (okm) gather(next, idx, raw);
+      else
+        for (int i = 0; i < N; ++i) { idx[i] = MFGB_INVALID_DOF; raw[i] = VT(0); }
     }
 
 #pragma unroll
@@ -416,16 +470,16 @@ __global__ void __launch_bounds__(E * N * N)
         A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
       }
       const V y = A::finish(a);
-      if (idx[i] != MFGB_INVALID_DOF) {
-        const typename A::VecT yv = A::store_vec(y);
-        atomicAdd(dst + idx[i], yv);
-        if (WITH_ENERGY) energy = __fma_rn((double)__ldg(src + idx[i]), (double)yv, energy);
+      if (cur[i] != MFGB_INVALID_DOF) {
+        const VT yv = A::store_vec(y);
+        atomicAdd(dst + cur[i], yv);
+        if (WITH_ENERGY) energy = __fma_rn((double)cur_raw[i], (double)yv, energy);
       }
     }
-    __syncthreads();
   }
 
   if (WITH_ENERGY) {
+    __syncthreads();
     double *s_red = reinterpret_cast<double *>(s_u);  // work arrays are free now
     s_red[tid] = energy;
     __syncthreads();
