@@ -21,7 +21,7 @@ from ._abi import MfgbError, ARITH_FP64, ARITH_FP64_DF, lib, library_path  # noq
 
 __all__ = [
     "BoxMesh", "LaplaceOperator", "ReductionControl", "SolverCG", "DiagonalMatrix",
-    "PreconditionIdentity", "MfgbError", "ARITH_FP64", "ARITH_FP64_DF", "lib", "library_path",
+    "PreconditionIdentity", "MGPreconditioner", "MfgbError", "ARITH_FP64", "ARITH_FP64_DF", "lib", "library_path",
     "bk5_evector", "bk5_lvector", "dot",
 ]
 
@@ -67,6 +67,7 @@ class BoxMesh:
     amplitude: float = 0.05
     lo: tuple = (0.0, 0.0, 0.0)
     hi: tuple = (1.0, 1.0, 1.0)
+    geometry_degree: int = 0
 
     @property
     def n_dofs(self) -> int:
@@ -80,7 +81,7 @@ class BoxMesh:
     def _desc(self):
         return _abi.BoxDesc(self.nx, self.ny, self.nz, self.degree,
                             (ctypes.c_double * 3)(*self.lo), (ctypes.c_double * 3)(*self.hi),
-                            self.amplitude)
+                            self.amplitude, self.geometry_degree)
 
 
 class LaplaceOperator:
@@ -221,6 +222,52 @@ class PreconditionIdentity:
         return dst
 
 
+class MGPreconditioner:
+    """Geometric p-/h-multigrid V-cycle for a box mesh (mfgb_mg_* in the C ABI):
+    p_fine -> p_fine/2 -> ... -> 1, then Q1 on 2:1 coarsened meshes; Chebyshev
+    smoothing around Jacobi; FP64 Jacobi-CG coarse solve.  ``precision`` 32
+    runs the V-cycle in FP32 (the mixed-precision preconditioner inside FP64
+    CG), 64 in FP64."""
+
+    def __init__(self, mesh: BoxMesh, precision=32, chebyshev_degree=5, smoothing_range=15.0,
+                 eig_iterations=20, coarse_cells=4, coarse_tol=1e-12):
+        self.mesh = mesh
+        self.precision = precision
+        self._mg = ctypes.c_void_p()
+        prm = _abi.MgParams(precision, chebyshev_degree, smoothing_range, eig_iterations,
+                            coarse_cells, coarse_tol)
+        desc = mesh._desc()
+        _abi.check(lib().mfgb_mg_setup(ctypes.byref(desc), ctypes.byref(prm),
+                                       ctypes.byref(self._mg)))
+        nl = ctypes.c_int()
+        _abi.check(lib().mfgb_mg_info(self._mg, ctypes.byref(nl), None, None, None))
+        dofs = (ctypes.c_int64 * nl.value)()
+        deg = (ctypes.c_int * nl.value)()
+        lmax = (ctypes.c_double * nl.value)()
+        _abi.check(lib().mfgb_mg_info(self._mg, None, dofs, deg, lmax))
+        self.levels = [{"dofs": dofs[i], "degree": deg[i], "lambda_max": lmax[i]}
+                       for i in range(nl.value)]
+
+    def __del__(self):
+        mg = getattr(self, "_mg", None)
+        if mg is not None and mg.value:
+            try:
+                lib().mfgb_mg_destroy(mg)
+            except Exception:
+                pass
+            self._mg = None
+
+    def vmult(self, dst, src):
+        n = self.levels[0]["dofs"]
+        _abi.check(lib().mfgb_mg_vmult(self._mg, _check_vec(dst, n, "dst"),
+                                       _check_vec(src, n, "src"), _stream_ptr()))
+        return dst
+
+    @property
+    def handle(self):
+        return self._mg
+
+
 class ReductionControl:
     """deal.II ReductionControl(max_steps, tol, reduce)."""
 
@@ -252,6 +299,15 @@ class SolverCG:
                              A.arith if arith is None else _arith(arith))
         info = _abi.SolveInfo()
         inv = None
+        if isinstance(preconditioner, MGPreconditioner):
+            st = lib().mfgb_mg_cg_solve(A.handle, preconditioner.handle,
+                                        _check_vec(b, A.n(), "b"), _check_vec(x, A.n(), "x"),
+                                        ctypes.byref(ctl), ctypes.byref(info), _stream_ptr())
+            self.control._last_step = info.steps
+            self.control._initial = info.initial
+            self.control._last = info.last
+            _abi.check(st)
+            return x
         if isinstance(preconditioner, DiagonalMatrix):
             inv = _check_vec(preconditioner.vector, A.n(), "preconditioner")
         elif preconditioner is not None and not isinstance(preconditioner, PreconditionIdentity):

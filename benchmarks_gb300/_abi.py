@@ -22,12 +22,19 @@ class MfgbError(RuntimeError):
 class BoxDesc(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
                 ("degree", ctypes.c_int), ("lo", ctypes.c_double * 3),
-                ("hi", ctypes.c_double * 3), ("amplitude", ctypes.c_double)]
+                ("hi", ctypes.c_double * 3), ("amplitude", ctypes.c_double),
+                ("geometry_degree", ctypes.c_int)]
 
 
 class CgControl(ctypes.Structure):
     _fields_ = [("max_steps", ctypes.c_int), ("tol", ctypes.c_double),
                 ("reduce", ctypes.c_double), ("arith", ctypes.c_int)]
+
+
+class MgParams(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("chebyshev_degree", ctypes.c_int),
+                ("smoothing_range", ctypes.c_double), ("eig_iterations", ctypes.c_int),
+                ("coarse_cells", ctypes.c_int), ("coarse_tol", ctypes.c_double)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -66,6 +73,7 @@ def lib():
         "mfgb_operator_export": ([P, P, P, P], I32),
         "mfgb_vmult": ([P, P, P, I32, P], I32),
         "mfgb_vmult_add": ([P, P, P, I32, P], I32),
+        "mfgb_vmult_f32": ([P, P, P, P], I32),
         "mfgb_copy_constrained": ([P, P, P, P], I32),
         "mfgb_bk5_lvector": ([I32, I64, P, P, P, P, P, I32, P], I32),
         "mfgb_bk5_evector": ([I32, I64, P, P, P, P, I32, P], I32),
@@ -77,6 +85,12 @@ def lib():
         "mfgb_cg_solve_noalloc": ([P, P, P, P, ctypes.POINTER(CgControl),
                                    ctypes.POINTER(SolveInfo), P], I32),
         "mfgb_dot": ([I64, P, P, ctypes.POINTER(D), P], I32),
+        "mfgb_mg_setup": ([ctypes.POINTER(BoxDesc), ctypes.POINTER(MgParams), PP], I32),
+        "mfgb_mg_destroy": ([P], I32),
+        "mfgb_mg_info": ([P, P, P, P, P], I32),
+        "mfgb_mg_vmult": ([P, P, P, P], I32),
+        "mfgb_mg_cg_solve": ([P, P, P, P, ctypes.POINTER(CgControl), ctypes.POINTER(SolveInfo), P],
+                             I32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)

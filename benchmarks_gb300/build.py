@@ -19,6 +19,7 @@ SOURCES = [
     "mfgb_api.cu",
     "mfgb_setup.cu",
     "mfgb_cg.cu",
+    "mfgb_mg.cu",
     "mfgb_bk5_f64.cu",
     "mfgb_bk5_df.cu",
     "mfgb_bk5_f32.cu",

@@ -191,6 +191,7 @@ mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **o
   }
   *out = nullptr;
   if (box->degree < 1 || box->degree > 8 || box->nx < 1 || box->ny < 1 || box->nz < 1 ||
+      box->geometry_degree < 0 || box->geometry_degree > 8 ||
       !(box->hi[0] > box->lo[0]) || !(box->hi[1] > box->lo[1]) || !(box->hi[2] > box->lo[2])) {
     set_error("mfgb_operator_create_box: degree must be 1..8 and the box non-empty");
     return MFGB_ERR_INVALID_ARG;

@@ -1,4 +1,5 @@
 // mfgb_setup.cu -- bases, structured-box set-up kernels, diagonal, constraints.
+#include <algorithm>
 #include <cmath>
 
 #include "mfgb_common.cuh"
@@ -101,25 +102,30 @@ cudaError_t box_map(const mfgb_box_desc &b, uint32_t *d_map, cudaStream_t s) {
 }
 
 struct GeomParams {
-  double x[9], w[9], D[81];
+  double x[9], w[9];      // GLL points / weights of the operator degree
+  double xg[9];           // GLL points of the geometry degree
+  double V[81], Dv[81];   // V[i*ng+a] = l_a(x_i), Dv[i*ng+a] = l_a'(x_i) (geometry basis)
+  int ng;                 // geometry points per direction
 };
 
-// One CTA per cell: node coordinates (GLL points of the cell, deformed) in
-// shared memory, then J = dx/dxi by the derivative matrix, and
-// G = |det J| w_i w_j w_k Jinv Jinv^T at every GLL point.
+// One CTA per cell: the deformed geometry nodes (GLL points of the geometry
+// degree) in shared memory, then J = dx/dxi at the operator's GLL points
+// (the derivative matrix when both degrees agree, the tensor-product
+// geometry basis otherwise) and G = |det J| w_i w_j w_k Jinv Jinv^T.
 __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__restrict__ G) {
   __shared__ double xyz[729 * 3];
   const int n = b.degree + 1, n3 = n * n * n;
+  const int ng = gp.ng, ng3 = ng * ng * ng;
   const int64_t e = blockIdx.x;
   const int64_t cx = e % b.nx, cy = (e / b.nx) % b.ny, cz = e / ((int64_t)b.nx * b.ny);
   const double hx = (b.hi[0] - b.lo[0]) / b.nx, hy = (b.hi[1] - b.lo[1]) / b.ny,
                hz = (b.hi[2] - b.lo[2]) / b.nz;
   const double two_pi = 2.0 * M_PI;
-  for (int l = threadIdx.x; l < n3; l += blockDim.x) {
-    const int i = l / (n * n), j = (l / n) % n, k = l % n;
-    const double X = b.lo[0] + ((double)cx + 0.5 * (gp.x[k] + 1.0)) * hx;
-    const double Y = b.lo[1] + ((double)cy + 0.5 * (gp.x[j] + 1.0)) * hy;
-    const double Z = b.lo[2] + ((double)cz + 0.5 * (gp.x[i] + 1.0)) * hz;
+  for (int l = threadIdx.x; l < ng3; l += blockDim.x) {
+    const int i = l / (ng * ng), j = (l / ng) % ng, k = l % ng;
+    const double X = b.lo[0] + ((double)cx + 0.5 * (gp.xg[k] + 1.0)) * hx;
+    const double Y = b.lo[1] + ((double)cy + 0.5 * (gp.xg[j] + 1.0)) * hy;
+    const double Z = b.lo[2] + ((double)cz + 0.5 * (gp.xg[i] + 1.0)) * hz;
     const double s = b.amplitude * sin(two_pi * X) * sin(two_pi * Y) * sin(two_pi * Z);
     xyz[3 * l + 0] = X + s;
     xyz[3 * l + 1] = Y + s;
@@ -129,14 +135,31 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
   for (int l = threadIdx.x; l < n3; l += blockDim.x) {
     const int i = l / (n * n), j = (l / n) % n, k = l % n;
     double J[3][3];
-    for (int d = 0; d < 3; ++d) {
-      double jr = 0, js = 0, jt = 0;
-      for (int m = 0; m < n; ++m) {
-        jr += gp.D[i * n + m] * xyz[3 * (m * n * n + j * n + k) + d];
-        js += gp.D[j * n + m] * xyz[3 * (i * n * n + m * n + k) + d];
-        jt += gp.D[k * n + m] * xyz[3 * (i * n * n + j * n + m) + d];
+    if (ng == n) {
+      for (int d = 0; d < 3; ++d) {
+        double jr = 0, js = 0, jt = 0;
+        for (int m = 0; m < n; ++m) {
+          jr += gp.Dv[i * n + m] * xyz[3 * (m * n * n + j * n + k) + d];
+          js += gp.Dv[j * n + m] * xyz[3 * (i * n * n + m * n + k) + d];
+          jt += gp.Dv[k * n + m] * xyz[3 * (i * n * n + j * n + m) + d];
+        }
+        J[d][0] = jr; J[d][1] = js; J[d][2] = jt;
       }
-      J[d][0] = jr; J[d][1] = js; J[d][2] = jt;
+    } else {
+      for (int d = 0; d < 3; ++d) J[d][0] = J[d][1] = J[d][2] = 0.0;
+      for (int a = 0; a < ng; ++a)
+        for (int bb = 0; bb < ng; ++bb)
+          for (int c = 0; c < ng; ++c) {
+            const double *x = xyz + 3 * (a * ng * ng + bb * ng + c);
+            const double wr = gp.Dv[i * ng + a] * gp.V[j * ng + bb] * gp.V[k * ng + c];
+            const double ws = gp.V[i * ng + a] * gp.Dv[j * ng + bb] * gp.V[k * ng + c];
+            const double wt = gp.V[i * ng + a] * gp.V[j * ng + bb] * gp.Dv[k * ng + c];
+            for (int d = 0; d < 3; ++d) {
+              J[d][0] += wr * x[d];
+              J[d][1] += ws * x[d];
+              J[d][2] += wt * x[d];
+            }
+          }
     }
     const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
     const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
@@ -167,13 +190,28 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
 
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
                          const double *D, double *d_G, cudaStream_t s) {
-  GeomParams gp;
+  GeomParams gp{};
   const int n = b.degree + 1;
-  for (int i = 0; i < 9; ++i) { gp.x[i] = i < n ? gll_x[i] : 0.0; gp.w[i] = i < n ? gll_w[i] : 0.0; }
-  for (int i = 0; i < 81; ++i) gp.D[i] = i < n * n ? D[i] : 0.0;
+  const int g = b.geometry_degree > 0 ? b.geometry_degree : b.degree;
+  if (g < 1 || g > 8) return cudaErrorInvalidValue;
+  gp.ng = g + 1;
+  for (int i = 0; i < n; ++i) { gp.x[i] = gll_x[i]; gp.w[i] = gll_w[i]; }
+  if (gp.ng == n) {
+    for (int i = 0; i < n; ++i) gp.xg[i] = gll_x[i];
+    for (int i = 0; i < n * n; ++i) gp.Dv[i] = D[i];
+  } else {
+    double wg[9];
+    gll_nodes(gp.ng, gp.xg, wg);
+    for (int i = 0; i < n; ++i)
+      for (int a = 0; a < gp.ng; ++a) {
+        gp.V[i * gp.ng + a] = lagrange_value(gp.ng, gp.xg, a, gll_x[i]);
+        gp.Dv[i * gp.ng + a] = lagrange_derivative(gp.ng, gp.xg, a, gll_x[i]);
+      }
+  }
   const int64_t n_cells = (int64_t)b.nx * b.ny * b.nz;
   if (n_cells == 0) return cudaSuccess;
-  const int threads = ((n * n * n + 31) / 32) * 32;
+  const int pts = std::max(n * n * n, gp.ng * gp.ng * gp.ng);
+  const int threads = ((pts + 31) / 32) * 32;
   box_geometry_kernel<<<(unsigned)n_cells, threads > 256 ? 256 : threads, 0, s>>>(b, gp, d_G);
   return cudaGetLastError();
 }

@@ -45,12 +45,16 @@ typedef struct mfgb_operator mfgb_operator;
 
 /* Structured box mesh: nx*ny*nz hex cells of degree p with GLL nodes,
    every geometry node moved by x_d += amplitude*sin(2 pi x)sin(2 pi y)sin(2 pi z),
-   Dirichlet u = 0 on the whole boundary, lexicographic DoF numbering (x fastest). */
+   Dirichlet u = 0 on the whole boundary, lexicographic DoF numbering (x fastest).
+   The cell geometry is the Q_g interpolant of the deformed map at the GLL
+   points of degree g = geometry_degree (0: g = degree); multigrid levels use
+   the fine degree so coarse cells stay as accurate as the fine ones. */
 typedef struct {
   int nx, ny, nz;
   int degree;
   double lo[3], hi[3];
   double amplitude;
+  int geometry_degree;
 } mfgb_box_desc;
 
 typedef struct {
@@ -126,6 +130,10 @@ mfgb_status mfgb_vmult_add(const mfgb_operator *op, double *d_dst, const double 
 mfgb_status mfgb_copy_constrained(const mfgb_operator *op, double *d_dst, const double *d_src,
                                   void *stream);
 
+/* vmult in FP32 arithmetic on FP32 vectors (the multigrid levels; the FP32
+   copy of G is built on first use). */
+mfgb_status mfgb_vmult_f32(const mfgb_operator *op, float *d_dst, const float *d_src, void *stream);
+
 /* Kernel seam of BK3::Parallel::KokkosKernel_1D_Block
    (bakeoff_problems_dealii/include/bk3_kokkos_kernel.h:32-43) in the
    GLL-collocated form: accumulates sum_cells P^T A_e P src into d_dst (no
@@ -177,6 +185,36 @@ mfgb_status mfgb_cg_solve(const mfgb_operator *op, const double *d_b, double *d_
 mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const double *d_b, double *d_x,
                                   const double *d_inv_diag, const mfgb_cg_control *ctl,
                                   mfgb_solve_info *info, void *stream);
+
+/* ---- multigrid preconditioner (no counterpart in the reference) ----------
+ * Geometric p- and h-multigrid V-cycle for the structured box: p_fine ->
+ * p_fine/2 -> ... -> 1 on the fine mesh, then Q1 on 2:1 coarsened meshes
+ * while every cell count is even and the largest exceeds coarse_cells;
+ * Chebyshev(degree) around Jacobi on [lmax/smoothing_range, 1.2 lmax] with
+ * lmax from eig_iterations power iterations; FP64 Jacobi-CG on the coarsest
+ * level.  precision 32 runs the V-cycle (operators, smoother, transfers) in
+ * FP32, precision 64 in FP64 (double-float operator arithmetic). */
+typedef struct mfgb_mg mfgb_mg;
+typedef struct {
+  int precision;           /* 32 or 64 */
+  int chebyshev_degree;    /* e.g. 5 */
+  double smoothing_range;  /* lambda_max / lambda_min of the smoothing interval, e.g. 15 */
+  int eig_iterations;      /* power iterations for lambda_max, e.g. 20 */
+  int coarse_cells;        /* stop h-coarsening once max(nx,ny,nz) <= coarse_cells, e.g. 4 */
+  double coarse_tol;       /* relative residual of the coarse Jacobi-CG, e.g. 1e-12 */
+} mfgb_mg_params;
+
+mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_params *params, mfgb_mg **mg);
+mfgb_status mfgb_mg_destroy(mfgb_mg *mg);
+/* level sizes (h_* arrays of n_levels entries, any may be NULL) */
+mfgb_status mfgb_mg_info(const mfgb_mg *mg, int *n_levels, int64_t *h_dofs, int *h_degree,
+                         double *h_lmax);
+/* d_dst = M d_src: one V-cycle applied to an FP64 vector */
+mfgb_status mfgb_mg_vmult(mfgb_mg *mg, double *d_dst, const double *d_src, void *stream);
+/* FP64 PCG (SolverCG + ReductionControl semantics) with the V-cycle as the
+   preconditioner; ctl->arith is the arithmetic of the outer operator. */
+mfgb_status mfgb_mg_cg_solve(const mfgb_operator *op, mfgb_mg *mg, const double *d_b, double *d_x,
+                             const mfgb_cg_control *ctl, mfgb_solve_info *info, void *stream);
 
 /* ---- vector kernels used by the solver (exposed for tests) -------------- */
 /* result[0] = sum a_i b_i (deterministic two-stage reduction) */

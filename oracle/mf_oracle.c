@@ -170,8 +170,12 @@ int64_t orc_box_n_cells(const orc_box *b) {
   return (int64_t)b->nx * b->ny * b->nz;
 }
 
+static int geo_degree(const orc_box *b) {
+  return b->geometry_degree > 0 ? b->geometry_degree : b->degree;
+}
+
 void orc_box_cell_nodes(const orc_box *b, int64_t cell, double *xyz) {
-  const int n = b->degree + 1;
+  const int n = geo_degree(b) + 1;
   double xg[16], wg[16];
   orc_gll(n, xg, wg);
   const int64_t cx = cell % b->nx, cy = (cell / b->nx) % b->ny, cz = cell / ((int64_t)b->nx * b->ny);
@@ -273,20 +277,85 @@ int orc_cell_geometry(int n, const double *D, const double *w, const double *xyz
   return bad;
 }
 
+/* Same as orc_cell_geometry with the Jacobian of the Q_{ng-1} geometry
+   interpolant evaluated at the n GLL points per direction:
+   dx/dxi_r (i,j,k) = sum_abc Dv[i][a] V[j][b] V[k][c] x_abc (and cyclic). */
+int orc_cell_geometry_general(int n, int ng, const double *V, const double *Dv, const double *w,
+                              const double *xyz, double *Gc) {
+  const int nq = n * n * n, ng2 = ng * ng;
+  int bad = 0, sign0 = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < n; ++k) {
+        double J[3][3] = {{0}};
+        for (int a = 0; a < ng; ++a)
+          for (int bb = 0; bb < ng; ++bb)
+            for (int c = 0; c < ng; ++c) {
+              const double *x = xyz + 3 * (a * ng2 + bb * ng + c);
+              const double wr = Dv[i * ng + a] * V[j * ng + bb] * V[k * ng + c];
+              const double ws = V[i * ng + a] * Dv[j * ng + bb] * V[k * ng + c];
+              const double wt = V[i * ng + a] * V[j * ng + bb] * Dv[k * ng + c];
+              for (int d = 0; d < 3; ++d) {
+                J[d][0] += wr * x[d];
+                J[d][1] += ws * x[d];
+                J[d][2] += wt * x[d];
+              }
+            }
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const int sg = det > 0 ? 1 : (det < 0 ? -1 : 0);
+        if (sg == 0) bad = 1;
+        if (sign0 == 0) sign0 = sg; else if (sg != sign0) bad = 1;
+        double Ji[3][3];
+        Ji[0][0] = c00 / det;
+        Ji[1][0] = c01 / det;
+        Ji[2][0] = c02 / det;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        const double jxw = fabs(det) * w[i] * w[j] * w[k];
+        const int q = i * n * n + j * n + k;
+        int c = 0;
+        for (int a = 0; a < 3; ++a)
+          for (int bb = a; bb < 3; ++bb) {
+            double s = 0;
+            for (int d = 0; d < 3; ++d) s += Ji[a][d] * Ji[bb][d];
+            Gc[c * nq + q] = jxw * s;
+            ++c;
+          }
+      }
+  return bad;
+}
+
 int64_t orc_box_geometry(const orc_box *b, double *G) {
   const int n = b->degree + 1, nq = n * n * n;
-  double xg[16], wg[16], D[256];
+  const int ng = geo_degree(b) + 1, ngq = ng * ng * ng;
+  double xg[16], wg[16], D[256], xgeo[16], wgeo[16], V[256], Dv[256];
   orc_gll(n, xg, wg);
   orc_derivative_matrix(n, xg, D);
+  orc_gll(ng, xgeo, wgeo);
+  for (int i = 0; i < n; ++i)
+    for (int a = 0; a < ng; ++a) {
+      V[i * ng + a] = orc_lagrange_value(ng, xgeo, a, xg[i]);
+      Dv[i * ng + a] = orc_lagrange_derivative(ng, xgeo, a, xg[i]);
+    }
   const int64_t n_cells = orc_box_n_cells(b);
   int64_t bad = 0;
 #pragma omp parallel reduction(+ : bad)
   {
-    double *xyz = (double *)malloc(sizeof(double) * 3 * nq);
+    double *xyz = (double *)malloc(sizeof(double) * 3 * ngq);
 #pragma omp for schedule(static)
     for (int64_t e = 0; e < n_cells; ++e) {
       orc_box_cell_nodes(b, e, xyz);
-      bad += orc_cell_geometry(n, D, wg, xyz, G + e * 6 * nq);
+      if (ng == n)
+        bad += orc_cell_geometry(n, D, wg, xyz, G + e * 6 * nq);
+      else
+        bad += orc_cell_geometry_general(n, ng, V, Dv, wg, xyz, G + e * 6 * nq);
     }
     free(xyz);
   }

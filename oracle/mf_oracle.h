@@ -46,20 +46,26 @@ typedef struct {
   int degree;         /* p */
   double lo[3], hi[3];/* box corners */
   double amplitude;   /* x_d += a sin(2 pi x) sin(2 pi y) sin(2 pi z) */
+  int geometry_degree;/* Q_g geometry from the deformed GLL nodes of degree g (0: g = degree) */
 } orc_box;
 
 int64_t orc_box_n_dofs(const orc_box *b);
 int64_t orc_box_n_cells(const orc_box *b);
-/* node coordinates of cell e at its n^3 GLL points: xyz[l*3 + d] */
+/* node coordinates of cell e at the (g+1)^3 GLL points of the geometry degree
+   g: xyz[l*3 + d] */
 void orc_box_cell_nodes(const orc_box *b, int64_t cell, double *xyz);
 /* element-to-DoF map (constrained -> ORC_INVALID_DOF) and constrained list.
    Returns the number of constrained DoFs; `constrained` may be NULL. */
 int64_t orc_box_dof_map(const orc_box *b, uint32_t *map, int64_t *constrained);
 /* G[cell][6][n^3] for every cell; returns number of cells with det J <= 0 */
 int64_t orc_box_geometry(const orc_box *b, double *G);
-/* Geometric factors of one cell from its node coordinates. */
+/* Geometric factors of one cell from its node coordinates (same degree). */
 int orc_cell_geometry(int n, const double *D, const double *w,
                       const double *xyz, double *Gcell);
+/* Geometric factors at the n^3 GLL points from geometry nodes of another
+   degree: V[i*ng + a] = l_a(x_i), Dv[i*ng + a] = l_a'(x_i). */
+int orc_cell_geometry_general(int n, int ng, const double *V, const double *Dv,
+                              const double *w, const double *xyz, double *Gcell);
 
 /* ---- operator ------------------------------------------------------------ */
 /* E-vector BK5: out_e = D^T G_e D in_e for every element (no gather) */

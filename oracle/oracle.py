@@ -41,7 +41,7 @@ class _Box(ctypes.Structure):
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
         ("degree", ctypes.c_int),
         ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
-        ("amplitude", ctypes.c_double),
+        ("amplitude", ctypes.c_double), ("geometry_degree", ctypes.c_int),
     ]
 
 
@@ -160,11 +160,12 @@ class BoxProblem:
     amplitude: float = 0.05
     lo: tuple = (0.0, 0.0, 0.0)
     hi: tuple = (1.0, 1.0, 1.0)
+    geometry_degree: int = 0
 
     def __post_init__(self):
         self._box = _Box(self.nx, self.ny, self.nz, self.degree,
                          (ctypes.c_double * 3)(*self.lo), (ctypes.c_double * 3)(*self.hi),
-                         self.amplitude)
+                         self.amplitude, self.geometry_degree)
         L = lib()
         self.n = self.degree + 1
         self.n_dofs = int(L.orc_box_n_dofs(ctypes.byref(self._box)))
@@ -180,7 +181,8 @@ class BoxProblem:
         self.D = derivative_matrix(x)
 
     def cell_nodes(self, cell: int) -> np.ndarray:
-        xyz = np.zeros(self.n ** 3 * 3)
+        ng = (self.geometry_degree or self.degree) + 1
+        xyz = np.zeros(ng ** 3 * 3)
         lib().orc_box_cell_nodes(ctypes.byref(self._box), cell, _p(xyz))
         return xyz.reshape(-1, 3)
 
