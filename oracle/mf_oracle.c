@@ -471,6 +471,192 @@ void orc_invert_diagonal(int64_t n, double *d) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Gauss-quadrature operator (BP5-variant q = p+1, BP3 q = p+2)               */
+/* ------------------------------------------------------------------------ */
+
+void orc_gauss_basis_matrices(int p, int nq, double *B, double *DG) {
+  const int n = p + 1;
+  double xg[16], wg[16], xq[16], wq[16];
+  orc_gll(n, xg, wg);
+  orc_gauss(nq, xq, wq);
+  for (int q = 0; q < nq; ++q)
+    for (int i = 0; i < n; ++i) B[q * n + i] = orc_lagrange_value(n, xg, i, xq[q]);
+  orc_derivative_matrix(nq, xq, DG);
+}
+
+int64_t orc_box_geometry_gauss(const orc_box *b, int nq, double *Gg) {
+  const int ng = geo_degree(b) + 1, ngq = ng * ng * ng, nq3 = nq * nq * nq;
+  double xgeo[16], wgeo[16], xq[16], wq[16], V[256], Dv[256];
+  orc_gll(ng, xgeo, wgeo);
+  orc_gauss(nq, xq, wq);
+  for (int i = 0; i < nq; ++i)
+    for (int a = 0; a < ng; ++a) {
+      V[i * ng + a] = orc_lagrange_value(ng, xgeo, a, xq[i]);
+      Dv[i * ng + a] = orc_lagrange_derivative(ng, xgeo, a, xq[i]);
+    }
+  const int64_t n_cells = orc_box_n_cells(b);
+  int64_t bad = 0;
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *xyz = (double *)malloc(sizeof(double) * 3 * ngq);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < n_cells; ++e) {
+      orc_box_cell_nodes(b, e, xyz);
+      bad += orc_cell_geometry_general(nq, ng, V, Dv, wq, xyz, Gg + e * 6 * nq3);
+    }
+    free(xyz);
+  }
+  return bad;
+}
+
+/* apply the 1D matrix M (rows x cols, M[r*cols + c]) along one direction of a
+   tensor t[a][b][c] with extents (e0, e1, e2); dir 0 contracts a, 2 contracts c;
+   transpose uses M^T */
+static void contract(const double *M, int rows, int cols, int dir, int transpose, const int *ext,
+                     const double *in, double *out) {
+  const int e0 = ext[0], e1 = ext[1], e2 = ext[2];
+  const int nin = transpose ? rows : cols, nout = transpose ? cols : rows;
+  const int o0 = dir == 0 ? nout : e0, o1 = dir == 1 ? nout : e1, o2 = dir == 2 ? nout : e2;
+  for (int a = 0; a < o0; ++a)
+    for (int bb = 0; bb < o1; ++bb)
+      for (int c = 0; c < o2; ++c) {
+        double s = 0;
+        for (int m = 0; m < nin; ++m) {
+          const double w = transpose ? M[m * cols + (dir == 0 ? a : dir == 1 ? bb : c)]
+                                     : M[(dir == 0 ? a : dir == 1 ? bb : c) * cols + m];
+          const int ia = dir == 0 ? m : a, ib = dir == 1 ? m : bb, ic = dir == 2 ? m : c;
+          s += w * in[(ia * e1 + ib) * e2 + ic];
+        }
+        out[(a * o1 + bb) * o2 + c] = s;
+      }
+}
+
+/* one cell: y = B^T D_G^T G D_G B u  (u, y: n^3 GLL nodal values) */
+static void bk5g_element(int n, int nq, const double *B, const double *DG, const double *G,
+                         const double *u, double *y, double *w) {
+  const int nq3 = nq * nq * nq;
+  double *t1 = w, *t2 = w + nq3, *uq = w + 2 * nq3, *vr = w + 3 * nq3, *vs = w + 4 * nq3,
+         *vt = w + 5 * nq3, *acc = w + 6 * nq3, *t3 = w + 7 * nq3;
+  int e_nnn[3] = {n, n, n}, e_qnn[3] = {nq, n, n}, e_qqn[3] = {nq, nq, n}, e_qqq[3] = {nq, nq, nq};
+  /* values at the Gauss points */
+  contract(B, nq, n, 0, 0, e_nnn, u, t1);
+  contract(B, nq, n, 1, 0, e_qnn, t1, t2);
+  contract(B, nq, n, 2, 0, e_qqn, t2, uq);
+  /* collocation gradient, metric */
+  contract(DG, nq, nq, 0, 0, e_qqq, uq, t1);
+  contract(DG, nq, nq, 1, 0, e_qqq, uq, t2);
+  contract(DG, nq, nq, 2, 0, e_qqq, uq, t3);
+  for (int q = 0; q < nq3; ++q) {
+    const double qr = t1[q], qs = t2[q], qt = t3[q];
+    const double grr = G[0 * nq3 + q], grs = G[1 * nq3 + q], grt = G[2 * nq3 + q];
+    const double gss = G[3 * nq3 + q], gst = G[4 * nq3 + q], gtt = G[5 * nq3 + q];
+    vr[q] = grr * qr + grs * qs + grt * qt;
+    vs[q] = grs * qr + gss * qs + gst * qt;
+    vt[q] = grt * qr + gst * qs + gtt * qt;
+  }
+  /* transpose gradient */
+  contract(DG, nq, nq, 0, 1, e_qqq, vr, acc);
+  contract(DG, nq, nq, 1, 1, e_qqq, vs, t1);
+  for (int q = 0; q < nq3; ++q) acc[q] += t1[q];
+  contract(DG, nq, nq, 2, 1, e_qqq, vt, t1);
+  for (int q = 0; q < nq3; ++q) acc[q] += t1[q];
+  /* back to the GLL nodal values */
+  int e_qqq2[3] = {nq, nq, nq}, e_qqn2[3] = {nq, nq, n}, e_qnn2[3] = {nq, n, n};
+  contract(B, nq, n, 2, 1, e_qqq2, acc, t2);
+  contract(B, nq, n, 1, 1, e_qqn2, t2, t1);
+  contract(B, nq, n, 0, 1, e_qnn2, t1, y);
+}
+
+void orc_bk5g_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                    const uint32_t *map, const double *Gg, int64_t n_dofs, int64_t n_constrained,
+                    const int64_t *constrained, const double *src, double *dst) {
+  const int n3 = n * n * n, nq3 = nq * nq * nq;
+  memset(dst, 0, sizeof(double) * n_dofs);
+#pragma omp parallel
+  {
+    double *u = (double *)malloc(sizeof(double) * (2 * n3 + 8 * nq3));
+    double *y = u + n3, *w = u + 2 * n3;
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < n_cells; ++e) {
+      const uint32_t *me = map + e * n3;
+      for (int l = 0; l < n3; ++l) u[l] = me[l] == ORC_INVALID_DOF ? 0.0 : src[me[l]];
+      bk5g_element(n, nq, B, DG, Gg + e * 6 * nq3, u, y, w);
+      for (int l = 0; l < n3; ++l)
+        if (me[l] != ORC_INVALID_DOF) {
+#pragma omp atomic
+          dst[me[l]] += y[l];
+        }
+    }
+    free(u);
+  }
+  for (int64_t c = 0; c < n_constrained; ++c) dst[constrained[c]] = src[constrained[c]];
+}
+
+void orc_box_rhs_unit_gauss(const orc_box *b, int nq, int64_t n_constrained,
+                            const int64_t *constrained, double *rhs) {
+  const int n = b->degree + 1, n3 = n * n * n, nq3 = nq * nq * nq;
+  const int64_t n_cells = orc_box_n_cells(b), N = orc_box_n_dofs(b);
+  double *Gg = (double *)malloc(sizeof(double) * 6 * nq3 * n_cells);
+  double *jxw = (double *)malloc(sizeof(double) * nq3 * n_cells);
+  uint32_t *map = (uint32_t *)malloc(sizeof(uint32_t) * n3 * n_cells);
+  /* JxW at the Gauss points: recompute det J from the geometry (Gg holds G) */
+  const int ng = geo_degree(b) + 1;
+  double xgeo[16], wgeo[16], xq[16], wq[16], V[256], Dv[256], xgl[16], wgl[16], B[256];
+  orc_gll(ng, xgeo, wgeo);
+  orc_gauss(nq, xq, wq);
+  orc_gll(n, xgl, wgl);
+  for (int i = 0; i < nq; ++i) {
+    for (int a = 0; a < ng; ++a) {
+      V[i * ng + a] = orc_lagrange_value(ng, xgeo, a, xq[i]);
+      Dv[i * ng + a] = orc_lagrange_derivative(ng, xgeo, a, xq[i]);
+    }
+    for (int a = 0; a < n; ++a) B[i * n + a] = orc_lagrange_value(n, xgl, a, xq[i]);
+  }
+  orc_box_dof_map(b, map, NULL);
+  memset(rhs, 0, sizeof(double) * N);
+  double *xyz = (double *)malloc(sizeof(double) * 3 * ng * ng * ng);
+  for (int64_t e = 0; e < n_cells; ++e) {
+    orc_box_cell_nodes(b, e, xyz);
+    for (int p = 0; p < nq; ++p)
+      for (int q = 0; q < nq; ++q)
+        for (int r = 0; r < nq; ++r) {
+          double J[3][3] = {{0}};
+          for (int a = 0; a < ng; ++a)
+            for (int bb = 0; bb < ng; ++bb)
+              for (int c = 0; c < ng; ++c) {
+                const double *x = xyz + 3 * ((a * ng + bb) * ng + c);
+                const double wr = Dv[p * ng + a] * V[q * ng + bb] * V[r * ng + c];
+                const double ws = V[p * ng + a] * Dv[q * ng + bb] * V[r * ng + c];
+                const double wt = V[p * ng + a] * V[q * ng + bb] * Dv[r * ng + c];
+                for (int d = 0; d < 3; ++d) {
+                  J[d][0] += wr * x[d];
+                  J[d][1] += ws * x[d];
+                  J[d][2] += wt * x[d];
+                }
+              }
+          const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                             J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                             J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+          jxw[e * nq3 + (p * nq + q) * nq + r] = fabs(det) * wq[p] * wq[q] * wq[r];
+        }
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        for (int k = 0; k < n; ++k) {
+          const uint32_t dof = map[e * n3 + (i * n + j) * n + k];
+          if (dof == ORC_INVALID_DOF) continue;
+          double s = 0;
+          for (int p = 0; p < nq; ++p)
+            for (int q = 0; q < nq; ++q)
+              for (int r = 0; r < nq; ++r)
+                s += B[p * n + i] * B[q * n + j] * B[r * n + k] * jxw[e * nq3 + (p * nq + q) * nq + r];
+          rhs[dof] += s;
+        }
+  }
+  for (int64_t c = 0; c < n_constrained; ++c) rhs[constrained[c]] = 0.0;
+  free(xyz); free(map); free(jxw); free(Gg);
+}
+
+/* ------------------------------------------------------------------------ */
 /* MT19937-64 (Matsumoto & Nishimura, 2000/2004 published algorithm)        */
 /* ------------------------------------------------------------------------ */
 typedef struct {
@@ -535,10 +721,9 @@ static double dot(int64_t n, const double *a, const double *b) {
   return s;
 }
 
-orc_solve_info orc_cg_solve(int n, int64_t n_cells, const uint32_t *map, const double *D,
-                            const double *G, int64_t N, int64_t n_constrained,
-                            const int64_t *constrained, const double *diag_inv,
-                            const double *b, double *x, orc_reduction_control ctl) {
+orc_solve_info orc_cg_solve_op(orc_apply_fn apply, void *ctx, int64_t N,
+                               const double *diag_inv, const double *b, double *x,
+                               orc_reduction_control ctl) {
   orc_solve_info info = {0, 0.0, 0.0, 0};
   double *r = (double *)malloc(sizeof(double) * N);
   double *z = (double *)malloc(sizeof(double) * N);
@@ -546,7 +731,7 @@ orc_solve_info orc_cg_solve(int n, int64_t n_cells, const uint32_t *map, const d
   double *v = (double *)malloc(sizeof(double) * N);
 
   /* r = b - A x */
-  orc_bk5_apply(n, n_cells, map, D, G, N, n_constrained, constrained, x, v);
+  apply(ctx, x, v);
   for (int64_t i = 0; i < N; ++i) r[i] = b[i] - v[i];
   double res = sqrt(dot(N, r, r));
   info.initial = res;
@@ -561,7 +746,7 @@ orc_solve_info orc_cg_solve(int n, int64_t n_cells, const uint32_t *map, const d
   double rz = dot(N, r, z);
 
   for (int it = 1;; ++it) {
-    orc_bk5_apply(n, n_cells, map, D, G, N, n_constrained, constrained, p, v);
+    apply(ctx, p, v);
     const double alpha = rz / dot(N, p, v);
     for (int64_t i = 0; i < N; ++i) {
       x[i] += alpha * p[i];
@@ -581,4 +766,48 @@ orc_solve_info orc_cg_solve(int n, int64_t n_cells, const uint32_t *map, const d
 done:
   free(r); free(z); free(p); free(v);
   return info;
+}
+
+typedef struct {
+  int n;
+  int64_t n_cells, N, nc;
+  const uint32_t *map;
+  const double *D, *G;
+  const int64_t *c;
+} gll_ctx;
+
+static void gll_apply(void *vc, const double *src, double *dst) {
+  gll_ctx *c = (gll_ctx *)vc;
+  orc_bk5_apply(c->n, c->n_cells, c->map, c->D, c->G, c->N, c->nc, c->c, src, dst);
+}
+
+orc_solve_info orc_cg_solve(int n, int64_t n_cells, const uint32_t *map, const double *D,
+                            const double *G, int64_t N, int64_t n_constrained,
+                            const int64_t *constrained, const double *diag_inv,
+                            const double *b, double *x, orc_reduction_control ctl) {
+  gll_ctx c = {n, n_cells, N, n_constrained, map, D, G, constrained};
+  return orc_cg_solve_op(gll_apply, &c, N, diag_inv, b, x, ctl);
+}
+
+typedef struct {
+  int n, nq;
+  const double *B, *DG;
+  int64_t n_cells, N, nc;
+  const uint32_t *map;
+  const double *G;
+  const int64_t *c;
+} gauss_ctx;
+
+static void gauss_apply(void *vc, const double *src, double *dst) {
+  gauss_ctx *c = (gauss_ctx *)vc;
+  orc_bk5g_apply(c->n, c->nq, c->B, c->DG, c->n_cells, c->map, c->G, c->N, c->nc, c->c, src, dst);
+}
+
+orc_solve_info orc_cg_solve_gauss(int n, int nq, const double *B, const double *DG,
+                                  int64_t n_cells, const uint32_t *map, const double *Gg,
+                                  int64_t N, int64_t n_constrained, const int64_t *constrained,
+                                  const double *diag_inv, const double *b, double *x,
+                                  orc_reduction_control ctl) {
+  gauss_ctx c = {n, nq, B, DG, n_cells, N, n_constrained, map, Gg, constrained};
+  return orc_cg_solve_op(gauss_apply, &c, N, diag_inv, b, x, ctl);
 }

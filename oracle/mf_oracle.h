@@ -82,6 +82,30 @@ void orc_bk5_diagonal(int n, int64_t n_cells, const uint32_t *map, const double 
 /* diag -> inverse with the d <= 0 -> 1 guard */
 void orc_invert_diagonal(int64_t n, double *d);
 
+/* ---- Gauss-quadrature (BP5-variant / BP3) operator ------------------------
+ * The deal.II-kernel form of the reference
+ * (bakeoff_problems_dealii/include/bk3_kokkos_kernel.h:156-228 interpolate GLL
+ * nodal values to nq Gauss points per direction, :230-302 collocation gradient
+ * at the Gauss points and metric apply, :305-334 transpose, :340-404
+ * interpolate back).  B[q*n + i] = l_i(g_q) (GLL basis at Gauss points),
+ * DG[q*nq + m] = L_m'(g_q) (Lagrange basis on the Gauss points);
+ * Gg[cell][6][nq^3] from orc_box_geometry_gauss. */
+typedef struct {
+  int n, nq;                 /* GLL points, Gauss points per direction */
+  const double *B, *DG;
+} orc_gauss_basis;
+/* B, DG (n <= 9, nq <= 10) for degree p and nq Gauss points */
+void orc_gauss_basis_matrices(int p, int nq, double *B, double *DG);
+/* G at the nq^3 Gauss points (Gauss weights) of every box cell */
+int64_t orc_box_geometry_gauss(const orc_box *b, int nq, double *Gg);
+/* b_i = int phi_i f dx, f = 1, by the nq-point Gauss rule; 0 on constrained */
+void orc_box_rhs_unit_gauss(const orc_box *b, int nq, int64_t n_constrained,
+                            const int64_t *constrained, double *rhs);
+void orc_bk5g_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                    const uint32_t *map, const double *Gg, int64_t n_dofs,
+                    int64_t n_constrained, const int64_t *constrained, const double *src,
+                    double *dst);
+
 /* ---- right-hand side ----------------------------------------------------- */
 uint64_t orc_mt19937_64_nth(uint64_t seed, int64_t nth);
 void orc_rhs_uniform(uint64_t seed, int64_t n_dofs, int64_t n_constrained,
@@ -100,6 +124,18 @@ typedef struct {
   double last;        /* last_value() */
   int converged;      /* 1 = success, 0 = failure (max steps / NaN) */
 } orc_solve_info;
+
+/* CG on any operator given as a callback (dst = A src) */
+typedef void (*orc_apply_fn)(void *ctx, const double *src, double *dst);
+orc_solve_info orc_cg_solve_op(orc_apply_fn apply, void *ctx, int64_t n_dofs,
+                               const double *diag_inv, const double *b, double *x,
+                               orc_reduction_control ctl);
+/* CG on the Gauss-quadrature operator (PreconditionIdentity if diag_inv NULL) */
+orc_solve_info orc_cg_solve_gauss(int n, int nq, const double *B, const double *DG,
+                                  int64_t n_cells, const uint32_t *map, const double *Gg,
+                                  int64_t n_dofs, int64_t n_constrained,
+                                  const int64_t *constrained, const double *diag_inv,
+                                  const double *b, double *x, orc_reduction_control ctl);
 
 /* Jacobi- (diag_inv != NULL) or identity-preconditioned CG on the BK5 operator */
 orc_solve_info orc_cg_solve(int n, int64_t n_cells, const uint32_t *map,

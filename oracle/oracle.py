@@ -258,3 +258,80 @@ def cg_solve(n, dof_map, D, G, n_dofs, constrained, diag_inv, b, max_steps=10000
 
 def num_threads() -> int:
     return int(lib().orc_num_threads())
+
+
+# ---- Gauss-quadrature (BP5-variant / BP3) operator --------------------------
+def _gauss_sigs():
+    L = lib()
+    if getattr(L, "_gauss_ready", False):
+        return L
+    P, i64 = ctypes.c_void_p, ctypes.c_int64
+    L.orc_gauss_basis_matrices.argtypes = [ctypes.c_int, ctypes.c_int, P, P]
+    L.orc_box_geometry_gauss.argtypes = [ctypes.POINTER(_Box), ctypes.c_int, P]
+    L.orc_box_geometry_gauss.restype = i64
+    L.orc_box_rhs_unit_gauss.argtypes = [ctypes.POINTER(_Box), ctypes.c_int, i64, P, P]
+    L.orc_bk5g_apply.argtypes = [ctypes.c_int, ctypes.c_int, P, P, i64, P, P, i64, i64, P, P, P]
+    L.orc_cg_solve_gauss.argtypes = [ctypes.c_int, ctypes.c_int, P, P, i64, P, P, i64, i64, P, P,
+                                     P, P, _Ctl]
+    L.orc_cg_solve_gauss.restype = _Info
+    L._gauss_ready = True
+    return L
+
+
+class GaussProblem(BoxProblem):
+    """The box problem discretised with nq Gauss points per direction and
+    interpolation from the GLL nodal values (the deal.II-kernel form of the
+    reference's BP5 variant, nq = p + 1, or BP3, nq = p + 2)."""
+
+    def __init__(self, nx, ny, nz, degree, nq=None, amplitude=0.0, lo=(0.0, 0.0, 0.0),
+                 hi=(1.0, 1.0, 1.0), geometry_degree=0):
+        super().__init__(nx, ny, nz, degree, amplitude, lo, hi, geometry_degree)
+        L = _gauss_sigs()
+        self.nq = nq or degree + 1
+        n, q = self.n, self.nq
+        self.B = np.zeros((q, n))
+        self.DG = np.zeros((q, q))
+        L.orc_gauss_basis_matrices(self.degree, q, _p(self.B), _p(self.DG))
+        self.Gg = np.zeros(self.n_cells * 6 * q ** 3)
+        self.n_bad_cells_gauss = int(L.orc_box_geometry_gauss(ctypes.byref(self._box), q,
+                                                              _p(self.Gg)))
+
+    def apply(self, src):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        dst = np.zeros(self.n_dofs)
+        _gauss_sigs().orc_bk5g_apply(self.n, self.nq, _p(self.B), _p(self.DG), self.n_cells,
+                                     _p(self.map), _p(self.Gg), self.n_dofs,
+                                     self.constrained.size, _p(self.constrained), _p(src),
+                                     _p(dst))
+        return dst
+
+    def rhs_unit(self):
+        b = np.zeros(self.n_dofs)
+        _gauss_sigs().orc_box_rhs_unit_gauss(ctypes.byref(self._box), self.nq,
+                                             self.constrained.size, _p(self.constrained), _p(b))
+        return b
+
+    def cg(self, b, diag_inv=None, max_steps=1000000000, tol=1e-16, reduce=1e-9, x0=None):
+        x = np.zeros(self.n_dofs) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        info = _gauss_sigs().orc_cg_solve_gauss(
+            self.n, self.nq, _p(self.B), _p(self.DG), self.n_cells, _p(self.map), _p(self.Gg),
+            self.n_dofs, self.constrained.size, _p(self.constrained),
+            _p(diag_inv) if diag_inv is not None else None, _p(b), _p(x),
+            _Ctl(min(max_steps, 2**31 - 1), tol, reduce))
+        return x, {"steps": info.steps, "initial": info.initial, "last": info.last,
+                   "converged": bool(info.converged)}
+
+
+def reference_scaling_mesh(cycle: int, degree: int):
+    """The mesh of cycle `cycle` of the reference's BP5-variant scaling study
+    (bakeoff_problems_dealii/tests/scaling_bp35_kokkos_kernel/program.cc:451-487):
+    n_refine = cycle // 3, the first (cycle % 3) directions span [-1, 2.8] with
+    two coarse cells, the others [-1, 0.9] with one, refined n_refine times."""
+    n_refine, rem = cycle // 3, cycle % 3
+    cells, hi = [], []
+    for d in range(3):
+        sub = 2 if d < rem else 1
+        cells.append(sub << n_refine)
+        hi.append(2.8 if d < rem else 0.9)
+    return cells, (-1.0, -1.0, -1.0), tuple(hi)

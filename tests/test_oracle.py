@@ -175,3 +175,44 @@ def test_cg_converges_and_counts(orc):
     assert infoj["converged"] and infoj["steps"] <= info["steps"]
     x2, info2 = prob.cg(b, reduce=1e-8, max_steps=3)
     assert not info2["converged"] and info2["steps"] == 3
+
+
+def test_published_bp5_cg_counts(orc):
+    """The reference's published BP5-variant CG runs (FE_Q(4), QGauss(5),
+    f = 1, identity preconditioner, ReductionControl(1e9, 1e-16, 1e-9)):
+    identical iteration counts and cg_reduction on cycles 8..12
+    (bakeoff_problems_dealii/tests/scaling_bp35_kokkos_kernel/results/1_GPU.out:640-644)."""
+    import json
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "published_bp5_cg.json")
+    rows = {r["dofs"]: r for r in json.load(open(path))["rows"]}
+    for cycle in range(8, 13):
+        cells, lo, hi = orc.reference_scaling_mesh(cycle, 4)
+        P = orc.GaussProblem(*cells, 4, lo=lo, hi=hi)
+        pub = rows[P.n_dofs]
+        assert P.n_cells == pub["cells"]
+        _, info = P.cg(P.rhs_unit())
+        assert info["steps"] == pub["cg_its"]
+        red = (info["last"] / info["initial"]) ** (1.0 / info["steps"])
+        assert f"{red:.3e}" == f"{pub['cg_reduction']:.3e}"
+
+
+def test_gauss_operator_is_exact_stiffness_on_affine_cells(orc):
+    """With nq = p + 1 Gauss points the operator on an affine cube equals the
+    exactly integrated stiffness matrix: its energy of a polynomial of degree
+    <= p is the exact Dirichlet integral."""
+    P = orc.GaussProblem(2, 2, 2, 3, lo=(0, 0, 0), hi=(1, 1, 1))
+    # u = x y z (1-x)(1-y)(1-z)-like interior polynomial sampled at the nodes is
+    # not degree 3 per direction; use u = x(1-x) y(1-y) z(1-z), degree 2 each
+    xyz = np.zeros((P.n_dofs, 3))
+    for e in range(P.n_cells):
+        nodes = P.cell_nodes(e)
+        m = P.map[e * 64:(e + 1) * 64]
+        valid = m != orc.INVALID_DOF
+        xyz[m[valid].astype(np.int64)] = nodes[valid]
+    x, y, z = xyz.T
+    u = x * (1 - x) * y * (1 - y) * z * (1 - z)
+    u[P.constrained] = 0.0
+    energy = u @ P.apply(u)
+    # exact: integral |grad u|^2 = 3 * (1/3) * (1/30)^2
+    assert abs(energy - 3 * (1 / 3) * (1 / 30) ** 2) <= 1e-13
