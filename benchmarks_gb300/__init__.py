@@ -95,12 +95,17 @@ class LaplaceOperator:
     default; both meet 1e-12 relative to the FP64 oracle)."""
 
     def __init__(self, mesh: BoxMesh | None = None, *, degree=None, n_dofs=None, dof_map=None,
-                 G=None, constrained=None, arith="df"):
+                 G=None, constrained=None, arith="df", quadrature="gll"):
         L = lib()
         self._op = ctypes.c_void_p()
+        if quadrature not in ("gll", "gauss"):
+            raise ValueError("quadrature must be 'gll' (collocation) or 'gauss' (BP5 variant)")
+        self.quadrature = quadrature
         if mesh is not None:
             desc = mesh._desc()
-            _abi.check(L.mfgb_operator_create_box(ctypes.byref(desc), ctypes.byref(self._op)))
+            create = (L.mfgb_operator_create_box if quadrature == "gll"
+                      else L.mfgb_operator_create_box_gauss)
+            _abi.check(create(ctypes.byref(desc), ctypes.byref(self._op)))
             self.mesh = mesh
         else:
             import numpy as np

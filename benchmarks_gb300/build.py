@@ -23,6 +23,7 @@ SOURCES = [
     "mfgb_bk5_f64.cu",
     "mfgb_bk5_df.cu",
     "mfgb_bk5_f32.cu",
+    "mfgb_bk5g.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -54,6 +55,27 @@ def _compile(src: str, extra) -> str:
     return obj
 
 
+EXAMPLE = os.path.join(BUILD, "bp5_solve")
+
+
+def build_example() -> str:
+    """Compile the C++ example driver (header-only adapter over the C ABI)."""
+    src = os.path.join(HERE, "examples", "bp5_solve.cc")
+    hdrs = [os.path.join(ROOT, "include", h) for h in ("mfgb.h", "mfgb_operator.hpp")]
+    if os.path.exists(EXAMPLE) and all(os.path.getmtime(EXAMPLE) >= os.path.getmtime(d)
+                                       for d in [src, LIB, *hdrs]):
+        return EXAMPLE
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(cuda, "include"), src, "-o", EXAMPLE, "-L" + HERE, "-lmfgb",
+           "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + HERE,
+           "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"example build failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    return EXAMPLE
+
+
 def build(verbose: bool = False, extra=()) -> str:
     os.makedirs(BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
@@ -67,6 +89,12 @@ def build(verbose: bool = False, extra=()) -> str:
     if verbose:
         print("built", LIB)
     return LIB
+
+
+def build_all(verbose: bool = False) -> str:
+    lib = build(verbose)
+    build_example()
+    return lib
 
 
 if __name__ == "__main__":

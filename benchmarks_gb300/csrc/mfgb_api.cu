@@ -57,10 +57,18 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
     return st;
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64) {
-    e = bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s, done);
+    e = op->quadrature
+            ? bk5g_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->DG, op->Bq, partials,
+                       grid, s, done)
+            : bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s,
+                      done);
   } else if (arith == MFGB_ARITH_FP64_DF) {
     if ((st = ensure_df(op))) return st;
-    e = bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s, done);
+    e = op->quadrature
+            ? bk5g_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->DG, op->Bq, partials,
+                      grid, s, done)
+            : bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s,
+                     done);
   } else {
     set_error("vmult: unknown arith mode");
     return MFGB_ERR_INVALID_ARG;
@@ -184,7 +192,17 @@ mfgb_status mfgb_get_kernel_shape(int arith, int degree, int *shape) {
   return MFGB_OK;
 }
 
+static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out);
+
 mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **out) {
+  return create_box_impl(box, 0, out);
+}
+
+mfgb_status mfgb_operator_create_box_gauss(const mfgb_box_desc *box, mfgb_operator **out) {
+  return create_box_impl(box, 1, out);
+}
+
+static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out) {
   if (!box || !out) {
     set_error("mfgb_operator_create_box: null argument");
     return MFGB_ERR_INVALID_ARG;
@@ -205,6 +223,14 @@ mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **o
   }
   mfgb_operator *op = new mfgb_operator();
   init_basis(op, box->degree);
+  op->quadrature = quadrature;
+  if (quadrature) {  // Gauss points = GLL count (BP5 variant, q = p + 1)
+    double xq[9], wq[9];
+    gauss_nodes(op->n, xq, wq);
+    derivative_matrix(op->n, xq, op->DG);
+    for (int q = 0; q < op->n; ++q)
+      for (int i = 0; i < op->n; ++i) op->Bq[q * op->n + i] = lagrange_value(op->n, op->gll_x, i, xq[q]);
+  }
   op->is_box = true;
   op->box = *box;
   op->n_dofs = n_dofs;
@@ -235,7 +261,8 @@ mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **o
                                    cudaMemcpyHostToDevice),
                         "constraints copy")) ||
       (st = cuda_status(box_map(*box, op->d_map, nullptr), "box map")) ||
-      (st = cuda_status(box_geometry(*box, op->gll_x, op->gll_w, op->D, op->d_G, nullptr),
+      (st = cuda_status(box_geometry(*box, op->gll_x, op->gll_w, op->D, op->d_G, nullptr,
+                                     quadrature != 0),
                         "box geometry")) ||
       (st = cuda_status(cudaDeviceSynchronize(), "box set-up"))) {
     free_operator(op);
@@ -363,10 +390,16 @@ mfgb_status mfgb_vmult_add(const mfgb_operator *op, double *d_dst, const double 
   cudaError_t e;
   mfgb_status st;
   if (arith == MFGB_ARITH_FP64) {
-    e = bk5_f64(o->n, o->n_cells, o->d_map, o->d_G, d_src, d_dst, o->D, nullptr, nullptr, s);
+    e = o->quadrature ? bk5g_f64(o->n, o->n_cells, o->d_map, o->d_G, d_src, d_dst, o->DG, o->Bq,
+                                 nullptr, nullptr, s)
+                      : bk5_f64(o->n, o->n_cells, o->d_map, o->d_G, d_src, d_dst, o->D, nullptr,
+                                nullptr, s);
   } else if (arith == MFGB_ARITH_FP64_DF) {
     if ((st = ensure_df(o))) return st;
-    e = bk5_df(o->n, o->n_cells, o->d_map, o->d_Gdf, d_src, d_dst, o->D, nullptr, nullptr, s);
+    e = o->quadrature ? bk5g_df(o->n, o->n_cells, o->d_map, o->d_Gdf, d_src, d_dst, o->DG, o->Bq,
+                                nullptr, nullptr, s)
+                      : bk5_df(o->n, o->n_cells, o->d_map, o->d_Gdf, d_src, d_dst, o->D, nullptr,
+                               nullptr, s);
   } else {
     set_error("mfgb_vmult_add: unknown arith mode");
     return MFGB_ERR_INVALID_ARG;
@@ -444,6 +477,10 @@ mfgb_status mfgb_compute_diagonal(const mfgb_operator *op, double *d_diag, void 
   if (!op || (op->n_dofs > 0 && !d_diag)) {
     set_error("mfgb_compute_diagonal: invalid argument");
     return MFGB_ERR_INVALID_ARG;
+  }
+  if (op->quadrature) {
+    set_error("mfgb_compute_diagonal: the Gauss-quadrature form has no diagonal kernel");
+    return MFGB_ERR_UNSUPPORTED;
   }
   cudaStream_t s = (cudaStream_t)stream;
   mfgb_status st;

@@ -492,3 +492,191 @@ __global__ void __launch_bounds__(E * N * N, TmaMinBlocks<N>::value)
 }
 
 }  // namespace mfgb
+
+namespace mfgb {
+
+// Gauss-quadrature form (BP5 variant, nq = p + 1 Gauss points per direction):
+// the deal.II-kernel form of the reference's L-vector kernel
+// (bakeoff_problems_dealii/include/bk3_kokkos_kernel.h:156-228 interpolate to
+// the Gauss points, :230-302 collocation gradient + metric, :305-334 transpose,
+// :340-404 interpolate back, :406-426 scatter).  Column layout as bk5_kernel;
+// basis.D is the collocation derivative on the Gauss points, B the GLL basis
+// at the Gauss points, B[q*N + i] = l_i(g_q).
+template <int N, class A>
+struct BasisG {
+  typename A::V D[N * N];
+  typename A::V B[N * N];
+};
+
+template <int N, int E, class A, bool WITH_ENERGY>
+__global__ void __launch_bounds__(E * N * N)
+    bk5g_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+                typename A::VecT *__restrict__ dst, const BasisG<N, A> basis,
+                double *__restrict__ energy_partials, const int *__restrict__ done_flag) {
+  if (done_flag != nullptr && *done_flag) return;
+  using V = typename A::V;
+  using Acc = typename A::Acc;
+  using VT = typename A::VecT;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  __shared__ V s_a[E * N3];
+  __shared__ V s_b[E * N3];
+  __shared__ V s_c[E * N3];
+
+  const int tid = threadIdx.x;
+  const int el = tid / N2;
+  const int jk = tid - el * N2;
+  const int j = jk / N;
+  const int k = jk - j * N;
+  V Dj[N], Dk[N], Dtj[N], Dtk[N];
+#pragma unroll
+  for (int m = 0; m < N; ++m) {
+    Dj[m] = basis.D[j * N + m];
+    Dk[m] = basis.D[k * N + m];
+    Dtj[m] = basis.D[m * N + j];
+    Dtk[m] = basis.D[m * N + k];
+  }
+  V *sa = s_a + el * N3, *sb = s_b + el * N3, *sc = s_c + el * N3;
+  double energy = 0.0;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  for (int64_t batch = blockIdx.x; batch < n_batches; batch += gridDim.x) {
+    const int64_t cell = batch * E + el;
+    const bool valid = cell < n_cells;
+    uint32_t idx[N];
+    VT raw[N];
+    V u[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      idx[i] = valid ? __ldg(map + cell * N3 + i * N2 + jk) : MFGB_INVALID_DOF;
+      raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + idx[i]) : VT(0);
+      u[i] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(raw[i]) : A::zero_v();
+      sa[i * N2 + jk] = u[i];
+    }
+    __syncthreads();
+    // ---- interpolate to the Gauss points: along k, j (shared), i (registers)
+    V t[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[k * N + m], sa[i * N2 + j * N + m]);
+      t[i] = A::finish(a);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) sb[i * N2 + jk] = t[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[j * N + m], sb[i * N2 + m * N + k]);
+      t[i] = A::finish(a);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[i * N + m], t[m]);
+      u[i] = A::finish(a);
+      sa[i * N2 + jk] = u[i];
+    }
+    __syncthreads();
+    // ---- collocation gradient at the Gauss points + metric
+    V vr[N];
+    const typename A::GType *Gc = G + (valid ? cell : 0) * 6 * N3 + jk;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc ar, as, at;
+      A::zero(ar);
+      A::zero(as);
+      A::zero(at);
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        A::fma(ar, basis.D[i * N + m], u[m]);
+        A::fma(as, Dj[m], sa[i * N2 + m * N + k]);
+        A::fma(at, Dk[m], sa[i * N2 + j * N + m]);
+      }
+      const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+      const V grr = A::load_g(__ldg(Gc + 0 * N3 + i * N2));
+      const V grs = A::load_g(__ldg(Gc + 1 * N3 + i * N2));
+      const V grt = A::load_g(__ldg(Gc + 2 * N3 + i * N2));
+      const V gss = A::load_g(__ldg(Gc + 3 * N3 + i * N2));
+      const V gst = A::load_g(__ldg(Gc + 4 * N3 + i * N2));
+      const V gtt = A::load_g(__ldg(Gc + 5 * N3 + i * N2));
+      Acc br, bs, bt;
+      A::zero(br);
+      A::zero(bs);
+      A::zero(bt);
+      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      vr[i] = A::finish(br);
+      sb[i * N2 + jk] = A::finish(bs);
+      sc[i * N2 + jk] = A::finish(bt);
+    }
+    __syncthreads();
+    // ---- transpose gradient, then back to the GLL nodes along i (registers)
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        A::fma(a, basis.D[m * N + i], vr[m]);
+        A::fma(a, Dtj[m], sb[i * N2 + m * N + k]);
+        A::fma(a, Dtk[m], sc[i * N2 + j * N + m]);
+      }
+      t[i] = A::finish(a);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + i], t[m]);
+      u[i] = A::finish(a);
+    }
+    __syncthreads();  // sb / sc consumed
+#pragma unroll
+    for (int i = 0; i < N; ++i) sa[i * N2 + jk] = u[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + j], sa[i * N2 + m * N + k]);
+      sb[i * N2 + jk] = A::finish(a);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + k], sb[i * N2 + j * N + m]);
+      const V y = A::finish(a);
+      if (idx[i] != MFGB_INVALID_DOF) {
+        const VT yv = A::store_vec(y);
+        atomicAdd(dst + idx[i], yv);
+        if (WITH_ENERGY) energy = __fma_rn((double)raw[i], (double)yv, energy);
+      }
+    }
+    __syncthreads();
+  }
+  if (WITH_ENERGY) {
+    double *s_red = reinterpret_cast<double *>(s_a);
+    s_red[tid] = energy;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int t2 = 0; t2 < E * N * N; ++t2) s += s_red[t2];
+      energy_partials[blockIdx.x] = s;
+    }
+  }
+}
+
+}  // namespace mfgb

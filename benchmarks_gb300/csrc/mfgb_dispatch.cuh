@@ -46,3 +46,43 @@ cudaError_t bk5_dispatch(int N, int64_t n_cells, const uint32_t *map, const type
 }
 
 }  // namespace mfgb
+
+namespace mfgb {
+
+template <int N, class A, bool EN>
+cudaError_t bk5g_with_basis(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
+                            const typename A::VecT *src, typename A::VecT *dst, const double *DG64,
+                            const double *B64, double *partials, int *grid, cudaStream_t s,
+                            const int *done) {
+  constexpr int E = ElemsPerCta<N>::value;
+  BasisG<N, A> b;
+  for (int q = 0; q < N * N; ++q) {
+    b.D[q] = BasisValue<A>::from(DG64[q]);
+    b.B[q] = BasisValue<A>::from(B64[q]);
+  }
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk5g_kernel<N, E, A, EN>, E * N * N, 0));
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(n_batches, (int64_t)per_sm * num_sms()));
+  if (grid) *grid = g;
+  if (n_cells <= 0) return cudaSuccess;
+  bk5g_kernel<N, E, A, EN><<<g, E * N * N, 0, s>>>(n_cells, map, G, src, dst, b, partials, done);
+  return cudaGetLastError();
+}
+
+template <class A, bool EN>
+cudaError_t bk5g_dispatch(int N, int64_t n_cells, const uint32_t *map, const typename A::GType *G,
+                          const typename A::VecT *src, typename A::VecT *dst, const double *DG,
+                          const double *B, double *partials, int *grid, cudaStream_t s,
+                          const int *done) {
+  switch (N) {
+#define MFGB_GCASE(NN) \
+  case NN: return bk5g_with_basis<NN, A, EN>(n_cells, map, G, src, dst, DG, B, partials, grid, s, done);
+    MFGB_GCASE(2) MFGB_GCASE(3) MFGB_GCASE(4) MFGB_GCASE(5) MFGB_GCASE(6) MFGB_GCASE(7)
+    MFGB_GCASE(8) MFGB_GCASE(9)
+#undef MFGB_GCASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace mfgb

@@ -17,6 +17,9 @@ struct mfgb_operator {
   int64_t *d_constrained = nullptr;
   double D[81] = {0};             // derivative matrix D[q*n + b]
   double gll_x[9] = {0}, gll_w[9] = {0};
+  int quadrature = 0;             // 0: GLL collocation, 1: Gauss (p+1 points, BP5 variant)
+  double DG[81] = {0};            // Gauss form: collocation derivative on the Gauss points
+  double Bq[81] = {0};            // Gauss form: GLL basis at the Gauss points, Bq[q*n + i]
   bool is_box = false;
   mfgb_box_desc box{};
   // workspace for reductions (per-CTA partials)
@@ -52,10 +55,19 @@ cudaError_t bk5_f32(int N, int64_t n_cells, const uint32_t *map, const float *G,
                     float *dst, const double *D, double *partials, int *grid, cudaStream_t s,
                     const int *done = nullptr);
 
+// Gauss-quadrature form (mfgb_bk5g.cu)
+cudaError_t bk5g_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                     const double *src, double *dst, const double *DG, const double *B,
+                     double *partials, int *grid, cudaStream_t s, const int *done = nullptr);
+cudaError_t bk5g_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G,
+                    const double *src, double *dst, const double *DG, const double *B,
+                    double *partials, int *grid, cudaStream_t s, const int *done = nullptr);
+void gauss_nodes(int n, double *x, double *w);
+
 // set-up kernels (mfgb_setup.cu)
 cudaError_t box_map(const mfgb_box_desc &b, uint32_t *d_map, cudaStream_t s);
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
-                         const double *D, double *d_G, cudaStream_t s);
+                         const double *D, double *d_G, cudaStream_t s, bool at_gauss = false);
 cudaError_t g_to_df(int64_t n, const double *G, float2 *Gdf, cudaStream_t s);
 cudaError_t g_to_f32(int64_t n, const double *G, float *G32, cudaStream_t s);
 cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,

@@ -106,6 +106,7 @@ struct GeomParams {
   double xg[9];           // GLL points of the geometry degree
   double V[81], Dv[81];   // V[i*ng+a] = l_a(x_i), Dv[i*ng+a] = l_a'(x_i) (geometry basis)
   int ng;                 // geometry points per direction
+  int general;            // 0: targets are the geometry nodes (J by the square D)
 };
 
 // One CTA per cell: the deformed geometry nodes (GLL points of the geometry
@@ -135,7 +136,7 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
   for (int l = threadIdx.x; l < n3; l += blockDim.x) {
     const int i = l / (n * n), j = (l / n) % n, k = l % n;
     double J[3][3];
-    if (ng == n) {
+    if (!gp.general) {
       for (int d = 0; d < 3; ++d) {
         double jr = 0, js = 0, jt = 0;
         for (int m = 0; m < n; ++m) {
@@ -188,15 +189,45 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
   }
 }
 
+// Gauss-Legendre points/weights (Newton on P_n from Chebyshev guesses), ascending
+void gauss_nodes(int n, double *x, double *w) {
+  for (int i = 0; i < n; ++i) {
+    double xi = -std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 200; ++it) {
+      double pm1, pn;
+      legendre_pair(n, xi, &pm1, &pn);
+      dp = n * (xi * pn - pm1) / (xi * xi - 1.0);
+      const double dx = pn / dp;
+      xi -= dx;
+      if (std::fabs(dx) < 1e-17) break;
+    }
+    double pm1, pn;
+    legendre_pair(n, xi, &pm1, &pn);
+    dp = n * (xi * pn - pm1) / (xi * xi - 1.0);
+    x[i] = xi;
+    w[i] = 2.0 / ((1.0 - xi * xi) * dp * dp);
+  }
+  for (int i = 0; i < n / 2; ++i) {
+    const double v = 0.5 * (x[n - 1 - i] - x[i]), ww = 0.5 * (w[n - 1 - i] + w[i]);
+    x[i] = -v; x[n - 1 - i] = v;
+    w[i] = ww; w[n - 1 - i] = ww;
+  }
+  if (n % 2) x[n / 2] = 0.0;
+}
+
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
-                         const double *D, double *d_G, cudaStream_t s) {
+                         const double *D, double *d_G, cudaStream_t s, bool at_gauss) {
   GeomParams gp{};
   const int n = b.degree + 1;
   const int g = b.geometry_degree > 0 ? b.geometry_degree : b.degree;
   if (g < 1 || g > 8) return cudaErrorInvalidValue;
   gp.ng = g + 1;
-  for (int i = 0; i < n; ++i) { gp.x[i] = gll_x[i]; gp.w[i] = gll_w[i]; }
-  if (gp.ng == n) {
+  double tx[9], tw[9];  // target points: the GLL points, or the Gauss points
+  if (at_gauss) gauss_nodes(n, tx, tw);
+  else for (int i = 0; i < n; ++i) { tx[i] = gll_x[i]; tw[i] = gll_w[i]; }
+  for (int i = 0; i < n; ++i) { gp.x[i] = tx[i]; gp.w[i] = tw[i]; }
+  gp.general = !(gp.ng == n && !at_gauss);
+  if (!gp.general) {
     for (int i = 0; i < n; ++i) gp.xg[i] = gll_x[i];
     for (int i = 0; i < n * n; ++i) gp.Dv[i] = D[i];
   } else {
@@ -204,8 +235,8 @@ cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const doub
     gll_nodes(gp.ng, gp.xg, wg);
     for (int i = 0; i < n; ++i)
       for (int a = 0; a < gp.ng; ++a) {
-        gp.V[i * gp.ng + a] = lagrange_value(gp.ng, gp.xg, a, gll_x[i]);
-        gp.Dv[i * gp.ng + a] = lagrange_derivative(gp.ng, gp.xg, a, gll_x[i]);
+        gp.V[i * gp.ng + a] = lagrange_value(gp.ng, gp.xg, a, tx[i]);
+        gp.Dv[i * gp.ng + a] = lagrange_derivative(gp.ng, gp.xg, a, tx[i]);
       }
   }
   const int64_t n_cells = (int64_t)b.nx * b.ny * b.nz;

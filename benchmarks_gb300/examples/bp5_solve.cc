@@ -1,0 +1,73 @@
+// bp5_solve.cc -- the reference's BP5 scaling driver shape
+// (bakeoff_problems_dealii/tests/scaling_bp35_kokkos_kernel/program.cc:245-328)
+// written against the header-only adapter include/mfgb_operator.hpp: set up the
+// operator on a deformed box, a seeded right-hand side, time best-of-5 batches
+// of vmult and a CG solve, print one row of the reference's convergence table
+// (cells dofs matvec CG_tot_time CG_time/iters cg_its cg_reduction).
+//
+// usage: bp5_solve nx ny nz [precond: none|jacobi|mg32|mg64] [reduce]
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "mfgb_operator.hpp"
+
+using Clock = std::chrono::steady_clock;
+
+int main(int argc, char **argv) {
+  if (argc < 4) {
+    std::fprintf(stderr, "usage: %s nx ny nz [none|jacobi|mg32|mg64] [reduce]\n", argv[0]);
+    return 1;
+  }
+  const int nx = std::atoi(argv[1]), ny = std::atoi(argv[2]), nz = std::atoi(argv[3]);
+  const std::string precond = argc > 4 ? argv[4] : "jacobi";
+  const double reduce = argc > 5 ? std::atof(argv[5]) : 1e-10;
+  try {
+    mfgb_box_desc box{nx, ny, nz, 4, {0, 0, 0}, {1, 1, 1}, 0.05, 0};
+    mfgb::LaplaceOperatorBK35<3, 4, double> A(box);
+    mfgb::DeviceVector x, b, y;
+    A.initialize_dof_vector(x);
+    A.initialize_dof_vector(b);
+    A.initialize_dof_vector(y);
+    mfgb::check(mfgb_rhs_uniform(A.handle(), 1, b.get_values(), nullptr));
+
+    double best_mv = 1e30;
+    for (int rep = 0; rep < 5; ++rep) {
+      const int n_mv = A.m() < 10000000 ? 200 : 50;
+      cudaDeviceSynchronize();
+      const auto t0 = Clock::now();
+      for (int i = 0; i < n_mv; ++i) A.vmult(y, b);
+      cudaDeviceSynchronize();
+      best_mv = std::min(best_mv, std::chrono::duration<double>(Clock::now() - t0).count() / n_mv);
+    }
+
+    mfgb::ReductionControl control(1000000, 1e-300, reduce);
+    mfgb::SolverCG cg(control);
+    cudaDeviceSynchronize();
+    const auto t0 = Clock::now();
+    if (precond == "none") {
+      cg.solve(A, x, b, mfgb::PreconditionIdentity());
+    } else if (precond == "jacobi") {
+      A.compute_diagonal();
+      cg.solve(A, x, b, *A.get_matrix_diagonal_inverse());
+    } else {
+      mfgb::MGPreconditioner mg(box, precond == "mg32" ? 32 : 64);
+      cg.solve(A, x, b, mg);
+    }
+    cudaDeviceSynchronize();
+    const double t_cg = std::chrono::duration<double>(Clock::now() - t0).count();
+    const int its = control.last_step();
+    const double red = its ? std::pow(control.last_value() / control.initial_value(), 1.0 / its) : 0.0;
+    std::printf("cells dofs matvec CG_tot_time CG_time/iters cg_its cg_reduction\n");
+    std::printf("%lld %lld %.3e %.3e %.3e %d %.3e\n", (long long)A.n_cells(), (long long)A.m(),
+                best_mv, t_cg, its ? t_cg / its : 0.0, its, red);
+    std::printf("GDoF/s %.3f\n", A.m() / best_mv * 1e-9);
+  } catch (const mfgb::Error &e) {
+    std::fprintf(stderr, "mfgb error %d: %s\n", e.status, e.what());
+    return 2;
+  }
+  return 0;
+}

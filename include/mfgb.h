@@ -95,6 +95,13 @@ int mfgb_version(void);
  * geometric factors G[cell][6][q] (:229-292), built on the device. */
 mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **op);
 
+/* The Gauss-quadrature form the reference runs (BP5 variant: QGauss(p+1),
+   values interpolated from the GLL nodes, collocation gradient at the Gauss
+   points; bakeoff_problems_dealii/include/portable_laplace_operator_bk35.h:114
+   and bk3_kokkos_kernel.h:156-404), on the same box mesh.  Exactly
+   integrated stiffness on affine cells.  (No diagonal kernel for this form.) */
+mfgb_status mfgb_operator_create_box_gauss(const mfgb_box_desc *box, mfgb_operator **op);
+
 /* Same, from caller-provided host arrays (the deal.II set-up path):
    h_dof_map[cell*(p+1)^3 + l] (0xFFFFFFFF = constrained), h_G[cell][6][(p+1)^3]
    in the order rr, rs, rt, ss, st, tt, and the list of constrained DoFs. */

@@ -1,0 +1,49 @@
+"""The header-only C++ adapter (include/mfgb_operator.hpp) used the way the
+reference's scaling driver uses its operator: the example program's CG counts
+equal the Python API's on the same problem."""
+import os
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def example():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from benchmarks_gb300 import build
+    build.build()
+    return build.build_example()
+
+
+def run(example, *args):
+    out = subprocess.run([example, *map(str, args)], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    assert lines[0].split() == ["cells", "dofs", "matvec", "CG_tot_time", "CG_time/iters",
+                                "cg_its", "cg_reduction"]
+    cells, dofs, mv, t, ti, its, red = lines[1].split()
+    return int(cells), int(dofs), float(mv), int(its), float(red)
+
+
+def test_cpp_adapter_matches_python_api(example):
+    import benchmarks_gb300 as mf
+    cells, dofs, mv, its, red = run(example, 8, 8, 4, "jacobi", 1e-8)
+    mesh = mf.BoxMesh(8, 8, 4, degree=4, amplitude=0.05)
+    A = mf.LaplaceOperator(mesh)
+    assert (cells, dofs) == (A.n_cells, A.m())
+    b = A.rhs_uniform(1)
+    x = A.initialize_dof_vector()
+    ctl = mf.ReductionControl(1000000, 1e-300, 1e-8)
+    mf.SolverCG(ctl).solve(A, x, b, A.get_matrix_diagonal_inverse())
+    assert its == ctl.last_step() and 0 < red < 1 and mv > 0
+    _, _, _, its_mg, _ = run(example, 8, 8, 4, "mg32", 1e-10)
+    assert 0 < its_mg < 30
+
+
+def test_cpp_adapter_reports_errors(example):
+    out = subprocess.run([example, "0", "1", "1"], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 2 and "invalid argument" in out.stderr
