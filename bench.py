@@ -314,7 +314,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         "config": config_dict(args, n, n_cells),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": f"bk5_kernel<{w['degree'] + 1},{'ArithDF' if arith else 'ArithF64'}>",
+                     "kernel": kernel_name(w['degree'], arith),
                      "kernel_ms": kernel_ms, "bytes_per_launch": bytes_per,
                      "flops_per_launch": flops,
                      "fp64_equiv_tflops": flops / (kernel_ms * 1e-3) / 1e12},
@@ -326,7 +326,111 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if not args.no_solve and world == 1 and is_headline():
+        line["bp5"] = bp5_solves(A)
+        line["bk6"] = bk6_rate(A, args)
+        line["bk5_gauss_like_for_like"] = gauss_like_for_like(args)
     print(json.dumps(line), flush=True)
+
+
+def bp5_solves(A):
+    """BP5 time to a 1e-10 relative residual on the bench mesh (seeded U[-1,1]
+    right-hand side): FP64 CG preconditioned by the FP32 p/h-multigrid V-cycle
+    against plain FP64 Jacobi-CG on the same GPU, and the error of the
+    mixed-precision solution against the FP64-multigrid solution."""
+    import torch
+
+    import benchmarks_gb300 as mf
+    w = WORKLOAD
+    mesh = mf.BoxMesh(w["nx"], w["ny"], w["nz"], degree=w["degree"], amplitude=w["amplitude"])
+    b = A.rhs_uniform(w["seed"])
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    out = {"tol": 1e-10, "workload": "same mesh, f ~ U[-1,1] (seed 1), x0 = 0"}
+    sols = {}
+    for prec in (32, 64):
+        M, t_setup = timed(lambda: mf.MGPreconditioner(mesh, precision=prec))
+        best = None
+        for _ in range(2):
+            x = A.initialize_dof_vector()
+            ctl = mf.ReductionControl(1000, 1e-300, 1e-10)
+            _, t = timed(lambda: mf.SolverCG(ctl).solve(A, x, b, M))
+            best = t if best is None else min(best, t)
+        sols[prec] = x
+        out[f"mg_cg_fp{prec}_vcycle"] = {"seconds": best, "setup_seconds": t_setup,
+                                         "iterations": ctl.last_step(),
+                                         "levels": [l["dofs"] for l in M.levels]}
+        del M
+    out["error_mixed_vs_fp64_mg"] = float(torch.linalg.norm(sols[32] - sols[64]) /
+                                          torch.linalg.norm(sols[64]))
+    x = A.initialize_dof_vector()
+    ctl = mf.ReductionControl(100000, 1e-300, 1e-10)
+    P = A.get_matrix_diagonal_inverse()
+    _, t = timed(lambda: mf.SolverCG(ctl).solve(A, x, b, P))
+    out["jacobi_cg_fp64"] = {"seconds": t, "iterations": ctl.last_step()}
+    out["speedup_mg_fp32_vs_jacobi"] = t / out["mg_cg_fp32_vcycle"]["seconds"]
+    out["speedup_incl_setup"] = t / (out["mg_cg_fp32_vcycle"]["seconds"] +
+                                     out["mg_cg_fp32_vcycle"]["setup_seconds"])
+    return out
+
+
+def bk6_rate(A, args):
+    """BK6 on the bench mesh: the vector Laplacian with 3 interleaved FP64
+    components per node; GDoF/s counts the 3 components (the CEED convention)."""
+    import torch
+    n = A.m()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    u = torch.rand(3 * n, dtype=torch.float64, device="cuda", generator=g)
+    y = torch.empty_like(u)
+    for _ in range(3):
+        A.vmult_vector(y, u, arith=args.arith)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        A.vmult_vector(y, u, arith=args.arith)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    n_cells, n3 = A.n_cells, (A.degree + 1) ** 3
+    bytes_per = 3 * 16 * n + n_cells * n3 * 52
+    return {"GDoF/s": 3 * n / ms / 1e6, "ms_per_vmult": ms, "components": 3,
+            "hbm_frac": bytes_per / (ms * 1e-3) / 1e9 / measured_peaks()[0]}
+
+
+def gauss_like_for_like(args):
+    """The reference's own published configuration: the BP5 variant (QGauss(5)
+    on GLL nodal values, affine mesh) at cycle 20 of its scaling study,
+    128 x 128 x 64 cells on [-1, 2.8]^2 x [-1, 0.9], 67,634,433 DoFs; published
+    6.83 GDoF/s on one A100 (bakeoff_problems_dealii/tests/
+    scaling_bp35_kokkos_kernel/results/1_GPU.out:652)."""
+    import torch
+
+    import benchmarks_gb300 as mf
+    mesh = mf.BoxMesh(128, 128, 64, degree=4, amplitude=0.0, lo=(-1.0, -1.0, -1.0),
+                      hi=(2.8, 2.8, 0.9))
+    A = mf.LaplaceOperator(mesh, quadrature="gauss", arith=args.arith)
+    u = A.rhs_uniform(1)
+    y = A.initialize_dof_vector()
+    for _ in range(3):
+        A.vmult(y, u)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(20):
+        A.vmult(y, u)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 20
+    rate = A.m() / ms / 1e6
+    return {"GDoF/s": rate, "ms_per_vmult": ms, "n_dofs": A.m(), "published_a100": 6.83,
+            "ratio_vs_published": rate / 6.83}
 
 
 def main():
@@ -338,6 +442,8 @@ def main():
     ap.add_argument("--arith", choices=["df", "fp64"], default="df")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
+    ap.add_argument("--no-solve", action="store_true",
+                    help="skip the BP5 solve comparison and the like-for-like Gauss figure")
     ap.add_argument("--cells", type=int, nargs=3, default=None,
                     help="override the mesh (cells per direction) for sweeps and profiling")
     ap.add_argument("--degree", type=int, default=None, help="override the degree p")
@@ -360,3 +466,16 @@ def main():
 
 if __name__ == "__main__":
     main()
+
+
+def kernel_name(degree, arith):
+    """Name of the operator kernel the library's shape table launches."""
+    import ctypes
+
+    import benchmarks_gb300 as mf
+    shape = ctypes.c_int()
+    mf.lib().mfgb_get_kernel_shape(arith, degree, ctypes.byref(shape))
+    n = degree + 1
+    pol = "ArithDF" if arith == 1 else "ArithF64"
+    return {0: f"bk5_kernel<{n},{pol}>", 1: f"bk5_pt_kernel<{n},{pol}>",
+            2: f"bk5_tma_kernel<{n},{pol}>"}.get(shape.value, "bk5")

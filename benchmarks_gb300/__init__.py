@@ -155,6 +155,14 @@ class LaplaceOperator:
                                     _check_vec(src, self._n_dofs, "src"), a, _stream_ptr()))
         return dst
 
+    def vmult_vector(self, dst, src, arith=None):
+        """BK6: the operator on 3 interleaved components (length 3 n)."""
+        a = self.arith if arith is None else _arith(arith)
+        _abi.check(lib().mfgb_vmult_vector(self._op, _check_vec(dst, 3 * self._n_dofs, "dst"),
+                                           _check_vec(src, 3 * self._n_dofs, "src"), 3, a,
+                                           _stream_ptr()))
+        return dst
+
     def Tvmult(self, dst, src, arith=None):
         # the operator is symmetric (portable_laplace_operator_bk35.h:386-400)
         return self.vmult(dst, src, arith)

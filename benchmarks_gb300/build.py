@@ -24,6 +24,7 @@ SOURCES = [
     "mfgb_bk5_df.cu",
     "mfgb_bk5_f32.cu",
     "mfgb_bk5g.cu",
+    "mfgb_bk6.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -680,3 +680,116 @@ __global__ void __launch_bounds__(E * N * N)
 }
 
 }  // namespace mfgb
+
+namespace mfgb {
+
+// BK6: the vector Laplacian with NC interleaved components (vec[NC*dof + c]),
+// every component through the same scalar operator.  A batch's G tile is
+// staged in shared memory once and used for all NC components, so the metric
+// bytes are shared; dof map indices stay in registers across components.
+template <int N, int E, class A, int NC>
+__global__ void __launch_bounds__(E * N * N)
+    bk6_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+               const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+               typename A::VecT *__restrict__ dst, const Basis<N, A> basis) {
+  using V = typename A::V;
+  using Acc = typename A::Acc;
+  using GT = typename A::GType;
+  using VT = typename A::VecT;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  extern __shared__ __align__(16) unsigned char smem6[];
+  GT *sG = reinterpret_cast<GT *>(smem6);
+  V *s_u = reinterpret_cast<V *>(smem6 + sizeof(GT) * E * 6 * N3);
+  V *s_vs = s_u + E * N3;
+  V *s_vt = s_vs + E * N3;
+  const int tid = threadIdx.x;
+  const int el = tid / N2;
+  const int jk = tid - el * N2;
+  const int j = jk / N;
+  const int k = jk - j * N;
+  V Dj[N], Dk[N], Dtj[N], Dtk[N];
+#pragma unroll
+  for (int m = 0; m < N; ++m) {
+    Dj[m] = basis.D[j * N + m];
+    Dk[m] = basis.D[k * N + m];
+    Dtj[m] = basis.D[m * N + j];
+    Dtk[m] = basis.D[m * N + k];
+  }
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  for (int64_t batch = blockIdx.x; batch < n_batches; batch += gridDim.x) {
+    const int64_t c0 = batch * E;
+    const int cells = (int)min((int64_t)E, n_cells - c0);
+    const bool valid = el < cells;
+    const int64_t cell = c0 + el;
+    // stage this batch's G tile (coalesced, read once for all components)
+    const GT *Gb = G + c0 * 6 * N3;
+    for (int t = tid; t < cells * 6 * N3; t += blockDim.x) sG[t] = __ldg(Gb + t);
+    uint32_t idx[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      idx[i] = valid ? __ldg(map + cell * N3 + i * N2 + jk) : MFGB_INVALID_DOF;
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c) {
+      V u[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        u[i] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(__ldg(src + (size_t)NC * idx[i] + c))
+                                          : A::zero_v();
+        s_u[el * N3 + i * N2 + jk] = u[i];
+      }
+      __syncthreads();
+      V vr[N];
+      const GT *Gc = sG + el * 6 * N3 + jk;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        Acc ar, as, at;
+        A::zero(ar);
+        A::zero(as);
+        A::zero(at);
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          A::fma(ar, basis.D[i * N + m], u[m]);
+          A::fma(as, Dj[m], s_u[el * N3 + i * N2 + m * N + k]);
+          A::fma(at, Dk[m], s_u[el * N3 + i * N2 + j * N + m]);
+        }
+        const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+        V grr = A::zero_v(), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+        if (valid) {
+          grr = A::load_g(Gc[0 * N3 + i * N2]);
+          grs = A::load_g(Gc[1 * N3 + i * N2]);
+          grt = A::load_g(Gc[2 * N3 + i * N2]);
+          gss = A::load_g(Gc[3 * N3 + i * N2]);
+          gst = A::load_g(Gc[4 * N3 + i * N2]);
+          gtt = A::load_g(Gc[5 * N3 + i * N2]);
+        }
+        Acc br, bs, bt;
+        A::zero(br);
+        A::zero(bs);
+        A::zero(bt);
+        A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+        A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+        A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+        vr[i] = A::finish(br);
+        s_vs[el * N3 + i * N2 + jk] = A::finish(bs);
+        s_vt[el * N3 + i * N2 + jk] = A::finish(bt);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        Acc a;
+        A::zero(a);
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          A::fma(a, basis.D[m * N + i], vr[m]);
+          A::fma(a, Dtj[m], s_vs[el * N3 + i * N2 + m * N + k]);
+          A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
+        }
+        const V y = A::finish(a);
+        if (idx[i] != MFGB_INVALID_DOF) atomicAdd(dst + (size_t)NC * idx[i] + c, A::store_vec(y));
+      }
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace mfgb

@@ -86,3 +86,38 @@ cudaError_t bk5g_dispatch(int N, int64_t n_cells, const uint32_t *map, const typ
 }
 
 }  // namespace mfgb
+
+namespace mfgb {
+
+template <int N, class A>
+cudaError_t bk6_with_basis(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
+                           const typename A::VecT *src, typename A::VecT *dst, const double *D64,
+                           cudaStream_t s) {
+  constexpr int E = ElemsPerCta<N>::value;
+  Basis<N, A> b;
+  for (int q = 0; q < N * N; ++q) b.D[q] = BasisValue<A>::from(D64[q]);
+  const size_t smem = sizeof(typename A::GType) * E * 6 * N * N * N +
+                      3 * sizeof(typename A::V) * E * N * N * N;
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk6_kernel<N, E, A, 3>, E * N * N, smem));
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(n_batches, (int64_t)per_sm * num_sms()));
+  if (n_cells <= 0) return cudaSuccess;
+  bk6_kernel<N, E, A, 3><<<g, E * N * N, smem, s>>>(n_cells, map, G, src, dst, b);
+  return cudaGetLastError();
+}
+
+template <class A>
+cudaError_t bk6_dispatch(int N, int64_t n_cells, const uint32_t *map, const typename A::GType *G,
+                         const typename A::VecT *src, typename A::VecT *dst, const double *D,
+                         cudaStream_t s) {
+  switch (N) {
+#define MFGB_VCASE(NN) case NN: return bk6_with_basis<NN, A>(n_cells, map, G, src, dst, D, s);
+    MFGB_VCASE(2) MFGB_VCASE(3) MFGB_VCASE(4) MFGB_VCASE(5) MFGB_VCASE(6) MFGB_VCASE(7)
+    MFGB_VCASE(8) MFGB_VCASE(9)
+#undef MFGB_VCASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace mfgb

@@ -64,6 +64,12 @@ cudaError_t bk5g_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G
                     double *partials, int *grid, cudaStream_t s, const int *done = nullptr);
 void gauss_nodes(int n, double *x, double *w);
 
+// BK6 vector Laplacian, 3 interleaved components (mfgb_bk6.cu)
+cudaError_t bk6_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                    const double *src, double *dst, const double *D, cudaStream_t s);
+cudaError_t bk6_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const double *src,
+                   double *dst, const double *D, cudaStream_t s);
+
 // set-up kernels (mfgb_setup.cu)
 cudaError_t box_map(const mfgb_box_desc &b, uint32_t *d_map, cudaStream_t s);
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,

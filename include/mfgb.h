@@ -137,6 +137,13 @@ mfgb_status mfgb_vmult_add(const mfgb_operator *op, double *d_dst, const double 
 mfgb_status mfgb_copy_constrained(const mfgb_operator *op, double *d_dst, const double *d_src,
                                   void *stream);
 
+/* BK6/BP6 vector Laplacian: the scalar operator applied to ncomp = 3
+   interleaved FP64 components (vec[3*dof + c]), constrained DoFs identity in
+   every component.  The CEED BK6 definition (vector form of BK5); no
+   counterpart kernel in the reference.  GLL operators only. */
+mfgb_status mfgb_vmult_vector(const mfgb_operator *op, double *d_dst, const double *d_src,
+                              int ncomp, int arith, void *stream);
+
 /* vmult in FP32 arithmetic on FP32 vectors (the multigrid levels; the FP32
    copy of G is built on first use). */
 mfgb_status mfgb_vmult_f32(const mfgb_operator *op, float *d_dst, const float *d_src, void *stream);
