@@ -369,6 +369,24 @@ def bp5_solves(A):
         del M
     out["error_mixed_vs_fp64_mg"] = float(torch.linalg.norm(sols[32] - sols[64]) /
                                           torch.linalg.norm(sols[64]))
+    # learned smoother weights (network trained by benchmarks_gb300/train_smoother.py);
+    # the calibration keeps the plain smoother unless the learned one needs fewer iterations
+    wpath = os.path.join(ROOT, "benchmarks_gb300", "data", "smoother_mlp.bin")
+    if os.path.exists(wpath):
+        from benchmarks_gb300.learned import LearnedSmoother
+        S = LearnedSmoother.load(wpath)
+        M = mf.MGPreconditioner(mesh, precision=32)
+        (used, its_plain, its_learned), t_cal = timed(
+            lambda: S.attach(M, A, calibrate=True, reduce=1e-10))
+        x = A.initialize_dof_vector()
+        ctl = mf.ReductionControl(1000, 1e-300, 1e-10)
+        _, t = timed(lambda: mf.SolverCG(ctl).solve(A, x, b, M))
+        out["mg_cg_fp32_learned"] = {
+            "seconds": t, "iterations": ctl.last_step(), "used_learned_weights": used,
+            "calibration_iterations_plain": its_plain,
+            "calibration_iterations_learned": its_learned, "calibration_seconds": t_cal,
+            "error_vs_fp64_mg": float(torch.linalg.norm(x - sols[64]) / torch.linalg.norm(sols[64]))}
+        del M
     x = A.initialize_dof_vector()
     ctl = mf.ReductionControl(100000, 1e-300, 1e-10)
     P = A.get_matrix_diagonal_inverse()

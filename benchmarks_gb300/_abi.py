@@ -87,6 +87,14 @@ def lib():
         "mfgb_cg_solve_noalloc": ([P, P, P, P, ctypes.POINTER(CgControl),
                                    ctypes.POINTER(SolveInfo), P], I32),
         "mfgb_dot": ([I64, P, P, ctypes.POINTER(D), P], I32),
+        "mfgb_mg_set_smoother_weights": ([P, P], I32),
+        "mfgb_mlp_n_params": ([], I32),
+        "mfgb_cell_features": ([P, P, P], I32),
+        "mfgb_cell_lambda": ([P, P, I32, P], I32),
+        "mfgb_mlp_loss_grad": ([P, P, P, I32, P, P], I32),
+        "mfgb_mlp_train": ([P, P, P, I64, I32, I32, ctypes.c_float, ctypes.c_uint64, P], I32),
+        "mfgb_mlp_forward_f32": ([P, P, I32, P], I32),
+        "mfgb_mlp_infer": ([P, P, I64, P, P], I32),
         "mfgb_mg_setup": ([ctypes.POINTER(BoxDesc), ctypes.POINTER(MgParams), PP], I32),
         "mfgb_mg_destroy": ([P], I32),
         "mfgb_mg_info": ([P, P, P, P, P], I32),

@@ -25,6 +25,7 @@ SOURCES = [
     "mfgb_bk5_f32.cu",
     "mfgb_bk5g.cu",
     "mfgb_bk6.cu",
+    "mfgb_mlp.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -64,6 +64,10 @@ cudaError_t bk5g_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G
                     double *partials, int *grid, cudaStream_t s, const int *done = nullptr);
 void gauss_nodes(int n, double *x, double *w);
 
+// assembled diagonal with per-cell weights: d_i = sum_e w_e (A_e)_ii (mfgb_mlp.cu)
+cudaError_t weighted_diagonal(const mfgb_operator *op, const double *w, double *diag,
+                              cudaStream_t s);
+
 // BK6 vector Laplacian, 3 interleaved components (mfgb_bk6.cu)
 cudaError_t bk6_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,
                     const double *src, double *dst, const double *D, cudaStream_t s);

@@ -592,7 +592,8 @@ mfgb_status mg_apply(mfgb_mg *mg, double *dst, const double *src, cudaStream_t s
 }
 
 // lambda_max of Dinv A by power iteration (FP64 host-driven, set-up only)
-mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax) {
+mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
+                          const double *dinv_given = nullptr) {
   const int64_t n = L.n;
   std::vector<double> h(n);
   uint64_t st64 = 0x9E3779B97F4A7C15ull;
@@ -613,9 +614,14 @@ mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax) {
   if (L.op->n_constrained)
     k_set_constrained<double><<<grid1d(L.op->n_constrained), T256>>>(L.op->n_constrained,
                                                                       L.op->d_constrained, v, 0.0);
-  if ((st = mfgb_compute_diagonal(L.op, dinv, nullptr)) ||
-      (st = cuda_status(invert_diagonal(n, dinv, nullptr), "invert diag")))
+  if (dinv_given) {
+    if ((st = cuda_status(cudaMemcpy(dinv, dinv_given, sizeof(double) * n, cudaMemcpyDeviceToDevice),
+                          "lmax dinv")))
+      return st;
+  } else if ((st = mfgb_compute_diagonal(L.op, dinv, nullptr)) ||
+             (st = cuda_status(invert_diagonal(n, dinv, nullptr), "invert diag"))) {
     return st;
+  }
   double lam = 0;
   for (int it = 0; it < iters; ++it) {
     double nv = 0;
@@ -789,6 +795,47 @@ extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_pa
   }
   *out = mg;
   return MFGB_OK;
+}
+
+// Learned smoother weights on the finest level: the Jacobi diagonal inside the
+// Chebyshev smoother becomes D~ = sum_e w_e D_e (w_e > 0 per cell, e.g. the
+// predicted lambda_max(D_e^-1 A_e)); d_cell_weights == NULL restores the plain
+// diagonal.  lambda_max of D~^-1 A is re-estimated.
+extern "C" mfgb_status mfgb_mg_set_smoother_weights(mfgb_mg *mg, const double *d_cell_weights) {
+  if (!mg || mg->levels.empty()) {
+    set_error("mfgb_mg_set_smoother_weights: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  MgLevel &L = mg->levels[0];
+  if (L.to_coarse == 0) {
+    set_error("mfgb_mg_set_smoother_weights: single-level hierarchy has no smoother");
+    return MFGB_ERR_UNSUPPORTED;
+  }
+  double *d64 = nullptr;
+  mfgb_status st = dalloc((void **)&d64, sizeof(double) * L.n);
+  if (st) return st;
+  if (d_cell_weights) {
+    st = cuda_status(cudaMemset(d64, 0, sizeof(double) * L.n), "diag = 0");
+    if (!st) st = cuda_status(weighted_diagonal(L.op, d_cell_weights, d64, nullptr), "weighted diag");
+    if (!st)
+      st = cuda_status(set_constrained(L.op->n_constrained, L.op->d_constrained, d64, 1.0, nullptr),
+                       "weighted diag constrained");
+  } else {
+    st = mfgb_compute_diagonal(L.op, d64, nullptr);
+  }
+  if (!st) st = cuda_status(invert_diagonal(L.n, d64, nullptr), "invert diag");
+  double lam = 0;
+  if (!st) st = estimate_lmax(L, mg->precision, 20, &lam, d64);
+  if (!st) {
+    L.lmax = 1.2 * lam;
+    if (mg->precision == 32)
+      k_convert<float, double><<<grid1d(L.n), T256>>>(L.n, d64, (float *)L.inv_diag);
+    else
+      cudaMemcpy(L.inv_diag, d64, sizeof(double) * L.n, cudaMemcpyDeviceToDevice);
+    st = cuda_status(cudaDeviceSynchronize(), "smoother weights");
+  }
+  cudaFree(d64);
+  return st;
 }
 
 extern "C" mfgb_status mfgb_mg_destroy(mfgb_mg *mg) {

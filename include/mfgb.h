@@ -230,6 +230,33 @@ mfgb_status mfgb_mg_vmult(mfgb_mg *mg, double *d_dst, const double *d_src, void 
 mfgb_status mfgb_mg_cg_solve(const mfgb_operator *op, mfgb_mg *mg, const double *d_b, double *d_x,
                              const mfgb_cg_control *ctl, mfgb_solve_info *info, void *stream);
 
+/* Learned smoother weights on the finest level (no counterpart in the
+   reference): the Chebyshev smoother's Jacobi diagonal becomes
+   D~ = sum_cells w_e D_e with w_e > 0 per cell (D_e the cell matrix's
+   diagonal); NULL restores the plain diagonal.  The V-cycle stays linear and
+   SPD.  lambda_max of D~^-1 A is re-estimated. */
+mfgb_status mfgb_mg_set_smoother_weights(mfgb_mg *mg, const double *d_cell_weights);
+
+/* ---- learned part: features, targets, MLP (no counterpart in the reference)
+ * features: per cell, dx/dxi at the 8 corner nodes (72 values, scaled by
+ *   |mean corner det J|^(-1/3)) and p/8 -> float[n_cells][73] (box operators)
+ * targets: lambda_max(D_e^-1 A_e) per cell by FP64 power iteration
+ * MLP 73-64-64-1, relu, softplus output; parameters FP32 in the order
+ *   W1[64][73], b1[64], W2[64][64], b2[64], w3[64], b3 (mfgb_mlp_n_params())
+ * training: Adam on MSE, minibatches drawn by a fixed hash of (seed, step)
+ * inference: BF16 tensor-core MMAs with FP32 accumulation */
+int mfgb_mlp_n_params(void);
+mfgb_status mfgb_cell_features(const mfgb_operator *op, float *d_features, void *stream);
+mfgb_status mfgb_cell_lambda(const mfgb_operator *op, double *d_lambda, int iterations,
+                             void *stream);
+mfgb_status mfgb_mlp_loss_grad(const float *d_params, const float *d_X, const float *d_t, int n,
+                               float *h_grad, float *h_loss);
+mfgb_status mfgb_mlp_train(float *d_params, const float *d_X, const float *d_t, int64_t n,
+                           int steps, int batch, float lr, uint64_t seed, float *h_loss);
+mfgb_status mfgb_mlp_forward_f32(const float *d_params, const float *d_X, int n, float *d_y);
+mfgb_status mfgb_mlp_infer(const float *d_params, const float *d_X, int64_t n, double *d_y,
+                           void *stream);
+
 /* ---- vector kernels used by the solver (exposed for tests) -------------- */
 /* result[0] = sum a_i b_i (deterministic two-stage reduction) */
 mfgb_status mfgb_dot(int64_t n, const double *d_a, const double *d_b, double *h_result,

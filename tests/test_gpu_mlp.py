@@ -1,0 +1,106 @@
+"""Learned smoother weights: features, targets, forward/backward kernels
+against the CPU oracle (oracle/mlp_oracle.py), BF16 tensor-core inference, GPU
+training, and what the trained network gains in the multigrid solver.
+
+Tolerances: features 1e-5 (FP32 output), cell targets 1e-6 after 400 power
+iterations, gradient 1e-4 relative (FP32 kernels vs FP64 oracle), BF16
+inference 3e-2 relative per cell against the FP32 forward.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mf():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import benchmarks_gb300 as mf
+    mf.lib()
+    return mf
+
+
+@pytest.fixture(scope="module")
+def mo():
+    from oracle import mlp_oracle
+    return mlp_oracle
+
+
+def test_features_and_targets(mf, orc, mo):
+    from benchmarks_gb300 import learned
+    for p, a in ((2, 0.1), (4, 0.06)):
+        A = mf.LaplaceOperator(mf.BoxMesh(3, 3, 2, degree=p, amplitude=a))
+        ref = orc.BoxProblem(3, 3, 2, p, amplitude=a)
+        F = learned.cell_features(A).cpu().numpy()
+        Fo = mo.cell_features(ref)
+        assert np.max(np.abs(F - Fo)) <= 1e-5 * np.max(np.abs(Fo))
+        lam = learned.cell_lambda(A, 400).cpu().numpy()
+        lo = mo.cell_lambda(ref)
+        assert np.max(np.abs(lam - lo) / lo) <= 1e-6
+
+
+def test_loss_and_gradient_match_oracle(mf, mo):
+    import torch
+    from benchmarks_gb300.learned import LearnedSmoother
+    rng = np.random.default_rng(3)
+    X = rng.normal(size=(200, 73)).astype(np.float32)
+    t = rng.uniform(1.5, 3.5, 200).astype(np.float32)
+    P = mo.init_params(5)
+    S = LearnedSmoother(mo.flatten(P))
+    L, g = S.loss_grad(torch.from_numpy(X).cuda(), torch.from_numpy(t).cuda())
+    Lo, go = mo.loss_and_grads(mo.unflatten(S.params.cpu().numpy().astype(np.float64)),
+                               X.astype(np.float64), t.astype(np.float64))
+    assert abs(L - Lo) <= 1e-5 * Lo
+    go = mo.flatten(go)
+    assert np.linalg.norm(g - go) <= 1e-4 * np.linalg.norm(go)
+
+
+def test_bf16_tensor_core_inference(mf, mo):
+    import torch
+    from benchmarks_gb300.learned import LearnedSmoother
+    rng = np.random.default_rng(4)
+    X = rng.normal(size=(1000, 73)).astype(np.float32)
+    S = LearnedSmoother(seed=2)
+    Xd = torch.from_numpy(X).cuda()
+    y16 = S.predict(Xd).cpu().numpy()
+    y32 = S.predict_f32(Xd).cpu().numpy()
+    yo, _ = mo.forward(mo.unflatten(S.params.cpu().numpy().astype(np.float64)), X.astype(np.float64))
+    assert np.max(np.abs(y32 - yo) / np.abs(yo)) <= 1e-5
+    assert np.max(np.abs(y16 - yo) / np.abs(yo)) <= 3e-2
+
+
+def test_training_and_solver_gain(mf, tmp_path):
+    """Train on deformed meshes (degrees 2..7, amplitude in [0, 0.12]: the
+    sinusoidal map folds beyond a = 0.138), check the held-out prediction of the
+    FP64 cell spectra, then compare MG-CG iterations with the plain and the
+    learned smoother; the calibration keeps whichever needs fewer."""
+    import torch
+    from benchmarks_gb300.learned import LearnedSmoother, cell_features, cell_lambda
+    rng = np.random.default_rng(0)
+    meshes = [mf.BoxMesh(8, 8, 6, degree=int(p), amplitude=float(a))
+              for p, a in zip(rng.integers(2, 8, 48), rng.uniform(0.0, 0.12, 48))]
+    X, t = LearnedSmoother.training_data(meshes)
+    S = LearnedSmoother(seed=1)
+    loss = S.train(X, t, steps=3000, batch=1024, lr=2e-3)
+    assert loss[-50:].mean() < 0.01 * loss[:10].mean()
+    mesh = mf.BoxMesh(8, 8, 8, degree=4, amplitude=0.12)  # held out
+    A = mf.LaplaceOperator(mesh)
+    pred = S.predict(cell_features(A))
+    true = cell_lambda(A)
+    r = (torch.abs(pred - true) / true).cpu().numpy()
+    assert np.median(r) < 0.05 and np.percentile(r, 95) < 0.15
+    path = tmp_path / "mlp.bin"
+    S.save(path)
+    assert torch.equal(LearnedSmoother.load(path).params, S.params)
+    M = mf.MGPreconditioner(mesh, precision=32)
+    used, plain, learned = S.attach(M, A, calibrate=True, reduce=1e-10)
+    print(f"MG-CG iterations to 1e-10: plain {plain}, learned {learned}, used learned: {used}")
+    assert used == (learned < plain)
+    b = A.rhs_uniform(3)
+    x = A.initialize_dof_vector()
+    ctl = mf.ReductionControl(1000, 1e-300, 1e-10)
+    mf.SolverCG(ctl).solve(A, x, b, M)
+    assert ctl.last_value() <= 1e-10 * ctl.initial_value()
+    assert ctl.last_step() <= min(plain, learned) + 1
