@@ -1,0 +1,95 @@
+"""Per-degree kernel-shape autotuner (no counterpart in the reference, whose
+launch shape is a compile-time choice: CEED_BK/src/BK5/templated_cuda_benchmark.cc:114-124).
+
+For each (arithmetic, degree) it times every thread layout the library has
+(0 column, 1 point-per-thread, 2 column with bulk-TMA prefetch) on a
+representative deformed box mesh with CUDA events, and installs the fastest in
+the library's shape table (``mfgb_set_kernel_shape``).  Results can be saved
+to and loaded from a small JSON file.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+
+from . import _abi
+from ._abi import lib
+
+ARITHS = {"fp64": 0, "df": 1, "fp32": 2}
+SHAPES = (0, 1, 2)
+
+
+def _mesh_for(degree, target_dofs):
+    import benchmarks_gb300 as mf
+    n = max(2, round((target_dofs ** (1.0 / 3.0) - 1) / degree))
+    return mf.BoxMesh(n, n, n, degree=degree, amplitude=0.05)
+
+
+def time_shape(A, arith, shape, reps=10):
+    """Milliseconds per operator application with the given shape."""
+    import torch
+    L = lib()
+    degree = A.degree
+    old = ctypes.c_int()
+    _abi.check(L.mfgb_get_kernel_shape(arith, degree, ctypes.byref(old)))
+    _abi.check(L.mfgb_set_kernel_shape(arith, degree, shape))
+    try:
+        n = A.m()
+        dt = torch.float32 if arith == 2 else torch.float64
+        src = torch.rand(n, dtype=dt, device="cuda")
+        dst = torch.zeros_like(src)
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+        def once():
+            if arith == 2:
+                _abi.check(L.mfgb_vmult_f32(A.handle, ctypes.c_void_p(dst.data_ptr()),
+                                            ctypes.c_void_p(src.data_ptr()), sp))
+            else:
+                _abi.check(L.mfgb_vmult(A.handle, ctypes.c_void_p(dst.data_ptr()),
+                                        ctypes.c_void_p(src.data_ptr()), arith, sp))
+        for _ in range(3):
+            once()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            once()
+        e1.record()
+        torch.cuda.synchronize()
+        _abi.check(L.mfgb_check_device_errors(sp))  # a timed-out kernel is not a result
+        return e0.elapsed_time(e1) / reps
+    finally:
+        _abi.check(L.mfgb_set_kernel_shape(arith, degree, old.value))
+
+
+def tune(degrees=range(1, 9), ariths=("df", "fp32"), target_dofs=2.0e7, reps=10, apply=True):
+    """Times every shape; returns {arith: {degree: {"best": s, "ms": [..]}}} and
+    (with apply) installs the winners."""
+    import benchmarks_gb300 as mf
+    result = {}
+    for d in degrees:
+        A = mf.LaplaceOperator(_mesh_for(d, target_dofs))
+        for name in ariths:
+            a = ARITHS[name]
+            ms = [time_shape(A, a, s, reps) for s in SHAPES]
+            best = min(range(len(SHAPES)), key=lambda i: ms[i])
+            result.setdefault(name, {})[d] = {"best": SHAPES[best], "ms": ms, "n_dofs": A.m()}
+            if apply:
+                _abi.check(lib().mfgb_set_kernel_shape(a, d, SHAPES[best]))
+        del A
+    return result
+
+
+def save(result, path):
+    with open(path, "w") as f:
+        json.dump(result, f, indent=1)
+
+
+def load(path, apply=True):
+    with open(path) as f:
+        result = json.load(f)
+    if apply:
+        for name, per in result.items():
+            for d, r in per.items():
+                _abi.check(lib().mfgb_set_kernel_shape(ARITHS[name], int(d), int(r["best"])))
+    return result

@@ -81,11 +81,12 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
 }
 
 // kernel shape per (arithmetic class, N): 0 column, 1 point-per-thread,
-// 2 column with TMA-prefetched geometric factors
+// 2 column with TMA-prefetched geometric factors.  Defaults are the fastest
+// shape per degree measured on a GB300 at ~3e7 DoFs (autotune.py re-measures).
 static int g_shape[3][10] = {
-    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0},  // FP64
-    {2, 2, 2, 2, 2, 2, 2, 2, 2, 2},  // double-float
-    {2, 2, 2, 2, 2, 2, 2, 2, 2, 2},  // FP32
+    {0, 0, 2, 2, 2, 1, 2, 1, 2, 1},  // FP64
+    {2, 2, 2, 2, 2, 2, 0, 2, 2, 2},  // double-float
+    {0, 0, 0, 0, 0, 0, 2, 0, 2, 2},  // FP32
 };
 
 // device-side error word (a TMA wait that ran out of time), one per device
@@ -109,6 +110,28 @@ int *device_error_flag() {
 int kernel_shape(int arith_class, int N) {
   if (arith_class < 0 || arith_class > 2 || N < 0 || N > 9) return 0;
   return g_shape[arith_class][N];
+}
+
+mfgb_status apply_add_impl(mfgb_operator *op, double *dst, const double *src, int arith,
+                           cudaStream_t s, const int *done) {
+  mfgb_status st;
+  cudaError_t e;
+  if (arith == MFGB_ARITH_FP64) {
+    e = op->quadrature ? bk5g_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->DG, op->Bq,
+                                  nullptr, nullptr, s, done)
+                       : bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, nullptr,
+                                 nullptr, s, done);
+  } else if (arith == MFGB_ARITH_FP64_DF) {
+    if ((st = ensure_df(op))) return st;
+    e = op->quadrature ? bk5g_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->DG,
+                                 op->Bq, nullptr, nullptr, s, done)
+                       : bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D,
+                                nullptr, nullptr, s, done);
+  } else {
+    set_error("apply: unknown arith mode");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return cuda_status(e, "apply: bk5 kernel");
 }
 
 static void free_operator(mfgb_operator *op) {

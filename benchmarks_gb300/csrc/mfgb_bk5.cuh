@@ -330,10 +330,14 @@ __global__ void __launch_bounds__(E * N * N, TmaMinBlocks<N>::value)
 
   auto cells_of = [&](int64_t b) { return (int)min((int64_t)E, n_cells - b * E); };
   auto map_by_tma = [&](int cells) { return L::map_tma && ((cells * N3 * 4) % 16 == 0); };
-  auto issue_g = [&](int64_t b) {  // one thread
-    const uint32_t gb = (uint32_t)(sizeof(GT) * cells_of(b) * 6 * N3);
+  // a bulk copy needs a 16-byte multiple: 4-byte G tiles of an odd number of
+  // cells with odd N^3 (possible only in the last batch) are loaded by plain loads
+  auto g_by_tma = [&](int cells) { return (sizeof(GT) * cells * 6 * N3) % 16 == 0; };
+  auto issue_g = [&](int64_t b) {  // one thread; completes the phase either way
+    const int cells = cells_of(b);
+    const uint32_t gb = g_by_tma(cells) ? (uint32_t)(sizeof(GT) * cells * 6 * N3) : 0u;
     mbar_arrive_expect_tx(mbar_g, gb);
-    bulk_g2s(sG, G + b * E * 6 * N3, gb, mbar_g);
+    if (gb) bulk_g2s(sG, G + b * E * 6 * N3, gb, mbar_g);
   };
   auto issue_map = [&](int64_t b) {  // one thread; completes the phase either way
     const int cells = cells_of(b);
@@ -386,6 +390,11 @@ __global__ void __launch_bounds__(E * N * N, TmaMinBlocks<N>::value)
     const bool okg = mbar_wait(mbar_g, ph_g);
     if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
     ph_g ^= 1u;
+    if (!g_by_tma(cells_of(batch))) {  // tail tile not 16-byte sized: plain loads
+      const int64_t nG = (int64_t)cells_of(batch) * 6 * N3;
+      const GT *Gb = G + batch * E * 6 * N3;
+      for (int64_t t = tid; t < nG; t += blockDim.x) sG[t] = __ldg(Gb + t);
+    }  // ordered before the metric phase by barrier B
     V u[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {

@@ -8,11 +8,12 @@
 // diagonal (DiagonalMatrix).
 //
 // GB300 layout of one iteration (all on the device, no host round trip):
-//   1. bk5 apply  v += A p, with per-CTA partials of sum_e p_e.(A_e p_e)
-//   2. constrained rows v_c = p_c, partial sum p_c^2
-//   3. update     alpha = rz / pAp; x += alpha p; r -= alpha v;
+//   1. bk5 apply  v += A p (cell loop)
+//   2. constrained rows v_c = p_c
+//   3. p.v        per-CTA partials (one read of p and v)
+//   4. update     alpha = rz / pAp; x += alpha p; r -= alpha v;
 //                 partials of r.r and r.z (z = Dinv r, never stored)
-//   4. direction  |r| test -> done flag; beta; p = z + beta p; v = 0
+//   5. direction  |r| test -> done flag; beta; p = z + beta p; v = 0
 // Each kernel returns at once when the done flag is set, so a CUDA graph of
 // K iterations can be replayed until the host sees the flag.  All reductions
 // are two-stage with a fixed order (deterministic).
@@ -63,20 +64,29 @@ __device__ __forceinline__ double sum_partials(const double *__restrict__ p, int
   return sh[32];
 }
 
+// identity rows of the constrained DoFs: v_c = p_c (many CTAs)
 __global__ void __launch_bounds__(VEC_THREADS)
-    cg_constrained_kernel(int64_t nc, const int64_t *__restrict__ c, const double *__restrict__ p,
-                          double *__restrict__ v, double *__restrict__ partial,
-                          const CgScalars *__restrict__ sc) {
+    cg_constrained_copy_kernel(int64_t nc, const int64_t *__restrict__ c,
+                               const double *__restrict__ p, double *__restrict__ v,
+                               const CgScalars *__restrict__ sc) {
+  if (sc->done) return;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nc;
+       t += (int64_t)gridDim.x * blockDim.x)
+    v[c[t]] = p[c[t]];
+}
+
+// per-CTA partials of p.v (v = A p including the identity rows)
+__global__ void __launch_bounds__(VEC_THREADS)
+    cg_dot_pv_kernel(int64_t n, const double *__restrict__ p, const double *__restrict__ v,
+                     double *__restrict__ partials, const CgScalars *__restrict__ sc) {
   if (sc->done) return;
   __shared__ double sh[40];
-  double acc = 0.0;
-  for (int64_t t = threadIdx.x; t < nc; t += blockDim.x) {
-    const double pv = p[c[t]];
-    v[c[t]] = pv;
-    acc += pv * pv;
-  }
-  const double s = block_sum<VEC_THREADS>(acc, sh);
-  if (threadIdx.x == 0) *partial = s;
+  double s = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    s = __fma_rn(p[t], v[t], s);
+  const double bs = block_sum<VEC_THREADS>(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = bs;
 }
 
 __global__ void __launch_bounds__(VEC_THREADS)
@@ -330,18 +340,14 @@ extern "C" mfgb_status mfgb_cg_solve(const mfgb_operator *cop, const double *d_b
   mfgb_status cap_st = MFGB_OK;
   for (int k = 0; k < K && cap_st == MFGB_OK; ++k) {
     const int parity = k & 1;
-    int grid = 0;
-    cap_st = vmult_impl(op, v, p, ctl->arith, pap_part, &grid, s, &sc->done);
+    cap_st = apply_add_impl(op, v, p, ctl->arith, s, &sc->done);
     if (cap_st) break;
-    if (grid + 1 > PAP_CAP) {
-      set_error("mfgb_cg_solve: partials buffer too small");
-      cap_st = MFGB_ERR_UNSUPPORTED;
-      break;
-    }
-    cg_constrained_kernel<<<1, VEC_THREADS, 0, s>>>(op->n_constrained, op->d_constrained, p, v,
-                                                     pap_part + grid, sc);
-    cg_update_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_x, r, p, v, dinv, pap_part, grid + 1,
-                                                        vec_part, sc, parity);
+    if (op->n_constrained)
+      cg_constrained_copy_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(op->n_constrained,
+                                                                    op->d_constrained, p, v, sc);
+    cg_dot_pv_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, p, v, pap_part, sc);
+    cg_update_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_x, r, p, v, dinv, pap_part,
+                                                        VEC_BLOCKS, vec_part, sc, parity);
     cg_direction_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, r, p, v, dinv, vec_part, VEC_BLOCKS,
                                                            sc, parity);
   }
@@ -373,6 +379,7 @@ extern "C" mfgb_status mfgb_cg_solve(const mfgb_operator *cop, const double *d_b
   info->steps = out.final_its;
   info->last = out.final_res;
   info->converged = out.done == 1;
+  if ((st = mfgb_check_device_errors(s))) return st;
   if (out.done == 1) return MFGB_OK;
   if (std::isnan(out.final_res)) {
     set_error("mfgb_cg_solve: residual became NaN");
@@ -440,10 +447,12 @@ static mfgb_status noalloc_scratch(double **out) {
 // double-float arithmetic uses the operator's split copy of G when an earlier
 // call created it, and otherwise splits the FP64 geometric factors on load.
 static mfgb_status noalloc_apply(const mfgb_operator *op, double *dst, const double *src, int arith,
-                                 double *partials, int *grid, cudaStream_t s, const int *done) {
+                                 double *partials, int *grid, cudaStream_t s, const int *done,
+                                 bool accumulate = false) {
   mfgb_status st;
-  if (!partials && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
-                                     "dst = 0")))
+  const bool full = !partials && !accumulate;
+  if (full && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
+                                "dst = 0")))
     return st;
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64)
@@ -456,7 +465,7 @@ static mfgb_status noalloc_apply(const mfgb_operator *op, double *dst, const dou
   else
     e = bk5_df_g64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, s);
   if ((st = cuda_status(e, "bk5 kernel"))) return st;
-  if (!partials)
+  if (full)
     return cuda_status(copy_constrained(op->n_constrained, op->d_constrained, src, dst, s),
                        "constrained rows");
   return MFGB_OK;
@@ -540,16 +549,15 @@ extern "C" mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const doub
   for (;;) {
     for (int k = 0; k < K; ++k) {
       const int parity = k & 1;
-      int grid = 0;
-      if ((st = noalloc_apply(op, v, p, ctl->arith, pap_part, &grid, s, &sc->done))) return st;
-      if (grid + 1 > NOALLOC_PAP_CAP) {
-        set_error("mfgb_cg_solve_noalloc: partials slot too small");
-        return MFGB_ERR_UNSUPPORTED;
-      }
-      cg_constrained_kernel<<<1, VEC_THREADS, 0, s>>>(op->n_constrained, op->d_constrained, p, v,
-                                                       pap_part + grid, sc);
+      if ((st = noalloc_apply(op, v, p, ctl->arith, nullptr, nullptr, s, &sc->done,
+                              /*accumulate=*/true)))
+        return st;
+      if (op->n_constrained)
+        cg_constrained_copy_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(op->n_constrained,
+                                                                      op->d_constrained, p, v, sc);
+      cg_dot_pv_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, p, v, pap_part, sc);
       cg_update_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_x, r, p, v, dinv, pap_part,
-                                                          grid + 1, vec_part, sc, parity);
+                                                          VEC_BLOCKS, vec_part, sc, parity);
       cg_direction_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, r, p, v, dinv, vec_part,
                                                              VEC_BLOCKS, sc, parity);
     }

@@ -91,6 +91,10 @@ cudaError_t invert_diagonal(int64_t n, double *d, cudaStream_t s);
 // operator helpers (mfgb_api.cu)
 mfgb_status ensure_df(mfgb_operator *op);
 mfgb_status ensure_partials(mfgb_operator *op, int n);
+// dst += A src (cell loop only: no zeroing, no identity rows); `done` lets
+// a captured solver iteration skip the work once converged
+mfgb_status apply_add_impl(mfgb_operator *op, double *dst, const double *src, int arith,
+                           cudaStream_t s, const int *done);
 // vmult with optional energy partials (p.Ap) for the solver
 mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int arith,
                        double *partials, int *grid, cudaStream_t s, const int *done = nullptr);

@@ -197,6 +197,86 @@ __global__ void k_p_restrict(int64_t n_cells, const uint32_t *__restrict__ map_f
   }
 }
 
+// Sum-factorised p-transfers: one CTA per cell, three 1D passes through
+// shared memory (nc^3 -> nc*nc*nf -> nc*nf*nf -> nf^3 and back).
+template <class T>
+__global__ void __launch_bounds__(128)
+    k_p_prolongate_sf(int64_t n_cells, const uint32_t *__restrict__ map_f,
+                      const uint32_t *__restrict__ map_c, const T *__restrict__ xc,
+                      T *__restrict__ tf, PTransferParams P) {
+  __shared__ T s0[729], s1[729];
+  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
+  for (int64_t e = blockIdx.x; e < n_cells; e += gridDim.x) {
+    for (int t = threadIdx.x; t < nc3; t += blockDim.x) {
+      const uint32_t dc = map_c[e * nc3 + t];
+      s0[t] = dc != MFGB_INVALID_DOF ? xc[dc] : T(0);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * nc * nf; t += blockDim.x) {  // along k: [a][b][kf]
+      const int a = t / (nc * nf), b = (t / nf) % nc, kf = t % nf;
+      T s = 0;
+      for (int c = 0; c < nc; ++c) s += bval<T>(P, kf * nc + c) * s0[(a * nc + b) * nc + c];
+      s1[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * nf * nf; t += blockDim.x) {  // along j: [a][jf][kf]
+      const int a = t / (nf * nf), jf = (t / nf) % nf, kf = t % nf;
+      T s = 0;
+      for (int b = 0; b < nc; ++b) s += bval<T>(P, jf * nc + b) * s1[(a * nc + b) * nf + kf];
+      s0[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nf3; t += blockDim.x) {  // along i: [if][jf][kf]
+      const int i = t / (nf * nf), jk = t % (nf * nf);
+      const uint32_t df = map_f[e * nf3 + t];
+      if (df == MFGB_INVALID_DOF) continue;
+      T s = 0;
+      for (int a = 0; a < nc; ++a) s += bval<T>(P, i * nc + a) * s0[a * nf * nf + jk];
+      tf[df] = s;
+    }
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(128)
+    k_p_restrict_sf(int64_t n_cells, const uint32_t *__restrict__ map_f,
+                    const uint32_t *__restrict__ map_c, const T *__restrict__ rf,
+                    const T *__restrict__ inv_val_f, T *__restrict__ rc, PTransferParams P) {
+  __shared__ T s0[729], s1[729];
+  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
+  for (int64_t e = blockIdx.x; e < n_cells; e += gridDim.x) {
+    for (int t = threadIdx.x; t < nf3; t += blockDim.x) {
+      const uint32_t df = map_f[e * nf3 + t];
+      s0[t] = df != MFGB_INVALID_DOF ? rf[df] * inv_val_f[df] : T(0);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * nf * nf; t += blockDim.x) {  // along i: [a][jf][kf]
+      const int a = t / (nf * nf), jk = t % (nf * nf);
+      T s = 0;
+      for (int i = 0; i < nf; ++i) s += bval<T>(P, i * nc + a) * s0[i * nf * nf + jk];
+      s1[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * nc * nf; t += blockDim.x) {  // along j: [a][b][kf]
+      const int a = t / (nc * nf), b = (t / nf) % nc, kf = t % nf;
+      T s = 0;
+      for (int j = 0; j < nf; ++j) s += bval<T>(P, j * nc + b) * s1[(a * nf + j) * nf + kf];
+      s0[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc3; t += blockDim.x) {  // along k: [a][b][c]
+      const int a = t / (nc * nc), b = (t / nc) % nc, c = t % nc;
+      const uint32_t dc = map_c[e * nc3 + t];
+      if (dc == MFGB_INVALID_DOF) continue;
+      T s = 0;
+      for (int k = 0; k < nf; ++k) s += bval<T>(P, k * nc + c) * s0[(a * nc + b) * nf + k];
+      atomicAdd(rc + dc, s);
+    }
+    __syncthreads();
+  }
+}
+
 // ---- h-transfer between nested structured Q1 grids -----------------------
 // fine grid (2nx+1)(2ny+1)(2nz+1) nodes, coarse (nx+1)(ny+1)(nz+1), x fastest
 struct HGrid {
@@ -547,7 +627,7 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
   if (L.to_coarse == 1) {
     const PTransferParams P = ptransfer(L.op, C.op);
     if ((st = cuda_status(cudaMemsetAsync(C.b, 0, sizeof(T) * C.n, s), "coarse b = 0"))) return st;
-    k_p_restrict<T><<<grid1d(L.op->n_cells * C.op->n * C.op->n * C.op->n), T256, 0, s>>>(
+    k_p_restrict_sf<T><<<(unsigned)std::min<int64_t>(L.op->n_cells, 152 * 16), 128, 0, s>>>(
         L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)L.r, (const T *)L.inv_val, (T *)C.b, P);
   } else {
     k_h_restrict<T><<<grid1d(C.n), T256, 0, s>>>(hgrid(L.box, C.box), (const T *)L.r, (T *)C.b);
@@ -557,7 +637,7 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
   if (L.to_coarse == 1) {
     const PTransferParams P = ptransfer(L.op, C.op);
     if ((st = cuda_status(cudaMemsetAsync(L.t, 0, sizeof(T) * L.n, s), "t = 0"))) return st;
-    k_p_prolongate<T><<<grid1d(L.op->n_cells * L.op->n * L.op->n * L.op->n), T256, 0, s>>>(
+    k_p_prolongate_sf<T><<<(unsigned)std::min<int64_t>(L.op->n_cells, 152 * 16), 128, 0, s>>>(
         L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)C.x, (T *)L.t, P);
     k_axpy<T><<<grid1d(L.n), T256, 0, s>>>(L.n, (T)1, (const T *)L.t, (T *)L.x);
   } else {
@@ -628,7 +708,13 @@ mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
     if ((st = mfgb_dot(n, v, v, &nv, nullptr))) return st;
     const double inv = nv > 0 ? 1.0 / std::sqrt(nv) : 0.0;
     k_axpy<double><<<grid1d(n), T256>>>(n, inv - 1.0, v, v);  // v *= inv
-    if ((st = vmult_impl(L.op, w, v, MFGB_ARITH_FP64, nullptr, nullptr, nullptr))) return st;
+    if (prec == 32) {  // the smoother's own FP32 operator, on a float copy
+      k_convert<float, double><<<grid1d(n), T256>>>(n, v, (float *)L.t);
+      if ((st = level_vmult(L.op, 32, L.d, L.t, nullptr))) return st;
+      k_convert<double, float><<<grid1d(n), T256>>>(n, (const float *)L.d, w);
+    } else if ((st = vmult_impl(L.op, w, v, MFGB_ARITH_FP64_DF, nullptr, nullptr, nullptr))) {
+      return st;
+    }
     if (L.op->n_constrained)  // power iteration on the unconstrained block
       k_set_constrained<double><<<grid1d(L.op->n_constrained), T256>>>(L.op->n_constrained,
                                                                         L.op->d_constrained, w, 0.0);
@@ -969,6 +1055,10 @@ extern "C" mfgb_status mfgb_mg_cg_solve(const mfgb_operator *cop, mfgb_mg *mg, c
   }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
+  if (result == MFGB_OK || result == MFGB_ERR_NOT_CONVERGED) {
+    const mfgb_status dev = mfgb_check_device_errors(s);
+    if (dev) return dev;
+  }
   if (result == MFGB_ERR_NOT_CONVERGED) set_error("mfgb_mg_cg_solve: max_steps reached");
   return result;
 }

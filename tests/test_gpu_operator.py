@@ -246,3 +246,49 @@ def test_bk6_vector_operator(mf, orc, p, arith):
 def torch_zeros(n):
     import torch
     return torch.zeros(n, dtype=torch.float64, device="cuda")
+
+
+@pytest.mark.parametrize("p", [2, 4, 8])
+def test_fp32_tma_tail_batch(mf, orc, p):
+    """FP32 geometric factors in an odd last batch (a 4-byte tile that is not a
+    16-byte multiple) go through plain loads: correct result, no timeout."""
+    import ctypes
+    import torch
+    from benchmarks_gb300 import _abi
+    L = mf.lib()
+    old = ctypes.c_int()
+    _abi.check(L.mfgb_get_kernel_shape(2, p, ctypes.byref(old)))
+    try:
+        _abi.check(L.mfgb_set_kernel_shape(2, p, 2))
+        cells = (3, 3, 3)  # 27 cells: odd last batch for every batch size
+        A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.1))
+        ref = orc.BoxProblem(*cells, p, amplitude=0.1)
+        src = np.random.default_rng(1).uniform(-1, 1, ref.n_dofs)
+        s32 = torch.from_numpy(src.astype(np.float32)).cuda()
+        d32 = torch.zeros_like(s32)
+        _abi.check(L.mfgb_vmult_f32(A.handle, ctypes.c_void_p(d32.data_ptr()),
+                                    ctypes.c_void_p(s32.data_ptr()), mf._stream_ptr()))
+        _abi.check(L.mfgb_check_device_errors(None))
+        assert rel(d32.cpu().numpy().astype(np.float64), ref.apply(src)) <= 1e-5
+    finally:
+        _abi.check(L.mfgb_set_kernel_shape(2, p, old.value))
+
+
+def test_autotune_small(mf, tmp_path):
+    """The autotuner times each shape, restores the table, and round-trips."""
+    import ctypes
+    from benchmarks_gb300 import _abi, autotune
+    L = mf.lib()
+    before = ctypes.c_int()
+    _abi.check(L.mfgb_get_kernel_shape(1, 3, ctypes.byref(before)))
+    r = autotune.tune(degrees=[3], ariths=("df", "fp32"), target_dofs=2e5, reps=2, apply=False)
+    after = ctypes.c_int()
+    _abi.check(L.mfgb_get_kernel_shape(1, 3, ctypes.byref(after)))
+    assert after.value == before.value
+    for name in ("df", "fp32"):
+        e = r[name][3]
+        assert e["best"] in autotune.SHAPES and len(e["ms"]) == 3 and min(e["ms"]) > 0
+    path = tmp_path / "tune.json"
+    autotune.save(r, path)
+    r2 = autotune.load(path, apply=False)
+    assert r2["df"]["3"]["best"] == r["df"][3]["best"]
