@@ -237,7 +237,8 @@ class PreconditionIdentity:
 
 class MGPreconditioner:
     """Geometric p-/h-multigrid V-cycle for a box mesh (mfgb_mg_* in the C ABI):
-    p_fine -> p_fine/2 -> ... -> 1, then Q1 on 2:1 coarsened meshes; Chebyshev
+    p_fine -> p_fine/2 -> ... -> 1, then Q1 on coarsened meshes (level l keeps
+    the fine nodes min(k 2^l, n) of each axis, nested for any n); Chebyshev
     smoothing around Jacobi; FP64 Jacobi-CG coarse solve.  ``precision`` 32
     runs the V-cycle in FP32 (the mixed-precision preconditioner inside FP64
     CG), 64 in FP64."""

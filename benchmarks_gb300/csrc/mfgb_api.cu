@@ -215,7 +215,8 @@ mfgb_status mfgb_get_kernel_shape(int arith, int degree, int *shape) {
   return MFGB_OK;
 }
 
-static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out);
+static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out,
+                                   const BoxStride *bs = nullptr);
 
 mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **out) {
   return create_box_impl(box, 0, out);
@@ -225,7 +226,8 @@ mfgb_status mfgb_operator_create_box_gauss(const mfgb_box_desc *box, mfgb_operat
   return create_box_impl(box, 1, out);
 }
 
-static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out) {
+static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out,
+                                   const BoxStride *bs) {
   if (!box || !out) {
     set_error("mfgb_operator_create_box: null argument");
     return MFGB_ERR_INVALID_ARG;
@@ -285,7 +287,7 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
                         "constraints copy")) ||
       (st = cuda_status(box_map(*box, op->d_map, nullptr), "box map")) ||
       (st = cuda_status(box_geometry(*box, op->gll_x, op->gll_w, op->D, op->d_G, nullptr,
-                                     quadrature != 0),
+                                     quadrature != 0, bs),
                         "box geometry")) ||
       (st = cuda_status(cudaDeviceSynchronize(), "box set-up"))) {
     free_operator(op);
@@ -544,3 +546,8 @@ mfgb_status mfgb_rhs_uniform(const mfgb_operator *op, uint64_t seed, double *d_b
 }
 
 }  // extern "C"
+
+mfgb_status mfgb::create_box_strided(const mfgb_box_desc *box, const BoxStride *bs,
+                                     mfgb_operator **out) {
+  return create_box_impl(box, 0, out, bs);
+}

@@ -76,8 +76,17 @@ cudaError_t bk6_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G,
 
 // set-up kernels (mfgb_setup.cu)
 cudaError_t box_map(const mfgb_box_desc &b, uint32_t *d_map, cudaStream_t s);
+// A coarsened box level: cell c of an axis spans fine mesh nodes
+// [min(c s, nf), min((c+1) s, nf)] of a uniform nf-cell axis, so the levels
+// of any nf stay nested (only the last cell of an axis can be narrower).
+// b.nx = ceil(nf[0] / s) etc.; s <= 1 is the uniform box itself.
+struct BoxStride {
+  int nf[3];
+  int s;
+};
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
-                         const double *D, double *d_G, cudaStream_t s, bool at_gauss = false);
+                         const double *D, double *d_G, cudaStream_t s, bool at_gauss = false,
+                         const BoxStride *bs = nullptr);
 cudaError_t g_to_df(int64_t n, const double *G, float2 *Gdf, cudaStream_t s);
 cudaError_t g_to_f32(int64_t n, const double *G, float *G32, cudaStream_t s);
 cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,
@@ -89,6 +98,8 @@ cudaError_t copy_constrained(int64_t n_constrained, const int64_t *constrained, 
 cudaError_t invert_diagonal(int64_t n, double *d, cudaStream_t s);
 
 // operator helpers (mfgb_api.cu)
+mfgb_status create_box_strided(const mfgb_box_desc *box, const BoxStride *bs,
+                               mfgb_operator **out);
 mfgb_status ensure_df(mfgb_operator *op);
 mfgb_status ensure_partials(mfgb_operator *op, int n);
 // dst += A src (cell loop only: no zeroing, no identity rows); `done` lets

@@ -278,14 +278,24 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---- h-transfer between nested structured Q1 grids -----------------------
-// fine grid (2nx+1)(2ny+1)(2nz+1) nodes, coarse (nx+1)(ny+1)(nz+1), x fastest
+// Level nodes of an axis sit at fine mesh nodes min(k s, nf) (BoxStride); the
+// coarse level (stride 2s) keeps every other node and the last one.  x fastest.
 struct HGrid {
   int64_t fx, fy, fz, cx, cy, cz;  // node counts
+  int nf[3];                       // cells of the uniform mesh the strides refer to
+  int s;                           // stride of the fine level
 };
 
-__device__ __forceinline__ int hw(int64_t I, int64_t c) {  // 1D weight * 2 of coarse c at fine I
-  const int64_t d = I - 2 * c;
-  return d == 0 ? 2 : ((d == 1 || d == -1) ? 1 : 0);
+// 1D Q1 interpolation weight of coarse node c at fine node I: an even fine
+// node is coarse node I/2; an odd one lies between (I-1)/2 and (I+1)/2 at
+// the fraction of their distance its position gives (1/2 unless the last
+// coarse cell is narrower)
+__device__ __forceinline__ double hw(int64_t I, int64_t c, int nf, int s) {
+  if ((I & 1) == 0) return c == (I >> 1) ? 1.0 : 0.0;
+  const int64_t L = (I - 1) >> 1;
+  const int64_t A = (I - 1) * s, P = min(I * s, (int64_t)nf), B = min((I + 1) * s, (int64_t)nf);
+  const double wr = (double)(P - A) / (double)(B - A);
+  return c == L ? 1.0 - wr : (c == L + 1 ? wr : 0.0);
 }
 
 // x_f += P x_c on interior fine nodes
@@ -299,7 +309,8 @@ __global__ void k_h_prolongate_add(HGrid g, const T *__restrict__ xc, T *__restr
     for (int64_t kk = k0; kk <= k0 + (K & 1); ++kk)
       for (int64_t jj = j0; jj <= j0 + (J & 1); ++jj)
         for (int64_t ii = i0; ii <= i0 + (I & 1); ++ii) {
-          const T w = (T)(hw(I, ii) * hw(J, jj) * hw(K, kk)) * (T)0.125;
+          const T w = (T)(hw(I, ii, g.nf[0], g.s) * hw(J, jj, g.nf[1], g.s) *
+                          hw(K, kk, g.nf[2], g.s));
           acc += w * xc[ii + g.cx * (jj + g.cy * kk)];
         }
     xf[t] += acc;
@@ -315,11 +326,12 @@ __global__ void k_h_restrict(HGrid g, const T *__restrict__ rf, T *__restrict__ 
       rc[t] = 0;
       continue;
     }
-    T acc = 0;
+    T acc = 0;  // fine neighbours 2i-1 .. 2i+1 exist for every interior coarse node
     for (int64_t K = 2 * k - 1; K <= 2 * k + 1; ++K)
       for (int64_t J = 2 * j - 1; J <= 2 * j + 1; ++J)
         for (int64_t I = 2 * i - 1; I <= 2 * i + 1; ++I) {
-          const T w = (T)(hw(I, i) * hw(J, j) * hw(K, k)) * (T)0.125;
+          const T w = (T)(hw(I, i, g.nf[0], g.s) * hw(J, j, g.nf[1], g.s) *
+                          hw(K, k, g.nf[2], g.s));
           acc += w * rf[I + g.fx * (J + g.fy * K)];
         }
     rc[t] = acc;
@@ -489,6 +501,7 @@ __global__ void k_copy_scalar(double *__restrict__ scal, int from, int to) {
 
 struct MgLevel {
   mfgb_box_desc box{};
+  BoxStride bs{};  // s = 1 on the fine mesh (p-levels), 2^l on the l-th h-level
   mfgb_operator *op = nullptr;
   int64_t n = 0;
   void *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *t = nullptr;
@@ -589,9 +602,10 @@ mfgb_status chebyshev(const MgLevel &L, int degree, double range, bool zero_star
   return cuda_status(cudaGetLastError(), "chebyshev");
 }
 
-HGrid hgrid(const mfgb_box_desc &fine, const mfgb_box_desc &coarse) {
-  return HGrid{fine.nx + 1, fine.ny + 1, fine.nz + 1, coarse.nx + 1, coarse.ny + 1,
-               coarse.nz + 1};
+HGrid hgrid(const MgLevel &fine, const MgLevel &coarse) {
+  return HGrid{fine.box.nx + 1, fine.box.ny + 1, fine.box.nz + 1,
+               coarse.box.nx + 1, coarse.box.ny + 1, coarse.box.nz + 1,
+               {fine.bs.nf[0], fine.bs.nf[1], fine.bs.nf[2]}, fine.bs.s};
 }
 
 PTransferParams ptransfer(const mfgb_operator *fine, const mfgb_operator *coarse) {
@@ -630,7 +644,7 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
     k_p_restrict_sf<T><<<(unsigned)std::min<int64_t>(L.op->n_cells, 152 * 16), 128, 0, s>>>(
         L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)L.r, (const T *)L.inv_val, (T *)C.b, P);
   } else {
-    k_h_restrict<T><<<grid1d(C.n), T256, 0, s>>>(hgrid(L.box, C.box), (const T *)L.r, (T *)C.b);
+    k_h_restrict<T><<<grid1d(C.n), T256, 0, s>>>(hgrid(L, C), (const T *)L.r, (T *)C.b);
   }
   if ((st = cuda_status(cudaGetLastError(), "restrict"))) return st;
   if ((st = vcycle<T>(mg, l + 1, s))) return st;
@@ -641,7 +655,7 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
         L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)C.x, (T *)L.t, P);
     k_axpy<T><<<grid1d(L.n), T256, 0, s>>>(L.n, (T)1, (const T *)L.t, (T *)L.x);
   } else {
-    k_h_prolongate_add<T><<<grid1d(L.n), T256, 0, s>>>(hgrid(L.box, C.box), (const T *)C.x,
+    k_h_prolongate_add<T><<<grid1d(L.n), T256, 0, s>>>(hgrid(L, C), (const T *)C.x,
                                                         (T *)L.x);
   }
   if ((st = cuda_status(cudaGetLastError(), "prolongate"))) return st;
@@ -764,21 +778,26 @@ extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_pa
   mg->coarse_tol = prm->coarse_tol > 0 ? prm->coarse_tol : 1e-12;
   // level boxes: p-coarsening by halving, then h-coarsening of Q1 by 2
   std::vector<mfgb_box_desc> boxes;
-  std::vector<int> kinds;
+  std::vector<int> kinds, strides;
   mfgb_box_desc b = *fine;
   // every level keeps the fine level's geometry degree (coarse Q1 cells of a
   // deformed mesh would otherwise fold)
   b.geometry_degree = fine->geometry_degree > 0 ? fine->geometry_degree : fine->degree;
   boxes.push_back(b);
+  strides.push_back(1);
   while (b.degree > 1) {
     b.degree = std::max(1, b.degree / 2);
     boxes.push_back(b);
+    strides.push_back(1);
     kinds.push_back(1);
   }
-  while (std::max({b.nx, b.ny, b.nz}) > prm->coarse_cells && b.nx % 2 == 0 && b.ny % 2 == 0 &&
-         b.nz % 2 == 0) {
-    b.nx /= 2; b.ny /= 2; b.nz /= 2;
+  // h-levels: stride 2^l, ceil(n / 2^l) cells per axis (nested for any n)
+  for (int s = 2; std::max({b.nx, b.ny, b.nz}) > prm->coarse_cells; s *= 2) {
+    b.nx = (fine->nx + s - 1) / s;
+    b.ny = (fine->ny + s - 1) / s;
+    b.nz = (fine->nz + s - 1) / s;
     boxes.push_back(b);
+    strides.push_back(s);
     kinds.push_back(2);
   }
   kinds.push_back(0);
@@ -788,7 +807,8 @@ extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_pa
     MgLevel L;
     L.box = boxes[l];
     L.to_coarse = kinds[l];
-    st = mfgb_operator_create_box(&boxes[l], &L.op);
+    L.bs = BoxStride{{fine->nx, fine->ny, fine->nz}, strides[l]};
+    st = create_box_strided(&boxes[l], &L.bs, &L.op);
     if (st) break;
     L.n = L.op->n_dofs;
     mg->levels.push_back(L);

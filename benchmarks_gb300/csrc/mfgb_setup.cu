@@ -107,7 +107,15 @@ struct GeomParams {
   double V[81], Dv[81];   // V[i*ng+a] = l_a(x_i), Dv[i*ng+a] = l_a'(x_i) (geometry basis)
   int ng;                 // geometry points per direction
   int general;            // 0: targets are the geometry nodes (J by the square D)
+  int nf[3], s;           // axis spans in fine-mesh units (BoxStride)
 };
+
+// fine-node range [a, b) of cell c on an axis of nf fine cells coarsened by s
+__device__ __forceinline__ void axis_span(int64_t c, int nf, int s, double &a, double &w) {
+  const int64_t lo = min(c * s, (int64_t)nf), hi = min((c + 1) * s, (int64_t)nf);
+  a = (double)lo;
+  w = (double)(hi - lo);
+}
 
 // One CTA per cell: the deformed geometry nodes (GLL points of the geometry
 // degree) in shared memory, then J = dx/dxi at the operator's GLL points
@@ -119,14 +127,18 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
   const int ng = gp.ng, ng3 = ng * ng * ng;
   const int64_t e = blockIdx.x;
   const int64_t cx = e % b.nx, cy = (e / b.nx) % b.ny, cz = e / ((int64_t)b.nx * b.ny);
-  const double hx = (b.hi[0] - b.lo[0]) / b.nx, hy = (b.hi[1] - b.lo[1]) / b.ny,
-               hz = (b.hi[2] - b.lo[2]) / b.nz;
+  const double hx = (b.hi[0] - b.lo[0]) / gp.nf[0], hy = (b.hi[1] - b.lo[1]) / gp.nf[1],
+               hz = (b.hi[2] - b.lo[2]) / gp.nf[2];
+  double ax, wx, ay, wy, az, wz;  // uniform box: a = c, w = 1 (the same bits as c + t)
+  axis_span(cx, gp.nf[0], gp.s, ax, wx);
+  axis_span(cy, gp.nf[1], gp.s, ay, wy);
+  axis_span(cz, gp.nf[2], gp.s, az, wz);
   const double two_pi = 2.0 * M_PI;
   for (int l = threadIdx.x; l < ng3; l += blockDim.x) {
     const int i = l / (ng * ng), j = (l / ng) % ng, k = l % ng;
-    const double X = b.lo[0] + ((double)cx + 0.5 * (gp.xg[k] + 1.0)) * hx;
-    const double Y = b.lo[1] + ((double)cy + 0.5 * (gp.xg[j] + 1.0)) * hy;
-    const double Z = b.lo[2] + ((double)cz + 0.5 * (gp.xg[i] + 1.0)) * hz;
+    const double X = b.lo[0] + (ax + 0.5 * (gp.xg[k] + 1.0) * wx) * hx;
+    const double Y = b.lo[1] + (ay + 0.5 * (gp.xg[j] + 1.0) * wy) * hy;
+    const double Z = b.lo[2] + (az + 0.5 * (gp.xg[i] + 1.0) * wz) * hz;
     const double s = b.amplitude * sin(two_pi * X) * sin(two_pi * Y) * sin(two_pi * Z);
     xyz[3 * l + 0] = X + s;
     xyz[3 * l + 1] = Y + s;
@@ -216,8 +228,19 @@ void gauss_nodes(int n, double *x, double *w) {
 }
 
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
-                         const double *D, double *d_G, cudaStream_t s, bool at_gauss) {
+                         const double *D, double *d_G, cudaStream_t s, bool at_gauss,
+                         const BoxStride *bs) {
   GeomParams gp{};
+  if (bs && bs->s > 1) {
+    for (int d = 0; d < 3; ++d) gp.nf[d] = bs->nf[d];
+    gp.s = bs->s;
+    if ((b.nx != (gp.nf[0] + gp.s - 1) / gp.s) || (b.ny != (gp.nf[1] + gp.s - 1) / gp.s) ||
+        (b.nz != (gp.nf[2] + gp.s - 1) / gp.s))
+      return cudaErrorInvalidValue;
+  } else {
+    gp.nf[0] = b.nx; gp.nf[1] = b.ny; gp.nf[2] = b.nz;
+    gp.s = 1;
+  }
   const int n = b.degree + 1;
   const int g = b.geometry_degree > 0 ? b.geometry_degree : b.degree;
   if (g < 1 || g > 8) return cudaErrorInvalidValue;

@@ -178,17 +178,25 @@ void orc_box_cell_nodes(const orc_box *b, int64_t cell, double *xyz) {
   const int n = geo_degree(b) + 1;
   double xg[16], wg[16];
   orc_gll(n, xg, wg);
-  const int64_t cx = cell % b->nx, cy = (cell / b->nx) % b->ny, cz = cell / ((int64_t)b->nx * b->ny);
-  const double hx = (b->hi[0] - b->lo[0]) / b->nx;
-  const double hy = (b->hi[1] - b->lo[1]) / b->ny;
-  const double hz = (b->hi[2] - b->lo[2]) / b->nz;
+  const int64_t c[3] = {cell % b->nx, (cell / b->nx) % b->ny, cell / ((int64_t)b->nx * b->ny)};
+  const int strided = b->stride > 1;
+  const int s = strided ? b->stride : 1;
+  const int nc[3] = {b->nx, b->ny, b->nz};
+  double h[3], a[3], w[3];  /* node range [a, a + w) of the cell in units of h */
+  for (int d = 0; d < 3; ++d) {
+    const int64_t nf = strided ? b->nf[d] : nc[d];
+    const int64_t lo = c[d] * s < nf ? c[d] * s : nf, hi = (c[d] + 1) * s < nf ? (c[d] + 1) * s : nf;
+    h[d] = (b->hi[d] - b->lo[d]) / (double)nf;
+    a[d] = (double)lo;
+    w[d] = (double)(hi - lo);
+  }
   const double two_pi = 2.0 * M_PI;
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j)
       for (int k = 0; k < n; ++k) {
-        const double X = b->lo[0] + ((double)cx + 0.5 * (xg[k] + 1.0)) * hx;
-        const double Y = b->lo[1] + ((double)cy + 0.5 * (xg[j] + 1.0)) * hy;
-        const double Z = b->lo[2] + ((double)cz + 0.5 * (xg[i] + 1.0)) * hz;
+        const double X = b->lo[0] + (a[0] + 0.5 * (xg[k] + 1.0) * w[0]) * h[0];
+        const double Y = b->lo[1] + (a[1] + 0.5 * (xg[j] + 1.0) * w[1]) * h[1];
+        const double Z = b->lo[2] + (a[2] + 0.5 * (xg[i] + 1.0) * w[2]) * h[2];
         const double s = b->amplitude * sin(two_pi * X) * sin(two_pi * Y) * sin(two_pi * Z);
         double *o = xyz + 3 * (i * n * n + j * n + k);
         o[0] = X + s;

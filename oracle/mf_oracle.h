@@ -47,6 +47,9 @@ typedef struct {
   double lo[3], hi[3];/* box corners */
   double amplitude;   /* x_d += a sin(2 pi x) sin(2 pi y) sin(2 pi z) */
   int geometry_degree;/* Q_g geometry from the deformed GLL nodes of degree g (0: g = degree) */
+  int stride;         /* coarsened level (> 1): cell c of an axis spans the nodes */
+  int nf[3];          /* [min(c s, nf), min((c+1) s, nf)] of a uniform nf-cell axis;
+                         nx = ceil(nf[0] / s) etc.  0 / 1: the uniform box itself */
 } orc_box;
 
 int64_t orc_box_n_dofs(const orc_box *b);

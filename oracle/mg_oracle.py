@@ -5,9 +5,11 @@ as the CUDA library, in FP64 numpy over the C oracle's operator.
 The reference has no multigrid for this path, so this oracle restates the
 standard algorithms the library implements (parity unpinned by the
 reference):
-  * levels: p -> p//2 -> ... -> 1 on the fine mesh, then Q1 on 2:1 coarsened
-    meshes while all cell counts are even and the largest exceeds coarse_cells;
-    every level keeps the fine degree's geometry interpolant
+  * levels: p -> p//2 -> ... -> 1 on the fine mesh, then Q1 on coarsened
+    meshes while the largest cell count exceeds coarse_cells: level l keeps
+    the fine nodes min(k 2^l, n) of each axis (ceil(n / 2^l) cells, nested for
+    any n; only the last cell of an axis can be narrower); every level keeps
+    the fine degree's geometry interpolant
   * p-transfer: cell-wise tensor-product Lagrange interpolation at the fine
     GLL points; restriction = transpose with 1/valence weighting of fine DoFs
   * h-transfer: Q1 interpolation on nested structured grids
@@ -37,11 +39,13 @@ def _power_start(n: int) -> np.ndarray:
 
 
 class Level:
-    def __init__(self, nx, ny, nz, degree, amplitude, geometry_degree=0):
+    def __init__(self, nx, ny, nz, degree, amplitude, geometry_degree=0, stride=1,
+                 nf=(0, 0, 0)):
         self.box = (nx, ny, nz)
         self.degree = degree
+        self.stride, self.nf = stride, nf
         self.prob = orc.BoxProblem(nx, ny, nz, degree, amplitude=amplitude,
-                                   geometry_degree=geometry_degree)
+                                   geometry_degree=geometry_degree, stride=stride, nf=nf)
         self.n = self.prob.n_dofs
         d = self.prob.diagonal()
         self.dinv = orc.invert_diagonal(d)
@@ -58,20 +62,25 @@ class MGOracle:
                  smoothing_range=15.0, eig_iterations=20, coarse_cells=4):
         self.k = chebyshev_degree
         self.range = smoothing_range
-        boxes, kinds = [(nx, ny, nz, degree)], []
+        nf = (nx, ny, nz)
+        boxes, kinds = [(nx, ny, nz, degree, 1)], []
         p = degree
         while p > 1:
             p = max(1, p // 2)
-            boxes.append((nx, ny, nz, p))
+            boxes.append((nx, ny, nz, p, 1))
             kinds.append(1)
-        while max(nx, ny, nz) > coarse_cells and nx % 2 == 0 and ny % 2 == 0 and nz % 2 == 0:
-            nx, ny, nz = nx // 2, ny // 2, nz // 2
-            boxes.append((nx, ny, nz, 1))
+        s = 2
+        while max(nx, ny, nz) > coarse_cells:
+            nx, ny, nz = (-(-f // s) for f in nf)
+            boxes.append((nx, ny, nz, 1, s))
             kinds.append(2)
+            s *= 2
         kinds.append(0)
+        self.nf = nf
         self.levels = []
-        for (bx, by, bz, bp), kind in zip(boxes, kinds):
-            L = Level(bx, by, bz, bp, amplitude, geometry_degree=degree)
+        for (bx, by, bz, bp, bs), kind in zip(boxes, kinds):
+            L = Level(bx, by, bz, bp, amplitude, geometry_degree=degree, stride=bs,
+                      nf=nf if bs > 1 else (0, 0, 0))
             L.to_coarse = kind
             self.levels.append(L)
         for L in self.levels[:-1]:
@@ -139,19 +148,29 @@ class MGOracle:
         return rc
 
     @staticmethod
-    def _h_matrix_1d(nc_cells):
-        """fine (2n+1) x coarse (n+1) Q1 interpolation in one direction."""
-        P = np.zeros((2 * nc_cells + 1, nc_cells + 1))
-        for I in range(2 * nc_cells + 1):
+    def _h_matrix_1d(nf, s):
+        """Q1 interpolation on one axis from the level of stride 2s to the level
+        of stride s: [fine nodes, coarse nodes]; node k of a level sits at fine
+        mesh node min(k stride, nf)."""
+        m = -(-nf // s)
+        mc = -(-nf // (2 * s))
+        P = np.zeros((m + 1, mc + 1))
+        for I in range(m + 1):
             if I % 2 == 0:
                 P[I, I // 2] = 1.0
             else:
-                P[I, I // 2] = P[I, I // 2 + 1] = 0.5
+                A, pos, B = (I - 1) * s, min(I * s, nf), min((I + 1) * s, nf)
+                w = (pos - A) / (B - A)
+                P[I, I // 2] = 1.0 - w
+                P[I, I // 2 + 1] = w
         return P
+
+    def _h_mats(self, L):
+        return [self._h_matrix_1d(f, L.stride) for f in self.nf]
 
     def h_prolongate_add(self, L, C, xc, xf):
         cx, cy, cz = C.box
-        Px, Py, Pz = (self._h_matrix_1d(c) for c in (cx, cy, cz))
+        Px, Py, Pz = self._h_mats(L)
         X = xc.reshape(cz + 1, cy + 1, cx + 1)
         F = np.einsum("Kk,Jj,Ii,kji->KJI", Pz, Py, Px, X).reshape(-1)
         mask = np.ones(L.n, bool)
@@ -159,9 +178,9 @@ class MGOracle:
         return xf + np.where(mask, F, 0.0)
 
     def h_restrict(self, L, C, rf):
-        cx, cy, cz = C.box
-        Px, Py, Pz = (self._h_matrix_1d(c) for c in (cx, cy, cz))
-        R = rf.reshape(2 * cz + 1, 2 * cy + 1, 2 * cx + 1)
+        fx, fy, fz = L.box
+        Px, Py, Pz = self._h_mats(L)
+        R = rf.reshape(fz + 1, fy + 1, fx + 1)
         rc = np.einsum("Kk,Jj,Ii,KJI->kji", Pz, Py, Px, R).reshape(-1)
         rc[C.constrained] = 0.0
         return rc

@@ -42,6 +42,7 @@ class _Box(ctypes.Structure):
         ("degree", ctypes.c_int),
         ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
         ("amplitude", ctypes.c_double), ("geometry_degree", ctypes.c_int),
+        ("stride", ctypes.c_int), ("nf", ctypes.c_int * 3),
     ]
 
 
@@ -161,11 +162,18 @@ class BoxProblem:
     lo: tuple = (0.0, 0.0, 0.0)
     hi: tuple = (1.0, 1.0, 1.0)
     geometry_degree: int = 0
+    stride: int = 1            # > 1: coarsened level of a uniform mesh with nf cells
+    nf: tuple = (0, 0, 0)      # per axis (nx = ceil(nf / stride))
 
     def __post_init__(self):
+        if self.stride > 1:
+            for n, f in zip((self.nx, self.ny, self.nz), self.nf):
+                if n != -(-f // self.stride):
+                    raise ValueError("cell counts must be ceil(nf / stride)")
         self._box = _Box(self.nx, self.ny, self.nz, self.degree,
                          (ctypes.c_double * 3)(*self.lo), (ctypes.c_double * 3)(*self.hi),
-                         self.amplitude, self.geometry_degree)
+                         self.amplitude, self.geometry_degree, self.stride,
+                         (ctypes.c_int * 3)(*self.nf))
         L = lib()
         self.n = self.degree + 1
         self.n_dofs = int(L.orc_box_n_dofs(ctypes.byref(self._box)))

@@ -98,3 +98,43 @@ def test_mg_cg_matches_oracle_and_mixed_precision(mf, orc, mgo):
     x = A.initialize_dof_vector()
     mf.SolverCG(ctl).solve(A, x, b, A.get_matrix_diagonal_inverse())
     assert ctl.last_step() > 3 * 25
+
+
+def test_odd_mesh_hierarchy_and_vcycle(mf):
+    """Cell counts that are not powers of two coarsen too (level l keeps the
+    fine nodes min(k 2^l, n)); hierarchy, lambda_max and the FP64 V-cycle
+    match the oracle."""
+    from oracle import mg_oracle
+    mgo = mg_oracle.MGOracle(7, 7, 5, 2, amplitude=0.08, coarse_cells=2)
+    mesh = mf.BoxMesh(7, 7, 5, degree=2, amplitude=0.08)
+    M = mf.MGPreconditioner(mesh, precision=64, coarse_cells=2)
+    assert [l["dofs"] for l in M.levels] == [L.n for L in mgo.levels]
+    assert [l["degree"] for l in M.levels] == [2, 1, 1, 1]
+    for l, L in zip(M.levels[:-1], mgo.levels[:-1]):
+        assert l["lambda_max"] == pytest.approx(L.lmax, rel=1e-10)
+    A = mf.LaplaceOperator(mesh)
+    r = A.rhs_uniform(3)
+    z = A.initialize_dof_vector()
+    M.vmult(z, r)
+    assert rel(z.cpu().numpy(), mgo.vcycle(r.cpu().numpy())) <= 1e-9
+    x = A.initialize_dof_vector()
+    ctl = mf.ReductionControl(200, 1e-300, 1e-10)
+    mf.SolverCG(ctl).solve(A, x, r, M)
+    _, info = mgo.pcg(r.cpu().numpy(), reduce=1e-10)
+    assert abs(ctl.last_step() - info["steps"]) <= 1 and ctl.last_step() <= 30
+
+
+@pytest.mark.parametrize("n", [19, 25, 31])
+def test_odd_mesh_mg_cg_converges_fast(mf, n):
+    """Odd cell counts that used to leave a coarse problem too large for the
+    dense coarse solve now reach the 4^3 coarse mesh."""
+    mesh = mf.BoxMesh(n, n, n, degree=2, amplitude=0.05)
+    M = mf.MGPreconditioner(mesh, precision=32)
+    assert M.levels[-1]["dofs"] <= 5 ** 3
+    A = mf.LaplaceOperator(mesh)
+    b = A.rhs_uniform(n)
+    x = A.initialize_dof_vector()
+    ctl = mf.ReductionControl(200, 1e-300, 1e-10)
+    mf.SolverCG(ctl).solve(A, x, b, M)
+    assert ctl.last_value() <= 1e-10 * ctl.initial_value()
+    assert ctl.last_step() <= 25
