@@ -363,3 +363,6 @@ def dot(a, b) -> float:
     _abi.check(lib().mfgb_dot(a.numel(), ctypes.c_void_p(a.data_ptr()),
                               ctypes.c_void_p(b.data_ptr()), ctypes.byref(r), _stream_ptr()))
     return r.value
+
+
+from .batch import BatchSolver, batch_workload  # noqa: E402

@@ -101,6 +101,13 @@ def lib():
         "mfgb_mg_vmult": ([P, P, P, P], I32),
         "mfgb_mg_cg_solve": ([P, P, P, P, ctypes.POINTER(CgControl), ctypes.POINTER(SolveInfo), P],
                              I32),
+        "mfgb_batch_create": ([ctypes.POINTER(BoxDesc), I32, ctypes.POINTER(MgParams), PP], I32),
+        "mfgb_batch_destroy": ([P], I32),
+        "mfgb_batch_info": ([P, P, P, P, P, P], I32),
+        "mfgb_batch_rhs_uniform": ([P, P, P, P], I32),
+        "mfgb_batch_vmult": ([P, P, P, P], I32),
+        "mfgb_batch_precondition": ([P, P, P, P], I32),
+        "mfgb_batch_cg_solve": ([P, P, P, ctypes.POINTER(CgControl), P, P], I32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)

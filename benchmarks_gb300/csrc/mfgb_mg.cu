@@ -25,332 +25,12 @@
 
 #include "mfgb_common.cuh"
 #include "mfgb_internal.h"
+#include "mfgb_mg_kernels.cuh"
+#include "mfgb_mg_internal.h"
 
 namespace mfgb {
 
 namespace {
-
-constexpr int T256 = 256;
-
-unsigned grid1d(int64_t n) {
-  const int64_t g = (n + T256 - 1) / T256;
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
-}
-
-#define GRID_STRIDE(t, n)                                                             \
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (n); \
-       t += (int64_t)gridDim.x * blockDim.x)
-
-template <class T>
-__global__ void k_fill(int64_t n, T *x, T v) {
-  GRID_STRIDE(t, n) x[t] = v;
-}
-
-template <class T>
-__global__ void k_copy_constrained(int64_t nc, const int64_t *__restrict__ c,
-                                   const T *__restrict__ src, T *__restrict__ dst) {
-  GRID_STRIDE(t, nc) dst[c[t]] = src[c[t]];
-}
-
-template <class T>
-__global__ void k_set_constrained(int64_t nc, const int64_t *__restrict__ c, T *__restrict__ v,
-                                  T val) {
-  GRID_STRIDE(t, nc) v[c[t]] = val;
-}
-
-template <class TO, class TI>
-__global__ void k_convert(int64_t n, const TI *__restrict__ a, TO *__restrict__ b) {
-  GRID_STRIDE(t, n) b[t] = (TO)a[t];
-}
-
-// Chebyshev first step from x0 = 0: x = d = (1/theta) Dinv b ; r = b
-template <class T>
-__global__ void k_cheb_first_zero(int64_t n, const T *__restrict__ b, const T *__restrict__ dinv,
-                                  T *__restrict__ x, T *__restrict__ d, T *__restrict__ r,
-                                  T inv_theta) {
-  GRID_STRIDE(t, n) {
-    const T bt = b[t];
-    const T dt = inv_theta * dinv[t] * bt;
-    r[t] = bt;
-    d[t] = dt;
-    x[t] = dt;
-  }
-}
-
-// Chebyshev first step from x0: r = b - Ax (Ax in ax); d = (1/theta) Dinv r; x += d
-template <class T>
-__global__ void k_cheb_first(int64_t n, const T *__restrict__ b, const T *__restrict__ ax,
-                             const T *__restrict__ dinv, T *__restrict__ x, T *__restrict__ d,
-                             T *__restrict__ r, T inv_theta) {
-  GRID_STRIDE(t, n) {
-    const T rt = b[t] - ax[t];
-    const T dt = inv_theta * dinv[t] * rt;
-    r[t] = rt;
-    d[t] = dt;
-    x[t] += dt;
-  }
-}
-
-// r -= A d (in ad); d = c1 d + c2 Dinv r; x += d
-template <class T>
-__global__ void k_cheb_step(int64_t n, const T *__restrict__ ad, const T *__restrict__ dinv,
-                            T *__restrict__ x, T *__restrict__ d, T *__restrict__ r, T c1, T c2) {
-  GRID_STRIDE(t, n) {
-    const T rt = r[t] - ad[t];
-    const T dt = c1 * d[t] + c2 * dinv[t] * rt;
-    r[t] = rt;
-    d[t] = dt;
-    x[t] += dt;
-  }
-}
-
-// r = b - ax
-template <class T>
-__global__ void k_residual(int64_t n, const T *__restrict__ b, const T *__restrict__ ax,
-                           T *__restrict__ r) {
-  GRID_STRIDE(t, n) r[t] = b[t] - ax[t];
-}
-
-template <class T>
-__global__ void k_axpy(int64_t n, T a, const T *__restrict__ x, T *__restrict__ y) {
-  GRID_STRIDE(t, n) y[t] += a * x[t];
-}
-
-template <class T>
-__global__ void k_scale_by(int64_t n, const T *__restrict__ s, T *__restrict__ v) {
-  GRID_STRIDE(t, n) v[t] *= s[t];
-}
-
-// ---- p-transfer: fine degree pf, coarse degree pc, same cells ------------
-struct PTransferParams {
-  float B32[81];
-  double B64[81];  // B[a*(pc+1) + b] = l^c_b(x^f_a)
-  int nf, nc;      // points per direction (fine, coarse)
-};
-
-template <class T>
-__device__ __forceinline__ T bval(const PTransferParams &P, int idx);
-template <>
-__device__ __forceinline__ float bval<float>(const PTransferParams &P, int idx) {
-  return P.B32[idx];
-}
-template <>
-__device__ __forceinline__ double bval<double>(const PTransferParams &P, int idx) {
-  return P.B64[idx];
-}
-
-// t_f[map_f] = sum_c B(i,a) B(j,b) B(k,c) x_c[map_c]  (plain writes: every cell
-// computes the same value for a shared fine DoF)
-template <class T>
-__global__ void k_p_prolongate(int64_t n_cells, const uint32_t *__restrict__ map_f,
-                               const uint32_t *__restrict__ map_c, const T *__restrict__ xc,
-                               T *__restrict__ tf, PTransferParams P) {
-  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
-  GRID_STRIDE(t, n_cells * nf3) {
-    const int64_t e = t / nf3;
-    const int q = (int)(t - e * nf3);
-    const uint32_t df = map_f[t];
-    if (df == MFGB_INVALID_DOF) continue;
-    const int i = q / (nf * nf), j = (q / nf) % nf, k = q % nf;
-    const uint32_t *mc = map_c + e * nc3;
-    T acc = 0;
-    for (int a = 0; a < nc; ++a) {
-      const T wa = bval<T>(P, i * nc + a);
-      for (int b = 0; b < nc; ++b) {
-        const T wab = wa * bval<T>(P, j * nc + b);
-        for (int c = 0; c < nc; ++c) {
-          const uint32_t dc = mc[a * nc * nc + b * nc + c];
-          if (dc != MFGB_INVALID_DOF) acc += wab * bval<T>(P, k * nc + c) * xc[dc];
-        }
-      }
-    }
-    tf[df] = acc;
-  }
-}
-
-// r_c[map_c] += sum_f B(i,a) B(j,b) B(k,c) r_f[map_f] / valence_f
-template <class T>
-__global__ void k_p_restrict(int64_t n_cells, const uint32_t *__restrict__ map_f,
-                             const uint32_t *__restrict__ map_c, const T *__restrict__ rf,
-                             const T *__restrict__ inv_val_f, T *__restrict__ rc,
-                             PTransferParams P) {
-  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
-  GRID_STRIDE(t, n_cells * nc3) {
-    const int64_t e = t / nc3;
-    const int q = (int)(t - e * nc3);
-    const uint32_t dc = map_c[t];
-    if (dc == MFGB_INVALID_DOF) continue;
-    const int a = q / (nc * nc), b = (q / nc) % nc, c = q % nc;
-    const uint32_t *mf = map_f + e * nf3;
-    T acc = 0;
-    for (int i = 0; i < nf; ++i) {
-      const T wa = bval<T>(P, i * nc + a);
-      for (int j = 0; j < nf; ++j) {
-        const T wab = wa * bval<T>(P, j * nc + b);
-        for (int k = 0; k < nf; ++k) {
-          const uint32_t df = mf[i * nf * nf + j * nf + k];
-          if (df != MFGB_INVALID_DOF) acc += wab * bval<T>(P, k * nc + c) * rf[df] * inv_val_f[df];
-        }
-      }
-    }
-    atomicAdd(rc + dc, acc);
-  }
-}
-
-// Sum-factorised p-transfers: one CTA per cell, three 1D passes through
-// shared memory (nc^3 -> nc*nc*nf -> nc*nf*nf -> nf^3 and back).
-template <class T>
-__global__ void __launch_bounds__(128)
-    k_p_prolongate_sf(int64_t n_cells, const uint32_t *__restrict__ map_f,
-                      const uint32_t *__restrict__ map_c, const T *__restrict__ xc,
-                      T *__restrict__ tf, PTransferParams P) {
-  __shared__ T s0[729], s1[729];
-  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
-  for (int64_t e = blockIdx.x; e < n_cells; e += gridDim.x) {
-    for (int t = threadIdx.x; t < nc3; t += blockDim.x) {
-      const uint32_t dc = map_c[e * nc3 + t];
-      s0[t] = dc != MFGB_INVALID_DOF ? xc[dc] : T(0);
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc * nc * nf; t += blockDim.x) {  // along k: [a][b][kf]
-      const int a = t / (nc * nf), b = (t / nf) % nc, kf = t % nf;
-      T s = 0;
-      for (int c = 0; c < nc; ++c) s += bval<T>(P, kf * nc + c) * s0[(a * nc + b) * nc + c];
-      s1[t] = s;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc * nf * nf; t += blockDim.x) {  // along j: [a][jf][kf]
-      const int a = t / (nf * nf), jf = (t / nf) % nf, kf = t % nf;
-      T s = 0;
-      for (int b = 0; b < nc; ++b) s += bval<T>(P, jf * nc + b) * s1[(a * nc + b) * nf + kf];
-      s0[t] = s;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nf3; t += blockDim.x) {  // along i: [if][jf][kf]
-      const int i = t / (nf * nf), jk = t % (nf * nf);
-      const uint32_t df = map_f[e * nf3 + t];
-      if (df == MFGB_INVALID_DOF) continue;
-      T s = 0;
-      for (int a = 0; a < nc; ++a) s += bval<T>(P, i * nc + a) * s0[a * nf * nf + jk];
-      tf[df] = s;
-    }
-    __syncthreads();
-  }
-}
-
-template <class T>
-__global__ void __launch_bounds__(128)
-    k_p_restrict_sf(int64_t n_cells, const uint32_t *__restrict__ map_f,
-                    const uint32_t *__restrict__ map_c, const T *__restrict__ rf,
-                    const T *__restrict__ inv_val_f, T *__restrict__ rc, PTransferParams P) {
-  __shared__ T s0[729], s1[729];
-  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
-  for (int64_t e = blockIdx.x; e < n_cells; e += gridDim.x) {
-    for (int t = threadIdx.x; t < nf3; t += blockDim.x) {
-      const uint32_t df = map_f[e * nf3 + t];
-      s0[t] = df != MFGB_INVALID_DOF ? rf[df] * inv_val_f[df] : T(0);
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc * nf * nf; t += blockDim.x) {  // along i: [a][jf][kf]
-      const int a = t / (nf * nf), jk = t % (nf * nf);
-      T s = 0;
-      for (int i = 0; i < nf; ++i) s += bval<T>(P, i * nc + a) * s0[i * nf * nf + jk];
-      s1[t] = s;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc * nc * nf; t += blockDim.x) {  // along j: [a][b][kf]
-      const int a = t / (nc * nf), b = (t / nf) % nc, kf = t % nf;
-      T s = 0;
-      for (int j = 0; j < nf; ++j) s += bval<T>(P, j * nc + b) * s1[(a * nf + j) * nf + kf];
-      s0[t] = s;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc3; t += blockDim.x) {  // along k: [a][b][c]
-      const int a = t / (nc * nc), b = (t / nc) % nc, c = t % nc;
-      const uint32_t dc = map_c[e * nc3 + t];
-      if (dc == MFGB_INVALID_DOF) continue;
-      T s = 0;
-      for (int k = 0; k < nf; ++k) s += bval<T>(P, k * nc + c) * s0[(a * nc + b) * nf + k];
-      atomicAdd(rc + dc, s);
-    }
-    __syncthreads();
-  }
-}
-
-// ---- h-transfer between nested structured Q1 grids -----------------------
-// Level nodes of an axis sit at fine mesh nodes min(k s, nf) (BoxStride); the
-// coarse level (stride 2s) keeps every other node and the last one.  x fastest.
-struct HGrid {
-  int64_t fx, fy, fz, cx, cy, cz;  // node counts
-  int nf[3];                       // cells of the uniform mesh the strides refer to
-  int s;                           // stride of the fine level
-};
-
-// 1D Q1 interpolation weight of coarse node c at fine node I: an even fine
-// node is coarse node I/2; an odd one lies between (I-1)/2 and (I+1)/2 at
-// the fraction of their distance its position gives (1/2 unless the last
-// coarse cell is narrower)
-__device__ __forceinline__ double hw(int64_t I, int64_t c, int nf, int s) {
-  if ((I & 1) == 0) return c == (I >> 1) ? 1.0 : 0.0;
-  const int64_t L = (I - 1) >> 1;
-  const int64_t A = (I - 1) * s, P = min(I * s, (int64_t)nf), B = min((I + 1) * s, (int64_t)nf);
-  const double wr = (double)(P - A) / (double)(B - A);
-  return c == L ? 1.0 - wr : (c == L + 1 ? wr : 0.0);
-}
-
-// x_f += P x_c on interior fine nodes
-template <class T>
-__global__ void k_h_prolongate_add(HGrid g, const T *__restrict__ xc, T *__restrict__ xf) {
-  GRID_STRIDE(t, g.fx * g.fy * g.fz) {
-    const int64_t I = t % g.fx, J = (t / g.fx) % g.fy, K = t / (g.fx * g.fy);
-    if (I == 0 || J == 0 || K == 0 || I == g.fx - 1 || J == g.fy - 1 || K == g.fz - 1) continue;
-    const int64_t i0 = I / 2, j0 = J / 2, k0 = K / 2;
-    T acc = 0;
-    for (int64_t kk = k0; kk <= k0 + (K & 1); ++kk)
-      for (int64_t jj = j0; jj <= j0 + (J & 1); ++jj)
-        for (int64_t ii = i0; ii <= i0 + (I & 1); ++ii) {
-          const T w = (T)(hw(I, ii, g.nf[0], g.s) * hw(J, jj, g.nf[1], g.s) *
-                          hw(K, kk, g.nf[2], g.s));
-          acc += w * xc[ii + g.cx * (jj + g.cy * kk)];
-        }
-    xf[t] += acc;
-  }
-}
-
-// r_c = P^T r_f on interior coarse nodes (boundary nodes -> 0)
-template <class T>
-__global__ void k_h_restrict(HGrid g, const T *__restrict__ rf, T *__restrict__ rc) {
-  GRID_STRIDE(t, g.cx * g.cy * g.cz) {
-    const int64_t i = t % g.cx, j = (t / g.cx) % g.cy, k = t / (g.cx * g.cy);
-    if (i == 0 || j == 0 || k == 0 || i == g.cx - 1 || j == g.cy - 1 || k == g.cz - 1) {
-      rc[t] = 0;
-      continue;
-    }
-    T acc = 0;  // fine neighbours 2i-1 .. 2i+1 exist for every interior coarse node
-    for (int64_t K = 2 * k - 1; K <= 2 * k + 1; ++K)
-      for (int64_t J = 2 * j - 1; J <= 2 * j + 1; ++J)
-        for (int64_t I = 2 * i - 1; I <= 2 * i + 1; ++I) {
-          const T w = (T)(hw(I, i, g.nf[0], g.s) * hw(J, j, g.nf[1], g.s) *
-                          hw(K, k, g.nf[2], g.s));
-          acc += w * rf[I + g.fx * (J + g.fy * K)];
-        }
-    rc[t] = acc;
-  }
-}
-
-// ---- valence (number of cells sharing a DoF) ----------------------------
-template <class T>
-__global__ void k_count_valence(int64_t n, const uint32_t *__restrict__ map, T *__restrict__ val) {
-  GRID_STRIDE(t, n) {
-    const uint32_t d = map[t];
-    if (d != MFGB_INVALID_DOF) atomicAdd(val + d, (T)1);
-  }
-}
-
-template <class T>
-__global__ void k_invert_pos(int64_t n, T *__restrict__ v) {
-  GRID_STRIDE(t, n) v[t] = v[t] > 0 ? (T)1 / v[t] : (T)0;
-}
 
 // ---- coarse solve: FP64 Jacobi-CG on a dense SPD matrix, one CTA ---------
 // A[n][n] row-major over the n interior coarse DoFs; x = A^{-1} b to a
@@ -499,43 +179,9 @@ __global__ void k_copy_scalar(double *__restrict__ scal, int from, int to) {
 // host side
 // --------------------------------------------------------------------------
 
-struct MgLevel {
-  mfgb_box_desc box{};
-  BoxStride bs{};  // s = 1 on the fine mesh (p-levels), 2^l on the l-th h-level
-  mfgb_operator *op = nullptr;
-  int64_t n = 0;
-  void *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *t = nullptr;
-  void *inv_diag = nullptr;  // Jacobi (precision T)
-  void *inv_val = nullptr;   // 1/valence (precision T), for p-restriction from this level
-  double lmax = 0;
-  int to_coarse = 0;  // 1 = p-transfer, 2 = h-transfer, 0 = coarsest
-};
-
-struct MgCoarse {
-  int n = 0;
-  double *A = nullptr, *dinv = nullptr, *work = nullptr;
-  int64_t *ids = nullptr;
-};
-
 }  // namespace mfgb
 
-struct mfgb_mg {
-  int precision = 32;
-  int degree = 5;
-  double range = 15.0;
-  double coarse_tol = 1e-12;
-  std::vector<mfgb::MgLevel> levels;
-  mfgb::MgCoarse coarse;
-  // outer PCG buffers (FP64)
-  double *r = nullptr, *z = nullptr, *p = nullptr, *v = nullptr, *part = nullptr,
-         *scal = nullptr;
-  int64_t outer_n = 0;
-};
-
 namespace mfgb {
-namespace {
-
-size_t tsize(int prec) { return prec == 32 ? sizeof(float) : sizeof(double); }
 
 mfgb_status dalloc(void **p, size_t bytes) {
   *p = nullptr;
@@ -556,6 +202,39 @@ mfgb_status ensure_g32(mfgb_operator *op) {
   if ((st = cuda_status(g_to_f32(ng, op->d_G, op->d_G32, nullptr), "G -> FP32"))) return st;
   return cuda_status(cudaDeviceSynchronize(), "G -> FP32");
 }
+
+void mg_plan_levels(const mfgb_box_desc &fine, int coarse_cells, std::vector<mfgb_box_desc> &boxes,
+                    std::vector<int> &kinds, std::vector<int> &strides) {
+  boxes.clear();
+  kinds.clear();
+  strides.clear();
+  mfgb_box_desc b = fine;
+  // every level keeps the fine level's geometry degree (coarse Q1 cells of a
+  // deformed mesh would otherwise fold)
+  b.geometry_degree = fine.geometry_degree > 0 ? fine.geometry_degree : fine.degree;
+  boxes.push_back(b);
+  strides.push_back(1);
+  while (b.degree > 1) {
+    b.degree = std::max(1, b.degree / 2);
+    boxes.push_back(b);
+    strides.push_back(1);
+    kinds.push_back(1);
+  }
+  // h-levels: stride 2^l, ceil(n / 2^l) cells per axis (nested for any n)
+  for (int s = 2; std::max({b.nx, b.ny, b.nz}) > coarse_cells; s *= 2) {
+    b.nx = (fine.nx + s - 1) / s;
+    b.ny = (fine.ny + s - 1) / s;
+    b.nz = (fine.nz + s - 1) / s;
+    boxes.push_back(b);
+    strides.push_back(s);
+    kinds.push_back(2);
+  }
+  kinds.push_back(0);
+}
+
+namespace {
+
+size_t tsize(int prec) { return prec == 32 ? sizeof(float) : sizeof(double); }
 
 // dst = A src on one level in the V-cycle precision
 mfgb_status level_vmult(mfgb_operator *op, int prec, void *dst, const void *src, cudaStream_t s) {
@@ -602,25 +281,6 @@ mfgb_status chebyshev(const MgLevel &L, int degree, double range, bool zero_star
   return cuda_status(cudaGetLastError(), "chebyshev");
 }
 
-HGrid hgrid(const MgLevel &fine, const MgLevel &coarse) {
-  return HGrid{fine.box.nx + 1, fine.box.ny + 1, fine.box.nz + 1,
-               coarse.box.nx + 1, coarse.box.ny + 1, coarse.box.nz + 1,
-               {fine.bs.nf[0], fine.bs.nf[1], fine.bs.nf[2]}, fine.bs.s};
-}
-
-PTransferParams ptransfer(const mfgb_operator *fine, const mfgb_operator *coarse) {
-  PTransferParams P{};
-  P.nf = fine->n;
-  P.nc = coarse->n;
-  for (int a = 0; a < P.nf; ++a)
-    for (int b = 0; b < P.nc; ++b) {
-      const double v = lagrange_value(P.nc, coarse->gll_x, b, fine->gll_x[a]);
-      P.B64[a * P.nc + b] = v;
-      P.B32[a * P.nc + b] = (float)v;
-    }
-  return P;
-}
-
 template <class T>
 mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
   MgLevel &L = mg->levels[l];
@@ -644,7 +304,7 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
     k_p_restrict_sf<T><<<(unsigned)std::min<int64_t>(L.op->n_cells, 152 * 16), 128, 0, s>>>(
         L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)L.r, (const T *)L.inv_val, (T *)C.b, P);
   } else {
-    k_h_restrict<T><<<grid1d(C.n), T256, 0, s>>>(hgrid(L, C), (const T *)L.r, (T *)C.b);
+    k_h_restrict<T><<<grid1d(C.n), T256, 0, s>>>(hgrid(L.box, L.bs, C.box), (const T *)L.r, (T *)C.b);
   }
   if ((st = cuda_status(cudaGetLastError(), "restrict"))) return st;
   if ((st = vcycle<T>(mg, l + 1, s))) return st;
@@ -655,7 +315,7 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
         L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)C.x, (T *)L.t, P);
     k_axpy<T><<<grid1d(L.n), T256, 0, s>>>(L.n, (T)1, (const T *)L.t, (T *)L.x);
   } else {
-    k_h_prolongate_add<T><<<grid1d(L.n), T256, 0, s>>>(hgrid(L, C), (const T *)C.x,
+    k_h_prolongate_add<T><<<grid1d(L.n), T256, 0, s>>>(hgrid(L.box, L.bs, C.box), (const T *)C.x,
                                                         (T *)L.x);
   }
   if ((st = cuda_status(cudaGetLastError(), "prolongate"))) return st;
@@ -779,28 +439,7 @@ extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_pa
   // level boxes: p-coarsening by halving, then h-coarsening of Q1 by 2
   std::vector<mfgb_box_desc> boxes;
   std::vector<int> kinds, strides;
-  mfgb_box_desc b = *fine;
-  // every level keeps the fine level's geometry degree (coarse Q1 cells of a
-  // deformed mesh would otherwise fold)
-  b.geometry_degree = fine->geometry_degree > 0 ? fine->geometry_degree : fine->degree;
-  boxes.push_back(b);
-  strides.push_back(1);
-  while (b.degree > 1) {
-    b.degree = std::max(1, b.degree / 2);
-    boxes.push_back(b);
-    strides.push_back(1);
-    kinds.push_back(1);
-  }
-  // h-levels: stride 2^l, ceil(n / 2^l) cells per axis (nested for any n)
-  for (int s = 2; std::max({b.nx, b.ny, b.nz}) > prm->coarse_cells; s *= 2) {
-    b.nx = (fine->nx + s - 1) / s;
-    b.ny = (fine->ny + s - 1) / s;
-    b.nz = (fine->nz + s - 1) / s;
-    boxes.push_back(b);
-    strides.push_back(s);
-    kinds.push_back(2);
-  }
-  kinds.push_back(0);
+  mg_plan_levels(*fine, prm->coarse_cells, boxes, kinds, strides);
   mfgb_status st = MFGB_OK;
   const size_t ts = tsize(prm->precision);
   for (size_t l = 0; l < boxes.size() && !st; ++l) {

@@ -202,8 +202,9 @@ mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const double *d_b, do
 
 /* ---- multigrid preconditioner (no counterpart in the reference) ----------
  * Geometric p- and h-multigrid V-cycle for the structured box: p_fine ->
- * p_fine/2 -> ... -> 1 on the fine mesh, then Q1 on 2:1 coarsened meshes
- * while every cell count is even and the largest exceeds coarse_cells;
+ * p_fine/2 -> ... -> 1 on the fine mesh, then Q1 on coarsened meshes while
+ * the largest cell count exceeds coarse_cells (level l keeps the fine mesh
+ * nodes min(k 2^l, n) of each axis: nested for any n);
  * Chebyshev(degree) around Jacobi on [lmax/smoothing_range, 1.2 lmax] with
  * lmax from eig_iterations power iterations; FP64 Jacobi-CG on the coarsest
  * level.  precision 32 runs the V-cycle (operators, smoother, transfers) in
@@ -236,6 +237,36 @@ mfgb_status mfgb_mg_cg_solve(const mfgb_operator *op, mfgb_mg *mg, const double 
    diagonal); NULL restores the plain diagonal.  The V-cycle stays linear and
    SPD.  lambda_max of D~^-1 A is re-estimated. */
 mfgb_status mfgb_mg_set_smoother_weights(mfgb_mg *mg, const double *d_cell_weights);
+
+/* ---- batched solves (no counterpart in the reference) ---------------------
+ * Many independent box problems (own cells, degree, deformation each) solved
+ * together: FP64 CG with per-problem scalars and SolverCG/ReductionControl
+ * semantics per problem, preconditioned by the FP32 multigrid V-cycle of
+ * mfgb_mg_setup applied to every problem at once (params->precision must be
+ * 32).  Vectors are the problems' DoF vectors concatenated in order
+ * (h_offsets from mfgb_batch_info, n_problems + 1 entries).  The problems'
+ * operators of one degree are applied by one kernel launch; one CG iteration
+ * of the whole batch is one CUDA graph launch. */
+typedef struct mfgb_batch mfgb_batch;
+mfgb_status mfgb_batch_create(const mfgb_box_desc *boxes, int n_problems,
+                              const mfgb_mg_params *params, mfgb_batch **batch);
+mfgb_status mfgb_batch_destroy(mfgb_batch *batch);
+/* any output may be NULL; h_depth_dofs has n_depths entries, h_levels
+   n_problems (multigrid levels of each problem) */
+mfgb_status mfgb_batch_info(const mfgb_batch *batch, int *n_problems, int64_t *h_offsets,
+                            int *n_depths, int64_t *h_depth_dofs, int *h_levels);
+/* b_i uniform in [-1, 1) from std::mt19937_64(h_seeds[i]), boundary DoFs 0 */
+mfgb_status mfgb_batch_rhs_uniform(const mfgb_batch *batch, const uint64_t *h_seeds, double *d_b,
+                                   void *stream);
+/* d_dst = A d_src for every problem (FP64, double-float arithmetic) */
+mfgb_status mfgb_batch_vmult(mfgb_batch *batch, double *d_dst, const double *d_src, void *stream);
+/* d_dst = M d_src: one batched V-cycle */
+mfgb_status mfgb_batch_precondition(mfgb_batch *batch, double *d_dst, const double *d_src,
+                                    void *stream);
+/* solves A_i x_i = b_i for every problem; h_info has n_problems entries.
+   MFGB_ERR_NOT_CONVERGED if any problem reached max_steps (infos filled). */
+mfgb_status mfgb_batch_cg_solve(mfgb_batch *batch, const double *d_b, double *d_x,
+                                const mfgb_cg_control *ctl, mfgb_solve_info *h_info, void *stream);
 
 /* ---- learned part: features, targets, MLP (no counterpart in the reference)
  * features: per cell, dx/dxi at the 8 corner nodes (72 values, scaled by
