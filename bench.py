@@ -330,6 +330,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         line["bp5"] = bp5_solves(A)
         line["bk6"] = bk6_rate(A, args)
         line["bk5_gauss_like_for_like"] = gauss_like_for_like(args)
+        line["batched"] = batched_solves()
     print(json.dumps(line), flush=True)
 
 
@@ -398,6 +399,59 @@ def bp5_solves(A):
     return out
 
 
+def batched_solves(n_problems=256, n_sequential=24):
+    """Batched BP5 solves: 256 independent problems (degree uniform in 2..7,
+    n^3 cells with n uniform in 6..32, amplitude uniform in [0, 0.1], one
+    seeded U[-1,1] right-hand side each) to a 1e-10 relative residual with the
+    batched FP32-multigrid FP64 CG, against the same method run problem by
+    problem (timed on the first n_sequential problems, scaled by DoFs)."""
+    import numpy as np
+    import torch
+
+    import benchmarks_gb300 as mf
+    meshes, seeds = mf.batch_workload(n_problems, seed=2024)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    B, t_setup = timed(lambda: mf.BatchSolver(meshes))
+    b = B.rhs_uniform(seeds)
+    best = None
+    for _ in range(2):
+        x = B.initialize_dof_vector()
+        _, t = timed(lambda: B.solve(x, b, max_steps=200, reduce=1e-10))
+        best = t if best is None else min(best, t)
+    steps = [i["steps"] for i in B.infos]
+    out = {"problems": n_problems, "n_dofs": B.n_dofs, "setup_seconds": t_setup,
+           "seconds": best, "dofs_per_second": B.n_dofs / best,
+           "iterations_min_mean_max": [min(steps), float(np.mean(steps)), max(steps)],
+           "all_converged": all(i["converged"] for i in B.infos),
+           "depth_dofs": B.depth_dofs}
+    seq_t, seq_dofs = 0.0, 0
+    for i in range(n_sequential):
+        A = mf.LaplaceOperator(meshes[i])
+        M = mf.MGPreconditioner(meshes[i], precision=32)
+        bi = B.split(b)[i].contiguous()
+        t_best = None
+        for _ in range(2):
+            xi = A.initialize_dof_vector()
+            ctl = mf.ReductionControl(200, 1e-300, 1e-10)
+            _, t = timed(lambda: mf.SolverCG(ctl).solve(A, xi, bi, M))
+            t_best = t if t_best is None else min(t_best, t)
+        seq_t += t_best
+        seq_dofs += A.m()
+        del A, M
+    out["one_by_one_dofs_per_second"] = seq_dofs / seq_t
+    out["one_by_one_sample"] = f"first {n_sequential} problems, {seq_dofs} DoFs, {seq_t:.3f} s"
+    out["speedup_vs_one_by_one"] = out["dofs_per_second"] / out["one_by_one_dofs_per_second"]
+    del B
+    return out
+
+
 def bk6_rate(A, args):
     """BK6 on the bench mesh: the vector Laplacian with 3 interleaved FP64
     components per node; GDoF/s counts the 3 components (the CEED convention)."""
@@ -451,6 +505,19 @@ def gauss_like_for_like(args):
             "ratio_vs_published": rate / 6.83}
 
 
+def kernel_name(degree, arith):
+    """Name of the operator kernel the library's shape table launches."""
+    import ctypes
+
+    import benchmarks_gb300 as mf
+    shape = ctypes.c_int()
+    mf.lib().mfgb_get_kernel_shape(arith, degree, ctypes.byref(shape))
+    n = degree + 1
+    pol = "ArithDF" if arith == 1 else "ArithF64"
+    return {0: f"bk5_kernel<{n},{pol}>", 1: f"bk5_pt_kernel<{n},{pol}>",
+            2: f"bk5_tma_kernel<{n},{pol}>"}.get(shape.value, "bk5")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -485,15 +552,3 @@ def main():
 if __name__ == "__main__":
     main()
 
-
-def kernel_name(degree, arith):
-    """Name of the operator kernel the library's shape table launches."""
-    import ctypes
-
-    import benchmarks_gb300 as mf
-    shape = ctypes.c_int()
-    mf.lib().mfgb_get_kernel_shape(arith, degree, ctypes.byref(shape))
-    n = degree + 1
-    pol = "ArithDF" if arith == 1 else "ArithF64"
-    return {0: f"bk5_kernel<{n},{pol}>", 1: f"bk5_pt_kernel<{n},{pol}>",
-            2: f"bk5_tma_kernel<{n},{pol}>"}.get(shape.value, "bk5")

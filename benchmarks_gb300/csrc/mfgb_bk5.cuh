@@ -20,9 +20,15 @@
 
 namespace mfgb {
 
+// Resident CTAs the compiler must fit per SM (register cap) for the column
+// kernel; 0 leaves the register count to the compiler.  FP32 applies are
+// memory-latency bound and at N = 5 the compiler's choice (67 registers)
+// stops at about 40 % of the warp slots (measured: 11 % faster capped).
+template <int N, class A> struct ColumnMinBlocks { static constexpr int value = 0; };
+template <> struct ColumnMinBlocks<5, ArithF32> { static constexpr int value = 5; };
+
 template <int N, int E, class A, bool EVEC, bool WITH_ENERGY>
-__global__ void __launch_bounds__(E * N * N)
-    bk5_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+__device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uint32_t *__restrict__ map,
                const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
                typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
                double *__restrict__ energy_partials, const int *__restrict__ done_flag) {
@@ -140,6 +146,29 @@ __global__ void __launch_bounds__(E * N * N)
       energy_partials[blockIdx.x] = s;
     }
   }
+}
+
+template <int N, int E, class A, bool EVEC, bool WITH_ENERGY>
+__global__ void __launch_bounds__(E * N * N)
+    bk5_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+               const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+               typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
+               double *__restrict__ energy_partials, const int *__restrict__ done_flag) {
+  bk5_column_body<N, E, A, EVEC, WITH_ENERGY>(n_cells, map, G, src, dst, basis, energy_partials,
+                                              done_flag);
+}
+
+// the same with the register cap of ColumnMinBlocks
+template <int N, int E, class A, bool EVEC, bool WITH_ENERGY>
+__global__ void __launch_bounds__(E * N * N, (ColumnMinBlocks<N, A>::value > 0
+                                                  ? ColumnMinBlocks<N, A>::value : 1))
+    bk5_kernel_capped(const int64_t n_cells, const uint32_t *__restrict__ map,
+                      const typename A::GType *__restrict__ G,
+                      const typename A::VecT *__restrict__ src, typename A::VecT *__restrict__ dst,
+                      const Basis<N, A> basis, double *__restrict__ energy_partials,
+                      const int *__restrict__ done_flag) {
+  bk5_column_body<N, E, A, EVEC, WITH_ENERGY>(n_cells, map, G, src, dst, basis, energy_partials,
+                                              done_flag);
 }
 
 }  // namespace mfgb
@@ -285,10 +314,13 @@ struct TmaLayout {
 //   integrate + atomic scatter of batch b
 // Shared memory holds one G tile, one map tile and the three work arrays.
 // err_flag (may be null) records a TMA wait that exceeded its time limit.
-template <int N> struct TmaMinBlocks { static constexpr int value = N <= 6 ? 2 : 1; };
+template <int N, class A> struct TmaMinBlocks { static constexpr int value = N <= 6 ? 2 : 1; };
+// FP32 at N = 4, 5: the compiler's 86 / 107 registers leave 2-3 CTAs per SM
+template <> struct TmaMinBlocks<4, ArithF32> { static constexpr int value = 4; };
+template <> struct TmaMinBlocks<5, ArithF32> { static constexpr int value = 4; };
 
 template <int N, int E, class A, bool WITH_ENERGY>
-__global__ void __launch_bounds__(E * N * N, TmaMinBlocks<N>::value)
+__global__ void __launch_bounds__(E * N * N, (TmaMinBlocks<N, A>::value))
     bk5_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
                    const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
                    typename A::VecT *__restrict__ dst, const Basis<N, A> basis,

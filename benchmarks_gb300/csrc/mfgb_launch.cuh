@@ -78,7 +78,12 @@ int bk5_grid(int64_t n_cells, int shape) {
       ps = ctas_per_sm(bk5_tma_kernel<N, ET, A, EN>, ET * N * N, TmaLayout<N, ET, A>::total);
   } else {
     E = ElemsPerCta<N>::value;
-    if (ps < 0) ps = ctas_per_sm(bk5_kernel<N, ElemsPerCta<N>::value, A, EVEC, EN>, E * N * N, 0);
+    if (ps < 0) {
+      if constexpr (ColumnMinBlocks<N, A>::value > 0)
+        ps = ctas_per_sm(bk5_kernel_capped<N, ElemsPerCta<N>::value, A, EVEC, EN>, E * N * N, 0);
+      else
+        ps = ctas_per_sm(bk5_kernel<N, ElemsPerCta<N>::value, A, EVEC, EN>, E * N * N, 0);
+    }
   }
   if (ps < 1) ps = 1;
   const int64_t n_batches = (n_cells + E - 1) / E;
@@ -112,8 +117,12 @@ cudaError_t bk5_launch(int64_t n_cells, const uint32_t *map, const typename A::G
     }
   } else {
     constexpr int E = ElemsPerCta<N>::value;
-    bk5_kernel<N, E, A, EVEC, EN><<<grid, E * N * N, 0, stream>>>(n_cells, map, G, src, dst,
-                                                                   basis, partials, done_flag);
+    if constexpr (ColumnMinBlocks<N, A>::value > 0)
+      bk5_kernel_capped<N, E, A, EVEC, EN><<<grid, E * N * N, 0, stream>>>(
+          n_cells, map, G, src, dst, basis, partials, done_flag);
+    else
+      bk5_kernel<N, E, A, EVEC, EN><<<grid, E * N * N, 0, stream>>>(n_cells, map, G, src, dst,
+                                                                     basis, partials, done_flag);
   }
   return cudaGetLastError();
 }
