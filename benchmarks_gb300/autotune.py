@@ -93,3 +93,42 @@ def load(path, apply=True):
             for d, r in per.items():
                 _abi.check(lib().mfgb_set_kernel_shape(ARITHS[name], int(d), int(r["best"])))
     return result
+
+
+def main(argv=None):
+    """Command line: re-measure the shape table, or time one shape (for profiling).
+
+    python -m benchmarks_gb300.autotune [--degrees 1 2 ...] [--ariths df fp32 fp64]
+        [--dofs 3e7] [--reps 10] [--shape S] [--out table.json]
+    """
+    import argparse
+    ap = argparse.ArgumentParser(prog="python -m benchmarks_gb300.autotune")
+    ap.add_argument("--degrees", type=int, nargs="+", default=list(range(1, 9)))
+    ap.add_argument("--ariths", nargs="+", choices=sorted(ARITHS), default=["df", "fp32"])
+    ap.add_argument("--dofs", type=float, default=2.0e7, help="DoFs of the timing mesh")
+    ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--shape", type=int, choices=SHAPES, default=None,
+                    help="time only this shape (no tuning)")
+    ap.add_argument("--out", default=None, help="write the measured table as JSON")
+    a = ap.parse_args(argv)
+    import torch
+
+    import benchmarks_gb300 as mf
+    torch.cuda.set_device(0)
+    if a.shape is not None:
+        for d in a.degrees:
+            A = mf.LaplaceOperator(_mesh_for(d, a.dofs))
+            for name in a.ariths:
+                ms = time_shape(A, ARITHS[name], a.shape, a.reps)
+                print(json.dumps({"arith": name, "degree": d, "shape": a.shape, "n_dofs": A.m(),
+                                  "ms": ms, "GDoF/s": A.m() / ms / 1e6}))
+            del A
+        return
+    r = tune(a.degrees, tuple(a.ariths), a.dofs, a.reps, apply=True)
+    print(json.dumps(r))
+    if a.out:
+        save(r, a.out)
+
+
+if __name__ == "__main__":
+    main()
