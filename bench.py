@@ -331,6 +331,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         line["bk6"] = bk6_rate(A, args)
         line["bk5_gauss_like_for_like"] = gauss_like_for_like(args)
         line["batched"] = batched_solves()
+        line["ceed_bk1_bk3_evector"] = bk1_bk3_rates()
     print(json.dumps(line), flush=True)
 
 
@@ -449,6 +450,50 @@ def batched_solves(n_problems=256, n_sequential=24):
     out["one_by_one_sample"] = f"first {n_sequential} problems, {seq_dofs} DoFs, {seq_t:.3f} s"
     out["speedup_vs_one_by_one"] = out["dofs_per_second"] / out["one_by_one_dofs_per_second"]
     del B
+    return out
+
+
+def bk1_bk3_rates(degree=4, target_dofs=6.7e7):
+    """CEED BK1 (mass) and BK3 (Laplacian, q = p + 2) E-vector applies, the
+    reference CEED_BK benchmarks' operators, at about 6.7e7 E-vector DoFs
+    (nelmt * (p+1)^3) with seeded inputs; GDoF/s and the HBM fraction of the
+    algorithmic bytes (E-vector in + out, JxW or G per point)."""
+    import numpy as np
+    import torch
+
+    import benchmarks_gb300 as mf
+    from oracle import oracle as orc  # GLL / Gauss points for the bases only
+    nq, nm = degree + 2, degree + 1
+    nel = int(target_dofs // nm ** 3)
+    xg, _ = orc.gll(nm)
+    xq, _ = orc.gauss(nq)
+    basis = torch.from_numpy(orc.interpolation_matrix(xg, xq).reshape(-1)).cuda()
+    dbasis = torch.from_numpy(orc.derivative_matrix(xq).reshape(-1)).cuda()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    u = torch.rand(nel * nm ** 3, dtype=torch.float64, device="cuda", generator=g)
+    y = torch.empty_like(u)
+    jxw = 0.5 + torch.rand(nel * nq ** 3, dtype=torch.float64, device="cuda", generator=g)
+    G = torch.rand(nel * 6 * nq ** 3, dtype=torch.float64, device="cuda", generator=g)
+    peak = measured_peaks()[0]
+    out = {"degree": degree, "n_q_1d": nq, "elements": nel, "evector_dofs": nel * nm ** 3}
+    for name, fn, coef_bytes in (
+            ("bk1", lambda a: mf.bk1_evector(degree, basis, jxw, u, y, arith=a), 8 * nq ** 3),
+            ("bk3", lambda a: mf.bk3_evector(degree, basis, dbasis, G, u, y, arith=a), 48 * nq ** 3)):
+        for arith in ("df", "fp64"):
+            for _ in range(3):
+                fn(arith)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                fn(arith)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 10
+            byts = nel * (16 * nm ** 3 + coef_bytes)
+            out[f"{name}_{arith}"] = {"GDoF/s": nel * nm ** 3 / ms / 1e6, "ms": ms,
+                                      "hbm_frac": byts / (ms * 1e-3) / 1e9 / peak}
+    del u, y, jxw, G
     return out
 
 

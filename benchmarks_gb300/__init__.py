@@ -346,6 +346,30 @@ def bk5_evector(degree, dbasis, G, u, out, arith="fp64"):
     return out
 
 
+def bk1_evector(degree, basis, JxW, u, out, arith="fp64"):
+    """E-vector seam of the CEED BK1 mass operator (BK1::Parallel::MassOperator),
+    nq = degree + 2 points: basis [nq * nm], JxW [e][nq^3], u/out [e][nm^3]."""
+    nm3 = (degree + 1) ** 3
+    _abi.check(lib().mfgb_bk1_evector(
+        int(degree), u.numel() // nm3, ctypes.c_void_p(basis.data_ptr()),
+        ctypes.c_void_p(JxW.data_ptr()), ctypes.c_void_p(u.data_ptr()),
+        ctypes.c_void_p(out.data_ptr()), _arith(arith), _stream_ptr()))
+    return out
+
+
+def bk3_evector(degree, basis, dbasis, G, u, out, arith="fp64"):
+    """E-vector seam of the CEED BK3 Laplacian (BK3::Parallel::LaplaceOperator),
+    nq = degree + 2 points: basis [nq * nm], dbasis [nq * nq], G [e][6][nq^3],
+    u/out [e][nm^3]."""
+    nm3 = (degree + 1) ** 3
+    _abi.check(lib().mfgb_bk3_evector(
+        int(degree), u.numel() // nm3, ctypes.c_void_p(basis.data_ptr()),
+        ctypes.c_void_p(dbasis.data_ptr()), ctypes.c_void_p(G.data_ptr()),
+        ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(out.data_ptr()), _arith(arith),
+        _stream_ptr()))
+    return out
+
+
 def bk5_lvector(degree, dbasis, G, src, dst, dof_indices, arith="fp64"):
     """L-vector kernel seam (BK3::Parallel::KokkosKernel_1D_Block, GLL form):
     accumulates into dst."""

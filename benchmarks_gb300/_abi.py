@@ -101,6 +101,8 @@ def lib():
         "mfgb_mg_vmult": ([P, P, P, P], I32),
         "mfgb_mg_cg_solve": ([P, P, P, P, ctypes.POINTER(CgControl), ctypes.POINTER(SolveInfo), P],
                              I32),
+        "mfgb_bk1_evector": ([I32, I64, P, P, P, P, I32, P], I32),
+        "mfgb_bk3_evector": ([I32, I64, P, P, P, P, P, I32, P], I32),
         "mfgb_batch_create": ([ctypes.POINTER(BoxDesc), I32, ctypes.POINTER(MgParams), PP], I32),
         "mfgb_batch_destroy": ([P], I32),
         "mfgb_batch_info": ([P, P, P, P, P, P], I32),

@@ -21,6 +21,7 @@ SOURCES = [
     "mfgb_cg.cu",
     "mfgb_mg.cu",
     "mfgb_batch.cu",
+    "mfgb_bkq.cu",
     "mfgb_bk5_f64.cu",
     "mfgb_bk5_df.cu",
     "mfgb_bk5_f32.cu",

@@ -1,0 +1,90 @@
+// mfgb_bkq.cu -- C ABI of the CEED BK1 / BK3 E-vector seams (nq = p + 2).
+#include <algorithm>
+#include <string>
+
+#include "mfgb_bkq.cuh"
+#include "mfgb_internal.h"
+
+namespace mfgb {
+namespace {
+
+template <int NM, int NQ, class A, bool LAPLACE>
+cudaError_t bkq_launch(int64_t nelmt, const double *basis, const double *dbasis, const double *coef,
+                       const double *in, double *out, cudaStream_t s) {
+  constexpr int E = BkqElems<NQ>::value;
+  constexpr int threads = E * NQ * NQ;
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bkq_kernel<NM, NQ, A, LAPLACE>,
+                                                      threads, 0) != cudaSuccess || per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+  }
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t batches = (nelmt + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(batches, (int64_t)per_sm * sms));
+  bkq_kernel<NM, NQ, A, LAPLACE><<<grid, threads, 0, s>>>(nelmt, basis, dbasis, coef, in, out);
+  return cudaGetLastError();
+}
+
+template <class A, bool LAPLACE>
+cudaError_t bkq_dispatch(int degree, int64_t nelmt, const double *basis, const double *dbasis,
+                         const double *coef, const double *in, double *out, cudaStream_t s) {
+  switch (degree) {
+    case 1: return bkq_launch<2, 3, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 2: return bkq_launch<3, 4, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 3: return bkq_launch<4, 5, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 4: return bkq_launch<5, 6, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 5: return bkq_launch<6, 7, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 6: return bkq_launch<7, 8, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 7: return bkq_launch<8, 9, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 8: return bkq_launch<9, 10, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+mfgb_status bkq_entry(const char *name, bool laplace, int degree, int64_t nelmt,
+                      const double *basis, const double *dbasis, const double *coef,
+                      const double *in, double *out, int arith, void *stream) {
+  if (degree < 1 || degree > 8 || nelmt < 0 || (nelmt > 0 && (!basis || !coef || !in || !out)) ||
+      (laplace && nelmt > 0 && !dbasis) ||
+      (arith != MFGB_ARITH_FP64 && arith != MFGB_ARITH_FP64_DF)) {
+    set_error(std::string(name) + ": invalid argument (degree 1..8, arith FP64 or FP64_DF)");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if (nelmt == 0) return MFGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (arith == MFGB_ARITH_FP64)
+    e = laplace ? bkq_dispatch<ArithF64, true>(degree, nelmt, basis, dbasis, coef, in, out, s)
+                : bkq_dispatch<ArithF64, false>(degree, nelmt, basis, dbasis, coef, in, out, s);
+  else
+    e = laplace ? bkq_dispatch<ArithDF, true>(degree, nelmt, basis, dbasis, coef, in, out, s)
+                : bkq_dispatch<ArithDF, false>(degree, nelmt, basis, dbasis, coef, in, out, s);
+  return cuda_status(e, name);
+}
+
+}  // namespace
+}  // namespace mfgb
+
+using namespace mfgb;
+
+extern "C" {
+
+mfgb_status mfgb_bk1_evector(int degree, int64_t nelmt, const double *d_basis, const double *d_JxW,
+                             const double *d_in, double *d_out, int arith, void *stream) {
+  return bkq_entry("mfgb_bk1_evector", false, degree, nelmt, d_basis, nullptr, d_JxW, d_in, d_out,
+                   arith, stream);
+}
+
+mfgb_status mfgb_bk3_evector(int degree, int64_t nelmt, const double *d_basis,
+                             const double *d_dbasis, const double *d_G, const double *d_in,
+                             double *d_out, int arith, void *stream) {
+  return bkq_entry("mfgb_bk3_evector", true, degree, nelmt, d_basis, d_dbasis, d_G, d_in, d_out,
+                   arith, stream);
+}
+
+}  // extern "C"

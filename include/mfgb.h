@@ -162,6 +162,25 @@ mfgb_status mfgb_bk5_lvector(int degree, int64_t n_cells, const double *d_dbasis
 mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, const double *d_G,
                              const double *d_in, double *d_out, int arith, void *stream);
 
+/* E-vector seam of BK1::Parallel::MassOperator<T,nq>
+   (CEED_BK/include/kernels/BK1/templated_cuda_kernels.cuh:11-13), the CEED BK1
+   mass operator with nq = degree + 2 points and nm = degree + 1 modes:
+   out_e = B^T (JxW_e o (B x B x B) in_e); d_basis[q*nm + i], d_JxW[e][nq^3],
+   d_in/d_out[e][nm^3], point and mode indices with direction 0 slowest (the
+   reference serial kernel's order, CEED_BK/include/kernels/BK1/serial_kernels.hpp;
+   its CUDA kernel indexes JxW with direction 2 slowest).  arith FP64 or FP64_DF. */
+mfgb_status mfgb_bk1_evector(int degree, int64_t nelmt, const double *d_basis, const double *d_JxW,
+                             const double *d_in, double *d_out, int arith, void *stream);
+
+/* E-vector seam of BK3::Parallel::LaplaceOperator<T,nq>
+   (CEED_BK/include/kernels/BK3/templated_cuda_kernels.cuh:11-14), the CEED BK3
+   Laplacian with interpolation: nq = degree + 2 points, d_basis[q*nm + i],
+   collocation derivative d_dbasis[q*nq + m] at the points, d_G[e][6][nq^3]
+   (rr rs rt ss st tt, the CUDA kernel's layout), d_in/d_out[e][nm^3]. */
+mfgb_status mfgb_bk3_evector(int degree, int64_t nelmt, const double *d_basis,
+                             const double *d_dbasis, const double *d_G, const double *d_in,
+                             double *d_out, int arith, void *stream);
+
 /* ---- diagonal -------------------------------------------------------------
  * compute_diagonal (bp5_kokkos/benchmark.cc:218-251): exact diagonal of the
  * operator (1 on constrained rows), then d -> (d > 0 ? 1/d : 1). */

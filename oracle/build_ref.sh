@@ -1,5 +1,5 @@
 #!/bin/sh
-# Compiles the reference's header-only CPU BK5 kernel and Lagrange basis (read
+# Compiles the reference's header-only CPU BK1, BK3 and BK5 kernels and Lagrange basis (read
 # in place from the reference checkout) with oracle/ref_driver.cc into
 # oracle/_ref/libref_bk5.so.  Test infrastructure only; needs the reference
 # sources, so it runs where they exist and is skipped elsewhere.

@@ -575,6 +575,49 @@ static void bk5g_element(int n, int nq, const double *B, const double *DG, const
   contract(B, nq, n, 0, 1, e_qnn2, t1, y);
 }
 
+/* BK3 E-vector (CEED_BK/include/kernels/BK3/serial_kernels.hpp:29-188): per
+   element, interpolation to nq points (basis[q*nm + i]), collocation derivative
+   there (dbasis[q*nq + m]), metric G[e][6][nq^3] (point index dir 0 slowest, the
+   layout of the reference's CUDA BK3 kernel, templated_cuda_kernels.cuh:156-161),
+   transposes back to the nm^3 modes.  in/out [e][nm^3]. */
+void orc_bk3_evector(int nm, int nq, int64_t nelmt, const double *basis, const double *dbasis,
+                     const double *G, const double *in, double *out) {
+  const int nm3 = nm * nm * nm, nq3 = nq * nq * nq;
+#pragma omp parallel
+  {
+    double *w = (double *)malloc(sizeof(double) * 8 * nq3);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < nelmt; ++e)
+      bk5g_element(nm, nq, basis, dbasis, G + e * 6 * nq3, in + e * nm3, out + e * nm3, w);
+    free(w);
+  }
+}
+
+/* BK1 E-vector mass operator (CEED_BK/include/kernels/BK1/serial_kernels.hpp:20-121):
+   out_e = B^T (JxW_e o (B x B x B) in_e), JxW[e][nq^3] with the point index
+   dir 0 slowest (the serial kernel's layout, :80-86). */
+void orc_bk1_evector(int nm, int nq, int64_t nelmt, const double *basis, const double *JxW,
+                     const double *in, double *out) {
+  const int nm3 = nm * nm * nm, nq3 = nq * nq * nq;
+  int e_mmm[3] = {nm, nm, nm}, e_qmm[3] = {nq, nm, nm}, e_qqm[3] = {nq, nq, nm},
+      e_qqq[3] = {nq, nq, nq};
+#pragma omp parallel
+  {
+    double *t1 = (double *)malloc(sizeof(double) * 2 * nq3), *t2 = t1 + nq3;
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < nelmt; ++e) {
+      contract(basis, nq, nm, 0, 0, e_mmm, in + e * nm3, t1);
+      contract(basis, nq, nm, 1, 0, e_qmm, t1, t2);
+      contract(basis, nq, nm, 2, 0, e_qqm, t2, t1);
+      for (int q = 0; q < nq3; ++q) t1[q] *= JxW[e * nq3 + q];
+      contract(basis, nq, nm, 2, 1, e_qqq, t1, t2);
+      contract(basis, nq, nm, 1, 1, e_qqm, t2, t1);
+      contract(basis, nq, nm, 0, 1, e_qmm, t1, out + e * nm3);
+    }
+    free(t1);
+  }
+}
+
 void orc_bk5g_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
                     const uint32_t *map, const double *Gg, int64_t n_dofs, int64_t n_constrained,
                     const int64_t *constrained, const double *src, double *dst) {

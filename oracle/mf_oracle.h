@@ -104,6 +104,13 @@ int64_t orc_box_geometry_gauss(const orc_box *b, int nq, double *Gg);
 /* b_i = int phi_i f dx, f = 1, by the nq-point Gauss rule; 0 on constrained */
 void orc_box_rhs_unit_gauss(const orc_box *b, int nq, int64_t n_constrained,
                             const int64_t *constrained, double *rhs);
+/* CEED BK3 / BK1 E-vector operators: nm modes, nq points (nq = nm + 1 in the
+   reference), basis[q*nm + i], dbasis[q*nq + m], G[e][6][nq^3], JxW[e][nq^3],
+   in/out [e][nm^3]; point and mode indices with direction 0 slowest */
+void orc_bk3_evector(int nm, int nq, int64_t nelmt, const double *basis, const double *dbasis,
+                     const double *G, const double *in, double *out);
+void orc_bk1_evector(int nm, int nq, int64_t nelmt, const double *basis, const double *JxW,
+                     const double *in, double *out);
 void orc_bk5g_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
                     const uint32_t *map, const double *Gg, int64_t n_dofs,
                     int64_t n_constrained, const int64_t *constrained, const double *src,

@@ -84,6 +84,8 @@ def lib():
         L.orc_cell_geometry.argtypes = [ctypes.c_int, P, P, P, P]
         L.orc_cell_geometry.restype = ctypes.c_int
         L.orc_bk5_evector.argtypes = [ctypes.c_int, i64, P, P, P, P]
+        L.orc_bk3_evector.argtypes = [ctypes.c_int, ctypes.c_int, i64, P, P, P, P, P]
+        L.orc_bk1_evector.argtypes = [ctypes.c_int, ctypes.c_int, i64, P, P, P, P]
         L.orc_bk5_apply.argtypes = [ctypes.c_int, i64, P, P, P, i64, i64, P, P, P]
         L.orc_bk5_diagonal.argtypes = [ctypes.c_int, i64, P, P, P, i64, i64, P, P]
         L.orc_invert_diagonal.argtypes = [i64, P]
@@ -115,6 +117,14 @@ def ref_lib():
         L.ref_lagrange_value.restype = ctypes.c_double
         L.ref_lagrange_derivative.argtypes = [ctypes.c_uint, P, ctypes.c_uint, ctypes.c_double]
         L.ref_lagrange_derivative.restype = ctypes.c_double
+        L.ref_bk1_serial.argtypes = [ctypes.c_uint, ctypes.c_uint, P, P, P, P]
+        L.ref_bk1_serial.restype = ctypes.c_double
+        L.ref_bk1_serial_verification_norm.argtypes = [ctypes.c_uint, ctypes.c_uint]
+        L.ref_bk1_serial_verification_norm.restype = ctypes.c_double
+        L.ref_bk3_serial.argtypes = [ctypes.c_uint, ctypes.c_uint, P, P, P, P, P]
+        L.ref_bk3_serial.restype = ctypes.c_double
+        L.ref_bk3_serial_verification_norm.argtypes = [ctypes.c_uint, ctypes.c_uint]
+        L.ref_bk3_serial_verification_norm.restype = ctypes.c_double
         _REF = L
     return _REF
 
@@ -215,6 +225,25 @@ def evector(n: int, D: np.ndarray, G: np.ndarray, u: np.ndarray) -> np.ndarray:
     nelmt = u.size // n ** 3
     out = np.zeros_like(u)
     lib().orc_bk5_evector(n, nelmt, _p(D), _p(G), _p(u), _p(out))
+    return out
+
+
+def bk3_evector(nm, nq, basis, dbasis, G, u):
+    """CEED BK3 E-vector: basis [nq, nm], dbasis [nq, nq], G [e][6][nq^3], u [e][nm^3]."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros_like(u)
+    lib().orc_bk3_evector(nm, nq, u.size // nm ** 3, _p(np.ascontiguousarray(basis, dtype=np.float64)),
+                          _p(np.ascontiguousarray(dbasis, dtype=np.float64)),
+                          _p(np.ascontiguousarray(G, dtype=np.float64)), _p(u), _p(out))
+    return out
+
+
+def bk1_evector(nm, nq, basis, JxW, u):
+    """CEED BK1 E-vector mass operator: basis [nq, nm], JxW [e][nq^3], u [e][nm^3]."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros_like(u)
+    lib().orc_bk1_evector(nm, nq, u.size // nm ** 3, _p(np.ascontiguousarray(basis, dtype=np.float64)),
+                          _p(np.ascontiguousarray(JxW, dtype=np.float64)), _p(u), _p(out))
     return out
 
 

@@ -24,3 +24,11 @@ def golden():
     import json
     with open(os.path.join(ROOT, "tests", "golden", "reference_bk5.json")) as f:
         return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def golden13():
+    """Outputs of the reference's serial BK1 / BK3 (tests/golden/make_golden.py)."""
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "reference_bk1_bk3.json")) as f:
+        return json.load(f)

@@ -54,6 +54,49 @@ def main():
     with open(path, "w") as f:
         json.dump(out, f)
     print("wrote", path, os.path.getsize(path), "bytes")
+    bk13()
+
+
+def bk13():
+    """tests/golden/reference_bk1_bk3.json from the reference's serial BK1 and BK3
+    (CEED_BK/include/kernels/BK{1,3}/serial_kernels.hpp), nq = p + 2, nm = p + 1:
+      bk1_norms / bk3_norms -- the serial_verification norms (nelmt = 1000), p = 1..8
+      bk1_cases / bk3_cases -- seeded random basis, dbasis, JxW or all six G
+                               components, in; nelmt = 1.  G is stored here as
+                               [e][6][nq^3] (the CUDA kernel's layout); the serial
+                               kernel reads [e][p][q][6][r], so it is reordered for it."""
+    R = oracle.ref_lib()
+    out = {"bk1_norms": {}, "bk3_norms": {}, "bk1_cases": {}, "bk3_cases": {}}
+    for p in range(1, 9):
+        out["bk1_norms"][str(p)] = R.ref_bk1_serial_verification_norm(p, 1000)
+        out["bk3_norms"][str(p)] = R.ref_bk3_serial_verification_norm(p, 1000)
+    rng = np.random.default_rng(20251204)
+    for p in range(1, 9):
+        nq, nm, nelmt = p + 2, p + 1, 1
+        nq3, nm3 = nq ** 3, nm ** 3
+        basis = rng.uniform(-1, 1, nq * nm)
+        dbasis = rng.uniform(-1, 1, nq * nq)
+        jxw = rng.uniform(0.5, 2.0, nelmt * nq3)
+        G = rng.uniform(-1, 1, (nelmt, 6, nq3))
+        G[:, 0] += 3.0
+        G[:, 3] += 3.0
+        G[:, 5] += 3.0
+        u = rng.uniform(-1, 1, nelmt * nm3)
+        y1 = np.zeros(nelmt * nm3)
+        R.ref_bk1_serial(nq, nelmt, oracle._p(basis), oracle._p(jxw), oracle._p(u), oracle._p(y1))
+        # serial layout [e][p][q][6][r] from [e][6][(p q r)]
+        Gs = np.ascontiguousarray(G.reshape(nelmt, 6, nq, nq, nq).transpose(0, 2, 3, 1, 4))
+        y3 = np.zeros(nelmt * nm3)
+        R.ref_bk3_serial(nq, nelmt, oracle._p(basis), oracle._p(dbasis), oracle._p(Gs),
+                         oracle._p(u), oracle._p(y3))
+        out["bk1_cases"][str(p)] = {"basis": basis.tolist(), "JxW": jxw.tolist(), "in": u.tolist(),
+                                    "out": y1.tolist()}
+        out["bk3_cases"][str(p)] = {"basis": basis.tolist(), "dbasis": dbasis.tolist(),
+                                    "G": G.reshape(-1).tolist(), "in": u.tolist(), "out": y3.tolist()}
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_bk1_bk3.json")
+    with open(path, "w") as f:
+        json.dump(out, f)
+    print("wrote", path, os.path.getsize(path), "bytes")
 
 
 if __name__ == "__main__":

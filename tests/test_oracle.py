@@ -216,3 +216,31 @@ def test_gauss_operator_is_exact_stiffness_on_affine_cells(orc):
     energy = u @ P.apply(u)
     # exact: integral |grad u|^2 = 3 * (1/3) * (1/30)^2
     assert abs(energy - 3 * (1 / 3) * (1 / 30) ** 2) <= 1e-13
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_bk1_bk3_match_reference_serial(orc, golden13, p):
+    """The oracle's BK1 / BK3 E-vector operators against the reference's serial
+    kernels (random basis, dbasis, JxW, six independent G components)."""
+    nq, nm = p + 2, p + 1
+    c = golden13["bk1_cases"][str(p)]
+    y = orc.bk1_evector(nm, nq, np.array(c["basis"]), np.array(c["JxW"]), np.array(c["in"]))
+    assert np.linalg.norm(y - c["out"]) <= 1e-13 * np.linalg.norm(c["out"])
+    c = golden13["bk3_cases"][str(p)]
+    y = orc.bk3_evector(nm, nq, np.array(c["basis"]), np.array(c["dbasis"]), np.array(c["G"]),
+                        np.array(c["in"]))
+    assert np.linalg.norm(y - c["out"]) <= 1e-13 * np.linalg.norm(c["out"])
+
+
+@pytest.mark.parametrize("p", [1, 4, 8])
+def test_bk1_bk3_verification_norms(orc, golden13, p):
+    """CEED_BK/src/BK{1,3}/serial_verification.cc inputs (cos bases, in = 3,
+    JxW = 1, G = 2, 1000 elements): the printed norms."""
+    nq, nm, nel = p + 2, p + 1, 1000
+    basis = np.cos(np.arange(nq * nm, dtype=float))
+    dbasis = np.cos(np.arange(nq * nq, dtype=float))
+    u = np.full(nel * nm ** 3, 3.0)
+    n1 = np.linalg.norm(orc.bk1_evector(nm, nq, basis, np.ones(nel * nq ** 3), u))
+    n3 = np.linalg.norm(orc.bk3_evector(nm, nq, basis, dbasis, np.full(nel * 6 * nq ** 3, 2.0), u))
+    assert n1 == pytest.approx(golden13["bk1_norms"][str(p)], rel=1e-12)
+    assert n3 == pytest.approx(golden13["bk3_norms"][str(p)], rel=1e-12)
