@@ -332,6 +332,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         line["bk5_gauss_like_for_like"] = gauss_like_for_like(args)
         line["batched"] = batched_solves()
         line["ceed_bk1_bk3_evector"] = bk1_bk3_rates()
+        line["helmholtz_bp5"] = helmholtz_bp5(args)
     print(json.dumps(line), flush=True)
 
 
@@ -495,6 +496,59 @@ def bk1_bk3_rates(degree=4, target_dofs=6.7e7):
                                       "hbm_frac": byts / (ms * 1e-3) / 1e9 / peak}
     del u, y, jxw, G
     return out
+
+
+def helmholtz_bp5(args):
+    """bp5_kokkos's benchmark on the bench mesh: the Helmholtz operator (mass +
+    stiffness at QGauss(p+1)), its exact diagonal, Jacobi-PCG with
+    ReductionControl(100, 1e-15, 1e-8), best of 4 solves from x = 0, and the
+    vmult time as the best of 4 x 50 applies (bp5_kokkos/benchmark.cc:352-397),
+    with the seeded U[-1,1] right-hand side."""
+    import torch
+
+    import benchmarks_gb300 as mf
+    w = WORKLOAD
+    mesh = mf.BoxMesh(w["nx"], w["ny"], w["nz"], degree=w["degree"], amplitude=w["amplitude"])
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    H, t_setup = timed(lambda: mf.HelmholtzOperator(mesh, arith=args.arith))
+    _, t_diag = timed(H.compute_diagonal)
+    P = H.get_matrix_diagonal_inverse()
+    b = H.rhs_uniform(w["seed"])
+    best, its, converged = None, None, True
+
+    def solve(x, ctl):
+        try:
+            mf.SolverCG(ctl).solve(H, x, b, P)
+        except mf.MfgbError as e:  # the reference catches NoConvergence the same way
+            if e.status != mf._abi.ERR_NOT_CONVERGED:
+                raise
+            return False
+        return True
+
+    for _ in range(4):
+        x = H.initialize_dof_vector()
+        ctl = mf.ReductionControl(100, 1e-15, 1e-8)
+        converged, t = timed(lambda: solve(x, ctl))
+        best = t if best is None else min(best, t)
+        its = ctl.last_step()
+        reduction = ctl.last_value() / ctl.initial_value()
+    y = H.initialize_dof_vector()
+    mv = None
+    for _ in range(4):
+        _, t = timed(lambda: [H.vmult(y, x) for _ in range(50)])
+        mv = t / 50 if mv is None else min(mv, t / 50)
+    del H
+    return {"n_dofs": mesh.n_dofs, "setup_seconds": t_setup, "diagonal_seconds": t_diag,
+            "cg_seconds": best, "cg_iterations": its, "cg_converged": converged,
+            "cg_residual_reduction": reduction, "vmult_seconds": mv,
+            "vmult_GDoF/s": mesh.n_dofs / mv / 1e9}
 
 
 def bk6_rate(A, args):

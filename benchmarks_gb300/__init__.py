@@ -17,12 +17,14 @@ import os
 from dataclasses import dataclass
 
 from . import _abi
+from . import _abi  # noqa: F401
 from ._abi import MfgbError, ARITH_FP64, ARITH_FP64_DF, lib, library_path  # noqa: F401
 
 __all__ = [
     "BoxMesh", "LaplaceOperator", "ReductionControl", "SolverCG", "DiagonalMatrix",
     "PreconditionIdentity", "MGPreconditioner", "MfgbError", "ARITH_FP64", "ARITH_FP64_DF", "lib", "library_path",
-    "bk5_evector", "bk5_lvector", "dot",
+    "bk5_evector", "bk5_lvector", "bk1_evector", "bk3_evector", "dot", "HelmholtzOperator",
+    "BatchSolver", "batch_workload",
 ]
 
 _ARITH = {"fp64": ARITH_FP64, "df": ARITH_FP64_DF, "fp64_df": ARITH_FP64_DF,
@@ -98,13 +100,14 @@ class LaplaceOperator:
                  G=None, constrained=None, arith="df", quadrature="gll"):
         L = lib()
         self._op = ctypes.c_void_p()
-        if quadrature not in ("gll", "gauss"):
-            raise ValueError("quadrature must be 'gll' (collocation) or 'gauss' (BP5 variant)")
+        if quadrature not in ("gll", "gauss", "helmholtz"):
+            raise ValueError("quadrature must be 'gll' (collocation), 'gauss' (BP5 variant) or "
+                             "'helmholtz' (mass + stiffness at the Gauss points)")
         self.quadrature = quadrature
         if mesh is not None:
             desc = mesh._desc()
-            create = (L.mfgb_operator_create_box if quadrature == "gll"
-                      else L.mfgb_operator_create_box_gauss)
+            create = {"gll": L.mfgb_operator_create_box, "gauss": L.mfgb_operator_create_box_gauss,
+                      "helmholtz": L.mfgb_operator_create_box_helmholtz}[quadrature]
             _abi.check(create(ctypes.byref(desc), ctypes.byref(self._op)))
             self.mesh = mesh
         else:
@@ -213,6 +216,16 @@ class LaplaceOperator:
     @property
     def handle(self):
         return self._op
+
+
+class HelmholtzOperator(LaplaceOperator):
+    """``Step64::HelmholtzOperator`` of bp5_kokkos (benchmark.cc:141-251): mass
+    plus stiffness at QGauss(p+1) on the GLL nodal values, with the same
+    ``vmult`` / ``initialize_dof_vector`` / ``compute_diagonal`` /
+    ``get_matrix_diagonal_inverse`` interface."""
+
+    def __init__(self, mesh: BoxMesh, arith="df"):
+        super().__init__(mesh, arith=arith, quadrature="helmholtz")
 
 
 class DiagonalMatrix:

@@ -45,6 +45,12 @@ mfgb_status ensure_df(mfgb_operator *op) {
   if (st) return st;
   st = cuda_status(g_to_df(ng, op->d_G, op->d_Gdf, nullptr), "G -> double-float");
   if (st) return st;
+  if (op->d_JxW && !op->d_JxWdf) {
+    const int64_t nw = op->n_cells * (int64_t)op->n * op->n * op->n;
+    if ((st = dev_alloc((void **)&op->d_JxWdf, sizeof(float2) * nw, "JxW (double-float)")) ||
+        (st = cuda_status(g_to_df(nw, op->d_JxW, op->d_JxWdf, nullptr), "JxW -> double-float")))
+      return st;
+  }
   return cuda_status(cudaDeviceSynchronize(), "G -> double-float");
 }
 
@@ -59,14 +65,14 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
   if (arith == MFGB_ARITH_FP64) {
     e = op->quadrature
             ? bk5g_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->DG, op->Bq, partials,
-                       grid, s, done)
+                       grid, s, done, op->d_JxW)
             : bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s,
                       done);
   } else if (arith == MFGB_ARITH_FP64_DF) {
     if ((st = ensure_df(op))) return st;
     e = op->quadrature
             ? bk5g_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->DG, op->Bq, partials,
-                      grid, s, done)
+                      grid, s, done, op->d_JxWdf)
             : bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s,
                      done);
   } else {
@@ -118,13 +124,13 @@ mfgb_status apply_add_impl(mfgb_operator *op, double *dst, const double *src, in
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64) {
     e = op->quadrature ? bk5g_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->DG, op->Bq,
-                                  nullptr, nullptr, s, done)
+                                  nullptr, nullptr, s, done, op->d_JxW)
                        : bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, nullptr,
                                  nullptr, s, done);
   } else if (arith == MFGB_ARITH_FP64_DF) {
     if ((st = ensure_df(op))) return st;
     e = op->quadrature ? bk5g_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->DG,
-                                 op->Bq, nullptr, nullptr, s, done)
+                                 op->Bq, nullptr, nullptr, s, done, op->d_JxWdf)
                        : bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D,
                                 nullptr, nullptr, s, done);
   } else {
@@ -142,6 +148,8 @@ static void free_operator(mfgb_operator *op) {
   cudaFree(op->d_G32);
   cudaFree(op->d_constrained);
   cudaFree(op->d_partials);
+  cudaFree(op->d_JxW);
+  cudaFree(op->d_JxWdf);
   delete op;
 }
 
@@ -216,7 +224,7 @@ mfgb_status mfgb_get_kernel_shape(int arith, int degree, int *shape) {
 }
 
 static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out,
-                                   const BoxStride *bs = nullptr);
+                                   const BoxStride *bs = nullptr, bool mass = false);
 
 mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **out) {
   return create_box_impl(box, 0, out);
@@ -226,8 +234,12 @@ mfgb_status mfgb_operator_create_box_gauss(const mfgb_box_desc *box, mfgb_operat
   return create_box_impl(box, 1, out);
 }
 
+mfgb_status mfgb_operator_create_box_helmholtz(const mfgb_box_desc *box, mfgb_operator **out) {
+  return create_box_impl(box, 1, out, nullptr, true);
+}
+
 static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out,
-                                   const BoxStride *bs) {
+                                   const BoxStride *bs, bool mass) {
   if (!box || !out) {
     set_error("mfgb_operator_create_box: null argument");
     return MFGB_ERR_INVALID_ARG;
@@ -278,7 +290,8 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
   mfgb_status st;
   if ((st = dev_alloc((void **)&op->d_map, sizeof(uint32_t) * op->n_cells * n3, "dof map")) ||
       (st = dev_alloc((void **)&op->d_G, sizeof(double) * op->n_cells * 6 * n3, "G")) ||
-      (st = dev_alloc((void **)&op->d_constrained, sizeof(int64_t) * cons.size(), "constraints"))) {
+      (st = dev_alloc((void **)&op->d_constrained, sizeof(int64_t) * cons.size(), "constraints")) ||
+      (mass && (st = dev_alloc((void **)&op->d_JxW, sizeof(double) * op->n_cells * n3, "JxW")))) {
     free_operator(op);
     return st;
   }
@@ -287,7 +300,7 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
                         "constraints copy")) ||
       (st = cuda_status(box_map(*box, op->d_map, nullptr), "box map")) ||
       (st = cuda_status(box_geometry(*box, op->gll_x, op->gll_w, op->D, op->d_G, nullptr,
-                                     quadrature != 0, bs),
+                                     quadrature != 0, bs, op->d_JxW),
                         "box geometry")) ||
       (st = cuda_status(cudaDeviceSynchronize(), "box set-up"))) {
     free_operator(op);
@@ -503,16 +516,18 @@ mfgb_status mfgb_compute_diagonal(const mfgb_operator *op, double *d_diag, void 
     set_error("mfgb_compute_diagonal: invalid argument");
     return MFGB_ERR_INVALID_ARG;
   }
-  if (op->quadrature) {
-    set_error("mfgb_compute_diagonal: the Gauss-quadrature form has no diagonal kernel");
-    return MFGB_ERR_UNSUPPORTED;
-  }
   cudaStream_t s = (cudaStream_t)stream;
   mfgb_status st;
-  if ((st = cuda_status(cudaMemsetAsync(d_diag, 0, sizeof(double) * op->n_dofs, s), "diag = 0")) ||
-      (st = cuda_status(diagonal_f64(op->n, op->n_cells, op->d_map, op->d_G, op->D, d_diag, s),
-                        "diagonal kernel")))
+  if ((st = cuda_status(cudaMemsetAsync(d_diag, 0, sizeof(double) * op->n_dofs, s), "diag = 0")))
     return st;
+  if (op->quadrature)
+    st = cuda_status(diagonal_gauss(op->n, op->n_cells, op->d_map, op->d_G, op->d_JxW, op->Bq,
+                                    op->DG, d_diag, s),
+                     "diagonal kernel (Gauss points)");
+  else
+    st = cuda_status(diagonal_f64(op->n, op->n_cells, op->d_map, op->d_G, op->D, d_diag, s),
+                     "diagonal kernel");
+  if (st) return st;
   return cuda_status(set_constrained(op->n_constrained, op->d_constrained, d_diag, 1.0, s),
                      "diagonal constrained rows");
 }

@@ -554,7 +554,8 @@ __global__ void __launch_bounds__(E * N * N)
     bk5g_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
                 const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
                 typename A::VecT *__restrict__ dst, const BasisG<N, A> basis,
-                double *__restrict__ energy_partials, const int *__restrict__ done_flag) {
+                double *__restrict__ energy_partials, const int *__restrict__ done_flag,
+                const typename A::GType *__restrict__ jxw) {
   if (done_flag != nullptr && *done_flag) return;
   using V = typename A::V;
   using Acc = typename A::Acc;
@@ -659,7 +660,8 @@ __global__ void __launch_bounds__(E * N * N)
       sc[i * N2 + jk] = A::finish(bt);
     }
     __syncthreads();
-    // ---- transpose gradient, then back to the GLL nodes along i (registers)
+    // ---- transpose gradient (+ JxW u for the mass term), then back to the GLL
+    // nodes along i (registers)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
@@ -670,6 +672,7 @@ __global__ void __launch_bounds__(E * N * N)
         A::fma(a, Dtj[m], sb[i * N2 + m * N + k]);
         A::fma(a, Dtk[m], sc[i * N2 + j * N + m]);
       }
+      if (jxw != nullptr && valid) A::fma(a, A::load_g(__ldg(jxw + cell * N3 + i * N2 + jk)), u[i]);
       t[i] = A::finish(a);
     }
 #pragma unroll

@@ -53,7 +53,7 @@ template <int N, class A, bool EN>
 cudaError_t bk5g_with_basis(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
                             const typename A::VecT *src, typename A::VecT *dst, const double *DG64,
                             const double *B64, double *partials, int *grid, cudaStream_t s,
-                            const int *done) {
+                            const int *done, const typename A::GType *jxw) {
   constexpr int E = ElemsPerCta<N>::value;
   BasisG<N, A> b;
   for (int q = 0; q < N * N; ++q) {
@@ -66,7 +66,8 @@ cudaError_t bk5g_with_basis(int64_t n_cells, const uint32_t *map, const typename
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>(n_batches, (int64_t)per_sm * num_sms()));
   if (grid) *grid = g;
   if (n_cells <= 0) return cudaSuccess;
-  bk5g_kernel<N, E, A, EN><<<g, E * N * N, 0, s>>>(n_cells, map, G, src, dst, b, partials, done);
+  bk5g_kernel<N, E, A, EN><<<g, E * N * N, 0, s>>>(n_cells, map, G, src, dst, b, partials, done,
+                                                   jxw);
   return cudaGetLastError();
 }
 
@@ -74,10 +75,11 @@ template <class A, bool EN>
 cudaError_t bk5g_dispatch(int N, int64_t n_cells, const uint32_t *map, const typename A::GType *G,
                           const typename A::VecT *src, typename A::VecT *dst, const double *DG,
                           const double *B, double *partials, int *grid, cudaStream_t s,
-                          const int *done) {
+                          const int *done, const typename A::GType *jxw) {
   switch (N) {
 #define MFGB_GCASE(NN) \
-  case NN: return bk5g_with_basis<NN, A, EN>(n_cells, map, G, src, dst, DG, B, partials, grid, s, done);
+  case NN:             \
+    return bk5g_with_basis<NN, A, EN>(n_cells, map, G, src, dst, DG, B, partials, grid, s, done, jxw);
     MFGB_GCASE(2) MFGB_GCASE(3) MFGB_GCASE(4) MFGB_GCASE(5) MFGB_GCASE(6) MFGB_GCASE(7)
     MFGB_GCASE(8) MFGB_GCASE(9)
 #undef MFGB_GCASE

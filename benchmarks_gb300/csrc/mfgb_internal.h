@@ -18,6 +18,8 @@ struct mfgb_operator {
   double D[81] = {0};             // derivative matrix D[q*n + b]
   double gll_x[9] = {0}, gll_w[9] = {0};
   int quadrature = 0;             // 0: GLL collocation, 1: Gauss (p+1 points, BP5 variant)
+  double *d_JxW = nullptr;        // Gauss form with a mass term (Helmholtz): [n_cells][n^3]
+  float2 *d_JxWdf = nullptr;      // same, double-float pairs
   double DG[81] = {0};            // Gauss form: collocation derivative on the Gauss points
   double Bq[81] = {0};            // Gauss form: GLL basis at the Gauss points, Bq[q*n + i]
   bool is_box = false;
@@ -56,12 +58,15 @@ cudaError_t bk5_f32(int N, int64_t n_cells, const uint32_t *map, const float *G,
                     const int *done = nullptr);
 
 // Gauss-quadrature form (mfgb_bk5g.cu)
+// (jxw != nullptr adds the mass term: the Helmholtz form)
 cudaError_t bk5g_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,
                      const double *src, double *dst, const double *DG, const double *B,
-                     double *partials, int *grid, cudaStream_t s, const int *done = nullptr);
+                     double *partials, int *grid, cudaStream_t s, const int *done = nullptr,
+                     const double *jxw = nullptr);
 cudaError_t bk5g_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G,
                     const double *src, double *dst, const double *DG, const double *B,
-                    double *partials, int *grid, cudaStream_t s, const int *done = nullptr);
+                    double *partials, int *grid, cudaStream_t s, const int *done = nullptr,
+                    const float2 *jxw = nullptr);
 void gauss_nodes(int n, double *x, double *w);
 
 // assembled diagonal with per-cell weights: d_i = sum_e w_e (A_e)_ii (mfgb_mlp.cu)
@@ -86,7 +91,12 @@ struct BoxStride {
 };
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
                          const double *D, double *d_G, cudaStream_t s, bool at_gauss = false,
-                         const BoxStride *bs = nullptr);
+                         const BoxStride *bs = nullptr, double *d_JxW = nullptr);
+// exact diagonal of the Gauss-point operator (Laplacian, plus mass when JxW is
+// given) on a box, accumulated into diag (not zeroed; constrained rows untouched)
+cudaError_t diagonal_gauss(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                           const double *JxW, const double *B, const double *DG, double *diag,
+                           cudaStream_t s);
 cudaError_t g_to_df(int64_t n, const double *G, float2 *Gdf, cudaStream_t s);
 cudaError_t g_to_f32(int64_t n, const double *G, float *G32, cudaStream_t s);
 cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,

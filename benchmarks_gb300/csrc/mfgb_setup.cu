@@ -121,7 +121,8 @@ __device__ __forceinline__ void axis_span(int64_t c, int nf, int s, double &a, d
 // degree) in shared memory, then J = dx/dxi at the operator's GLL points
 // (the derivative matrix when both degrees agree, the tensor-product
 // geometry basis otherwise) and G = |det J| w_i w_j w_k Jinv Jinv^T.
-__global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__restrict__ G) {
+__global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__restrict__ G,
+                                    double *__restrict__ JxW) {
   __shared__ double xyz[729 * 3];
   const int n = b.degree + 1, n3 = n * n * n;
   const int ng = gp.ng, ng3 = ng * ng * ng;
@@ -189,6 +190,7 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
     Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
     Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
     const double jxw = fabs(det) * gp.w[i] * gp.w[j] * gp.w[k];
+    if (JxW) JxW[e * n3 + l] = jxw;
     double *Gc = G + e * 6 * n3 + l;
     int c = 0;
     for (int a = 0; a < 3; ++a)
@@ -229,7 +231,7 @@ void gauss_nodes(int n, double *x, double *w) {
 
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
                          const double *D, double *d_G, cudaStream_t s, bool at_gauss,
-                         const BoxStride *bs) {
+                         const BoxStride *bs, double *d_JxW) {
   GeomParams gp{};
   if (bs && bs->s > 1) {
     for (int d = 0; d < 3; ++d) gp.nf[d] = bs->nf[d];
@@ -266,7 +268,8 @@ cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const doub
   if (n_cells == 0) return cudaSuccess;
   const int pts = std::max(n * n * n, gp.ng * gp.ng * gp.ng);
   const int threads = ((pts + 31) / 32) * 32;
-  box_geometry_kernel<<<(unsigned)n_cells, threads > 256 ? 256 : threads, 0, s>>>(b, gp, d_G);
+  box_geometry_kernel<<<(unsigned)n_cells, threads > 256 ? 256 : threads, 0, s>>>(b, gp, d_G,
+                                                                                   d_JxW);
   return cudaGetLastError();
 }
 
@@ -339,6 +342,71 @@ cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const doub
   DiagParams dp;
   for (int i = 0; i < 81; ++i) dp.D[i] = i < N * N ? D[i] : 0.0;
   diagonal_kernel<<<152 * 16, 256, 0, s>>>(N, n_cells, map, G, dp, diag);
+  return cudaGetLastError();
+}
+
+// Exact diagonal of the Gauss-point operator (the quantity deal.II's
+// MatrixFreeTools::compute_diagonal returns for bp5_kokkos/benchmark.cc:218-251):
+// for local DoF (a, b, c) of a cell, sum over the Gauss points q = (i, j, k) of
+// grad(phi)^T G grad(phi) + JxW phi^2 with phi = B[i][a] B[j][b] B[k][c] and
+// d phi / d xi_0 = (DG B)[i][a] B[j][b] B[k][c], etc.  One CTA per cell, one
+// thread per local DoF; G and JxW of the cell staged in shared memory.
+struct GaussDiagParams {
+  double B[81], DB[81];  // B[q*n + a], DB = DG B
+};
+
+__global__ void __launch_bounds__(256)
+    diagonal_gauss_kernel(int N, int64_t n_cells, const uint32_t *__restrict__ map,
+                          const double *__restrict__ G, const double *__restrict__ JxW,
+                          GaussDiagParams gp, double *__restrict__ diag) {
+  __shared__ double sG[6 * 729];
+  __shared__ double sW[729];
+  const int N2 = N * N, N3 = N2 * N;
+  for (int64_t e = blockIdx.x; e < n_cells; e += gridDim.x) {
+    for (int t = threadIdx.x; t < 6 * N3; t += blockDim.x) sG[t] = G[e * 6 * N3 + t];
+    for (int t = threadIdx.x; t < N3; t += blockDim.x) sW[t] = JxW ? JxW[e * N3 + t] : 0.0;
+    __syncthreads();
+    for (int l = threadIdx.x; l < N3; l += blockDim.x) {
+      const uint32_t dof = map[e * N3 + l];
+      if (dof == MFGB_INVALID_DOF) continue;
+      const int a = l / N2, b = (l / N) % N, c = l % N;
+      double acc = 0.0;
+      for (int i = 0; i < N; ++i) {
+        const double bi = gp.B[i * N + a], di = gp.DB[i * N + a];
+        for (int j = 0; j < N; ++j) {
+          const double bj = gp.B[j * N + b], dj = gp.DB[j * N + b];
+          for (int k = 0; k < N; ++k) {
+            const double bk = gp.B[k * N + c], dk = gp.DB[k * N + c];
+            const int q = (i * N + j) * N + k;
+            const double r = di * bj * bk, s = bi * dj * bk, t = bi * bj * dk, ph = bi * bj * bk;
+            acc += sG[0 * N3 + q] * r * r + sG[3 * N3 + q] * s * s + sG[5 * N3 + q] * t * t +
+                   2.0 * (sG[1 * N3 + q] * r * s + sG[2 * N3 + q] * r * t + sG[4 * N3 + q] * s * t) +
+                   sW[q] * ph * ph;
+          }
+        }
+      }
+      atomicAdd(diag + dof, acc);
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t diagonal_gauss(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                           const double *JxW, const double *B, const double *DG, double *diag,
+                           cudaStream_t s) {
+  if (N < 2 || N > 9) return cudaErrorInvalidValue;
+  GaussDiagParams gp{};
+  for (int q = 0; q < N; ++q)
+    for (int a = 0; a < N; ++a) {
+      gp.B[q * N + a] = B[q * N + a];
+      double d = 0.0;
+      for (int m = 0; m < N; ++m) d += DG[q * N + m] * B[m * N + a];
+      gp.DB[q * N + a] = d;
+    }
+  if (n_cells == 0) return cudaSuccess;
+  const int threads = std::min(256, ((N * N * N + 31) / 32) * 32);
+  const unsigned grid = (unsigned)std::min<int64_t>(n_cells, 152 * 16);
+  diagonal_gauss_kernel<<<grid, threads, 0, s>>>(N, n_cells, map, G, JxW, gp, diag);
   return cudaGetLastError();
 }
 

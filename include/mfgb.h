@@ -99,8 +99,15 @@ mfgb_status mfgb_operator_create_box(const mfgb_box_desc *box, mfgb_operator **o
    values interpolated from the GLL nodes, collocation gradient at the Gauss
    points; bakeoff_problems_dealii/include/portable_laplace_operator_bk35.h:114
    and bk3_kokkos_kernel.h:156-404), on the same box mesh.  Exactly
-   integrated stiffness on affine cells.  (No diagonal kernel for this form.) */
+   integrated stiffness on affine cells. */
 mfgb_status mfgb_operator_create_box_gauss(const mfgb_box_desc *box, mfgb_operator **op);
+
+/* The Helmholtz operator of bp5_kokkos (Step64::HelmholtzOperator,
+   bp5_kokkos/benchmark.cc:141-205): mass plus stiffness, (u, v) + (grad u,
+   grad v), at QGauss(p+1) on GLL nodal values (:93-94, :179-191); same box
+   mesh and Dirichlet rows.  mfgb_compute_diagonal gives its exact diagonal
+   (the compute_diagonal of :218-251). */
+mfgb_status mfgb_operator_create_box_helmholtz(const mfgb_box_desc *box, mfgb_operator **op);
 
 /* Same, from caller-provided host arrays (the deal.II set-up path):
    h_dof_map[cell*(p+1)^3 + l] (0xFFFFFFFF = constrained), h_G[cell][6][(p+1)^3]

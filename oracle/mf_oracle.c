@@ -288,8 +288,17 @@ int orc_cell_geometry(int n, const double *D, const double *w, const double *xyz
 /* Same as orc_cell_geometry with the Jacobian of the Q_{ng-1} geometry
    interpolant evaluated at the n GLL points per direction:
    dx/dxi_r (i,j,k) = sum_abc Dv[i][a] V[j][b] V[k][c] x_abc (and cyclic). */
+static int cell_geometry_general(int n, int ng, const double *V, const double *Dv, const double *w,
+                                 const double *xyz, double *Gc, double *JxWc);
+
 int orc_cell_geometry_general(int n, int ng, const double *V, const double *Dv, const double *w,
                               const double *xyz, double *Gc) {
+  return cell_geometry_general(n, ng, V, Dv, w, xyz, Gc, NULL);
+}
+
+/* the same, also writing JxW per point when JxWc != NULL */
+static int cell_geometry_general(int n, int ng, const double *V, const double *Dv, const double *w,
+                                 const double *xyz, double *Gc, double *JxWc) {
   const int nq = n * n * n, ng2 = ng * ng;
   int bad = 0, sign0 = 0;
   for (int i = 0; i < n; ++i)
@@ -328,6 +337,8 @@ int orc_cell_geometry_general(int n, int ng, const double *V, const double *Dv, 
         Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
         const double jxw = fabs(det) * w[i] * w[j] * w[k];
         const int q = i * n * n + j * n + k;
+        if (JxWc) JxWc[q] = jxw;
+        if (JxWc) JxWc[q] = jxw;
         int c = 0;
         for (int a = 0; a < 3; ++a)
           for (int bb = a; bb < 3; ++bb) {
@@ -493,6 +504,10 @@ void orc_gauss_basis_matrices(int p, int nq, double *B, double *DG) {
 }
 
 int64_t orc_box_geometry_gauss(const orc_box *b, int nq, double *Gg) {
+  return orc_box_geometry_gauss_jxw(b, nq, Gg, NULL);
+}
+
+int64_t orc_box_geometry_gauss_jxw(const orc_box *b, int nq, double *Gg, double *JxW) {
   const int ng = geo_degree(b) + 1, ngq = ng * ng * ng, nq3 = nq * nq * nq;
   double xgeo[16], wgeo[16], xq[16], wq[16], V[256], Dv[256];
   orc_gll(ng, xgeo, wgeo);
@@ -510,7 +525,8 @@ int64_t orc_box_geometry_gauss(const orc_box *b, int nq, double *Gg) {
 #pragma omp for schedule(static)
     for (int64_t e = 0; e < n_cells; ++e) {
       orc_box_cell_nodes(b, e, xyz);
-      bad += orc_cell_geometry_general(nq, ng, V, Dv, wq, xyz, Gg + e * 6 * nq3);
+      bad += cell_geometry_general(nq, ng, V, Dv, wq, xyz, Gg + e * 6 * nq3,
+                                   JxW ? JxW + e * nq3 : NULL);
     }
     free(xyz);
   }
@@ -541,7 +557,7 @@ static void contract(const double *M, int rows, int cols, int dir, int transpose
 
 /* one cell: y = B^T D_G^T G D_G B u  (u, y: n^3 GLL nodal values) */
 static void bk5g_element(int n, int nq, const double *B, const double *DG, const double *G,
-                         const double *u, double *y, double *w) {
+                         const double *W, const double *u, double *y, double *w) {
   const int nq3 = nq * nq * nq;
   double *t1 = w, *t2 = w + nq3, *uq = w + 2 * nq3, *vr = w + 3 * nq3, *vs = w + 4 * nq3,
          *vt = w + 5 * nq3, *acc = w + 6 * nq3, *t3 = w + 7 * nq3;
@@ -568,6 +584,9 @@ static void bk5g_element(int n, int nq, const double *B, const double *DG, const
   for (int q = 0; q < nq3; ++q) acc[q] += t1[q];
   contract(DG, nq, nq, 2, 1, e_qqq, vt, t1);
   for (int q = 0; q < nq3; ++q) acc[q] += t1[q];
+  /* mass term (Helmholtz form, bp5_kokkos/benchmark.cc:93): JxW u at the points */
+  if (W)
+    for (int q = 0; q < nq3; ++q) acc[q] += W[q] * uq[q];
   /* back to the GLL nodal values */
   int e_qqq2[3] = {nq, nq, nq}, e_qqn2[3] = {nq, nq, n}, e_qnn2[3] = {nq, n, n};
   contract(B, nq, n, 2, 1, e_qqq2, acc, t2);
@@ -588,7 +607,7 @@ void orc_bk3_evector(int nm, int nq, int64_t nelmt, const double *basis, const d
     double *w = (double *)malloc(sizeof(double) * 8 * nq3);
 #pragma omp for schedule(static)
     for (int64_t e = 0; e < nelmt; ++e)
-      bk5g_element(nm, nq, basis, dbasis, G + e * 6 * nq3, in + e * nm3, out + e * nm3, w);
+      bk5g_element(nm, nq, basis, dbasis, G + e * 6 * nq3, NULL, in + e * nm3, out + e * nm3, w);
     free(w);
   }
 }
@@ -618,9 +637,70 @@ void orc_bk1_evector(int nm, int nq, int64_t nelmt, const double *basis, const d
   }
 }
 
+static void bkg_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                      const uint32_t *map, const double *Gg, const double *JxW, int64_t n_dofs,
+                      int64_t n_constrained, const int64_t *constrained, const double *src,
+                      double *dst);
+
 void orc_bk5g_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
                     const uint32_t *map, const double *Gg, int64_t n_dofs, int64_t n_constrained,
                     const int64_t *constrained, const double *src, double *dst) {
+  bkg_apply(n, nq, B, DG, n_cells, map, Gg, NULL, n_dofs, n_constrained, constrained, src, dst);
+}
+
+/* Step64::HelmholtzOperator::vmult (bp5_kokkos/benchmark.cc:195-205): mass +
+   stiffness at the Gauss points, dst = 0, cell loop, identity rows */
+void orc_helmholtz_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                         const uint32_t *map, const double *Gg, const double *JxW, int64_t n_dofs,
+                         int64_t n_constrained, const int64_t *constrained, const double *src,
+                         double *dst) {
+  bkg_apply(n, nq, B, DG, n_cells, map, Gg, JxW, n_dofs, n_constrained, constrained, src, dst);
+}
+
+/* exact diagonal of the Gauss-point operator (plus mass when JxW != NULL), the
+   result of MatrixFreeTools::compute_diagonal (bp5_kokkos/benchmark.cc:231-236),
+   1 on constrained rows (not inverted) */
+void orc_gauss_diagonal(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                        const uint32_t *map, const double *Gg, const double *JxW, int64_t n_dofs,
+                        int64_t n_constrained, const int64_t *constrained, double *diag) {
+  const int n3 = n * n * n, nq3 = nq * nq * nq;
+  double DB[256];
+  for (int q = 0; q < nq; ++q)
+    for (int a = 0; a < n; ++a) {
+      double d = 0;
+      for (int m = 0; m < nq; ++m) d += DG[q * nq + m] * B[m * n + a];
+      DB[q * n + a] = d;
+    }
+  memset(diag, 0, sizeof(double) * n_dofs);
+  for (int64_t e = 0; e < n_cells; ++e) {
+    const double *G = Gg + e * 6 * nq3;
+    for (int l = 0; l < n3; ++l) {
+      const uint32_t dof = map[e * n3 + l];
+      if (dof == ORC_INVALID_DOF) continue;
+      const int a = l / (n * n), bb = (l / n) % n, c = l % n;
+      double acc = 0;
+      for (int i = 0; i < nq; ++i)
+        for (int j = 0; j < nq; ++j)
+          for (int k = 0; k < nq; ++k) {
+            const int q = (i * nq + j) * nq + k;
+            const double r = DB[i * n + a] * B[j * n + bb] * B[k * n + c];
+            const double sv = B[i * n + a] * DB[j * n + bb] * B[k * n + c];
+            const double t = B[i * n + a] * B[j * n + bb] * DB[k * n + c];
+            const double ph = B[i * n + a] * B[j * n + bb] * B[k * n + c];
+            acc += G[q] * r * r + G[3 * nq3 + q] * sv * sv + G[5 * nq3 + q] * t * t +
+                   2.0 * (G[nq3 + q] * r * sv + G[2 * nq3 + q] * r * t + G[4 * nq3 + q] * sv * t) +
+                   (JxW ? JxW[e * nq3 + q] * ph * ph : 0.0);
+          }
+      diag[dof] += acc;
+    }
+  }
+  for (int64_t i = 0; i < n_constrained; ++i) diag[constrained[i]] = 1.0;
+}
+
+static void bkg_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                      const uint32_t *map, const double *Gg, const double *JxW, int64_t n_dofs,
+                      int64_t n_constrained, const int64_t *constrained, const double *src,
+                      double *dst) {
   const int n3 = n * n * n, nq3 = nq * nq * nq;
   memset(dst, 0, sizeof(double) * n_dofs);
 #pragma omp parallel
@@ -631,7 +711,7 @@ void orc_bk5g_apply(int n, int nq, const double *B, const double *DG, int64_t n_
     for (int64_t e = 0; e < n_cells; ++e) {
       const uint32_t *me = map + e * n3;
       for (int l = 0; l < n3; ++l) u[l] = me[l] == ORC_INVALID_DOF ? 0.0 : src[me[l]];
-      bk5g_element(n, nq, B, DG, Gg + e * 6 * nq3, u, y, w);
+      bk5g_element(n, nq, B, DG, Gg + e * 6 * nq3, JxW ? JxW + e * nq3 : NULL, u, y, w);
       for (int l = 0; l < n3; ++l)
         if (me[l] != ORC_INVALID_DOF) {
 #pragma omp atomic
@@ -852,6 +932,27 @@ typedef struct {
 static void gauss_apply(void *vc, const double *src, double *dst) {
   gauss_ctx *c = (gauss_ctx *)vc;
   orc_bk5g_apply(c->n, c->nq, c->B, c->DG, c->n_cells, c->map, c->G, c->N, c->nc, c->c, src, dst);
+}
+
+typedef struct {
+  gauss_ctx g;
+  const double *JxW;
+} helmholtz_ctx;
+
+static void helmholtz_apply_cb(void *vc, const double *src, double *dst) {
+  helmholtz_ctx *h = (helmholtz_ctx *)vc;
+  gauss_ctx *c = &h->g;
+  orc_helmholtz_apply(c->n, c->nq, c->B, c->DG, c->n_cells, c->map, c->G, h->JxW, c->N, c->nc,
+                      c->c, src, dst);
+}
+
+orc_solve_info orc_cg_solve_helmholtz(int n, int nq, const double *B, const double *DG,
+                                      int64_t n_cells, const uint32_t *map, const double *Gg,
+                                      const double *JxW, int64_t N, int64_t n_constrained,
+                                      const int64_t *constrained, const double *diag_inv,
+                                      const double *b, double *x, orc_reduction_control ctl) {
+  helmholtz_ctx h = {{n, nq, B, DG, n_cells, N, n_constrained, map, Gg, constrained}, JxW};
+  return orc_cg_solve_op(helmholtz_apply_cb, &h, N, diag_inv, b, x, ctl);
 }
 
 orc_solve_info orc_cg_solve_gauss(int n, int nq, const double *B, const double *DG,

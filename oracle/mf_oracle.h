@@ -101,6 +101,8 @@ typedef struct {
 void orc_gauss_basis_matrices(int p, int nq, double *B, double *DG);
 /* G at the nq^3 Gauss points (Gauss weights) of every box cell */
 int64_t orc_box_geometry_gauss(const orc_box *b, int nq, double *Gg);
+/* the same, also JxW[cell][nq^3] at the Gauss points (JxW may be NULL) */
+int64_t orc_box_geometry_gauss_jxw(const orc_box *b, int nq, double *Gg, double *JxW);
 /* b_i = int phi_i f dx, f = 1, by the nq-point Gauss rule; 0 on constrained */
 void orc_box_rhs_unit_gauss(const orc_box *b, int nq, int64_t n_constrained,
                             const int64_t *constrained, double *rhs);
@@ -141,6 +143,20 @@ orc_solve_info orc_cg_solve_op(orc_apply_fn apply, void *ctx, int64_t n_dofs,
                                const double *diag_inv, const double *b, double *x,
                                orc_reduction_control ctl);
 /* CG on the Gauss-quadrature operator (PreconditionIdentity if diag_inv NULL) */
+/* Helmholtz form of bp5_kokkos (mass + stiffness at the Gauss points): apply,
+   exact diagonal (JxW NULL: the stiffness alone; 1 on constrained rows), CG */
+void orc_helmholtz_apply(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                         const uint32_t *map, const double *Gg, const double *JxW, int64_t n_dofs,
+                         int64_t n_constrained, const int64_t *constrained, const double *src,
+                         double *dst);
+void orc_gauss_diagonal(int n, int nq, const double *B, const double *DG, int64_t n_cells,
+                        const uint32_t *map, const double *Gg, const double *JxW, int64_t n_dofs,
+                        int64_t n_constrained, const int64_t *constrained, double *diag);
+orc_solve_info orc_cg_solve_helmholtz(int n, int nq, const double *B, const double *DG,
+                                      int64_t n_cells, const uint32_t *map, const double *Gg,
+                                      const double *JxW, int64_t N, int64_t n_constrained,
+                                      const int64_t *constrained, const double *diag_inv,
+                                      const double *b, double *x, orc_reduction_control ctl);
 orc_solve_info orc_cg_solve_gauss(int n, int nq, const double *B, const double *DG,
                                   int64_t n_cells, const uint32_t *map, const double *Gg,
                                   int64_t n_dofs, int64_t n_constrained,

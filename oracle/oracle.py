@@ -311,6 +311,14 @@ def _gauss_sigs():
     L.orc_cg_solve_gauss.argtypes = [ctypes.c_int, ctypes.c_int, P, P, i64, P, P, i64, i64, P, P,
                                      P, P, _Ctl]
     L.orc_cg_solve_gauss.restype = _Info
+    L.orc_box_geometry_gauss_jxw.argtypes = [ctypes.POINTER(_Box), ctypes.c_int, P, P]
+    L.orc_box_geometry_gauss_jxw.restype = i64
+    L.orc_helmholtz_apply.argtypes = [ctypes.c_int, ctypes.c_int, P, P, i64, P, P, P, i64, i64, P,
+                                      P, P]
+    L.orc_gauss_diagonal.argtypes = [ctypes.c_int, ctypes.c_int, P, P, i64, P, P, P, i64, i64, P, P]
+    L.orc_cg_solve_helmholtz.argtypes = [ctypes.c_int, ctypes.c_int, P, P, i64, P, P, P, i64, i64,
+                                         P, P, P, P, _Ctl]
+    L.orc_cg_solve_helmholtz.restype = _Info
     L._gauss_ready = True
     return L
 
@@ -372,3 +380,46 @@ def reference_scaling_mesh(cycle: int, degree: int):
         cells.append(sub << n_refine)
         hi.append(2.8 if d < rem else 0.9)
     return cells, (-1.0, -1.0, -1.0), tuple(hi)
+
+
+class HelmholtzProblem(GaussProblem):
+    """bp5_kokkos's Helmholtz operator (Step64::HelmholtzOperator,
+    bp5_kokkos/benchmark.cc:51-251): mass + stiffness at nq = p + 1 Gauss points
+    on the GLL nodal values, Dirichlet rows as identity."""
+
+    def __init__(self, nx, ny, nz, degree, amplitude=0.0, lo=(0.0, 0.0, 0.0),
+                 hi=(1.0, 1.0, 1.0), geometry_degree=0):
+        super().__init__(nx, ny, nz, degree, None, amplitude, lo, hi, geometry_degree)
+        q = self.nq
+        self.JxW = np.zeros(self.n_cells * q ** 3)
+        G2 = np.zeros_like(self.Gg)
+        _gauss_sigs().orc_box_geometry_gauss_jxw(ctypes.byref(self._box), q, _p(G2), _p(self.JxW))
+
+    def apply(self, src):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        dst = np.zeros(self.n_dofs)
+        _gauss_sigs().orc_helmholtz_apply(self.n, self.nq, _p(self.B), _p(self.DG), self.n_cells,
+                                          _p(self.map), _p(self.Gg), _p(self.JxW), self.n_dofs,
+                                          self.constrained.size, _p(self.constrained), _p(src),
+                                          _p(dst))
+        return dst
+
+    def diagonal(self):
+        d = np.zeros(self.n_dofs)
+        _gauss_sigs().orc_gauss_diagonal(self.n, self.nq, _p(self.B), _p(self.DG), self.n_cells,
+                                         _p(self.map), _p(self.Gg), _p(self.JxW), self.n_dofs,
+                                         self.constrained.size, _p(self.constrained), _p(d))
+        return d
+
+    def cg(self, b, diag_inv=None, max_steps=100, tol=1e-15, reduce=1e-8, x0=None):
+        """SolverCG + ReductionControl (defaults: bp5_kokkos/benchmark.cc:355)."""
+        x = np.zeros(self.n_dofs) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        info = _gauss_sigs().orc_cg_solve_helmholtz(
+            self.n, self.nq, _p(self.B), _p(self.DG), self.n_cells, _p(self.map), _p(self.Gg),
+            _p(self.JxW), self.n_dofs, self.constrained.size, _p(self.constrained),
+            _p(diag_inv) if diag_inv is not None else None, _p(b), _p(x),
+            _Ctl(min(max_steps, 2**31 - 1), tol, reduce))
+        return x, {"steps": info.steps, "initial": info.initial, "last": info.last,
+                   "converged": bool(info.converged)}
+

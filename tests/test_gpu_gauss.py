@@ -26,6 +26,11 @@ def rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
+def torch_from(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
 @pytest.mark.parametrize("p", range(1, 9))
 @pytest.mark.parametrize("arith", ["fp64", "df"])
 def test_gauss_operator_matches_oracle(mf, orc, p, arith):
@@ -56,3 +61,47 @@ def test_published_cg_counts_on_gpu(mf, orc, cycle):
     assert ctl.last_step() == pub["cg_its"]
     red = (ctl.last_value() / ctl.initial_value()) ** (1.0 / ctl.last_step())
     assert f"{red:.3e}" == f"{pub['cg_reduction']:.3e}"
+
+
+@pytest.mark.parametrize("arith", ["fp64", "df"])
+@pytest.mark.parametrize("p", [1, 2, 4, 6, 8])
+def test_helmholtz_operator_matches_oracle(mf, orc, p, arith):
+    """bp5_kokkos's Helmholtz operator (mass + stiffness at QGauss(p+1)) on a
+    deformed box: vmult and the exact diagonal against the oracle."""
+    cells = (3, 2, 4) if p <= 4 else (2, 2, 2)
+    H = mf.HelmholtzOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.05), arith=arith)
+    ref = orc.HelmholtzProblem(*cells, p, amplitude=0.05)
+    src = np.random.default_rng(p).uniform(-1, 1, ref.n_dofs)
+    dst = H.initialize_dof_vector()
+    H.vmult(dst, torch_from(src))
+    assert rel(dst.cpu().numpy(), ref.apply(src)) <= 1e-12
+    d = H.compute_diagonal()
+    assert rel(d.cpu().numpy(), ref.diagonal()) <= 1e-13
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_gauss_diagonal_matches_oracle(mf, orc, p):
+    A = mf.LaplaceOperator(mf.BoxMesh(3, 3, 2, degree=p, amplitude=0.08), quadrature="gauss")
+    ref = orc.GaussProblem(3, 3, 2, p, amplitude=0.08)
+    d = A.compute_diagonal()
+    dr = np.zeros(ref.n_dofs)
+    orc._gauss_sigs().orc_gauss_diagonal(ref.n, ref.nq, orc._p(ref.B), orc._p(ref.DG), ref.n_cells,
+                                         orc._p(ref.map), orc._p(ref.Gg), None, ref.n_dofs,
+                                         ref.constrained.size, orc._p(ref.constrained), orc._p(dr))
+    assert rel(d.cpu().numpy(), dr) <= 1e-13
+
+
+def test_helmholtz_jacobi_pcg_counts(mf, orc):
+    """Jacobi-PCG with bp5_kokkos's ReductionControl(100, 1e-15, 1e-8): the same
+    iteration count as the oracle and a solution within the tolerance."""
+    mesh = mf.BoxMesh(4, 4, 3, degree=3, amplitude=0.05)
+    H = mf.HelmholtzOperator(mesh)
+    ref = orc.HelmholtzProblem(4, 4, 3, 3, amplitude=0.05)
+    b = H.rhs_uniform(17)
+    x = H.initialize_dof_vector()
+    ctl = mf.ReductionControl(100, 1e-15, 1e-8)
+    mf.SolverCG(ctl).solve(H, x, b, H.get_matrix_diagonal_inverse())
+    dinv = 1.0 / ref.diagonal()
+    xr, info = ref.cg(b.cpu().numpy(), diag_inv=dinv)
+    assert ctl.last_step() == info["steps"]
+    assert rel(x.cpu().numpy(), xr) <= 1e-9

@@ -244,3 +244,31 @@ def test_bk1_bk3_verification_norms(orc, golden13, p):
     n3 = np.linalg.norm(orc.bk3_evector(nm, nq, basis, dbasis, np.full(nel * 6 * nq ** 3, 2.0), u))
     assert n1 == pytest.approx(golden13["bk1_norms"][str(p)], rel=1e-12)
     assert n3 == pytest.approx(golden13["bk3_norms"][str(p)], rel=1e-12)
+
+
+def test_helmholtz_mass_term_and_diagonal(orc):
+    """Helmholtz = stiffness + mass at QGauss(p+1): on an affine cube the mass
+    part integrates v^2 exactly for the bubble v = x(1-x) y(1-y) z(1-z); the
+    diagonal equals the operator's own diagonal entries."""
+    H = orc.HelmholtzProblem(2, 2, 3, 2, amplitude=0.0)
+    K = orc.GaussProblem(2, 2, 3, 2, amplitude=0.0)
+    free = np.setdiff1d(np.arange(H.n_dofs), H.constrained)
+    # nodal coordinates of the lexicographic GLL nodes (x fastest)
+    xg, _ = orc.gll(3)
+    def axis(n):
+        return np.concatenate([[0.0]] + [c / n + (xg[1:] + 1) / (2 * n) for c in range(n)])
+    X, Y, Z = np.meshgrid(axis(2), axis(2), axis(3), indexing="ij")
+    v = (X * (1 - X) * Y * (1 - Y) * Z * (1 - Z)).transpose(2, 1, 0).reshape(-1)
+    mass = v @ (H.apply(v) - K.apply(v))
+    assert mass == pytest.approx((1 / 30) ** 3, rel=1e-12)
+    d = H.diagonal()
+    for i in free[:: max(1, free.size // 15)]:
+        e = np.zeros(H.n_dofs)
+        e[i] = 1.0
+        assert d[i] == pytest.approx(H.apply(e)[i], rel=1e-12)
+    assert np.all(d[H.constrained] == 1.0)
+    # symmetric positive definite on the free DoFs
+    u, w = np.random.default_rng(0).uniform(-1, 1, (2, H.n_dofs))
+    u[H.constrained] = w[H.constrained] = 0
+    assert u @ H.apply(w) == pytest.approx(w @ H.apply(u), rel=1e-12)
+    assert u @ H.apply(u) > 0
