@@ -432,6 +432,7 @@ def batched_solves(n_problems=256, n_sequential=24):
            "seconds": best, "dofs_per_second": B.n_dofs / best,
            "iterations_min_mean_max": [min(steps), float(np.mean(steps)), max(steps)],
            "all_converged": all(i["converged"] for i in B.infos),
+           "replans": B.replans,
            "depth_dofs": B.depth_dofs}
     seq_t, seq_dofs = 0.0, 0
     for i in range(n_sequential):

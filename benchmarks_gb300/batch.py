@@ -112,5 +112,8 @@ class BatchSolver:
                                        ctypes.byref(ctl), infos, _stream_ptr())
         self.infos = [{"steps": i.steps, "initial": i.initial, "last": i.last,
                        "converged": bool(i.converged)} for i in infos]
+        r = ctypes.c_int()
+        _abi.check(lib().mfgb_batch_last_solve_stats(self._b, ctypes.byref(r)))
+        self.replans = r.value
         _abi.check(st)
         return x

@@ -189,37 +189,39 @@ __global__ void __launch_bounds__(T256)
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// sum of the chunk partials of problem blockIdx.x (chunks cbeg[p] .. cbeg[p+1])
+// CTA b handles problem pid[b]: the sum of its chunk partials cbeg[b] .. cbeg[b+1]
 __device__ __forceinline__ double problem_sum(const int *__restrict__ cbeg,
                                               const double *__restrict__ part, double *sh) {
-  const int p = blockIdx.x;
+  const int b = blockIdx.x;
   double s = 0;
-  for (int i = cbeg[p] + threadIdx.x; i < cbeg[p + 1]; i += blockDim.x) s += part[i];
+  for (int i = cbeg[b] + threadIdx.x; i < cbeg[b + 1]; i += blockDim.x) s += part[i];
   return cta_sum(s, sh);
 }
 
 __global__ void __launch_bounds__(T256)
-    kb_sum_pap(const int *__restrict__ cbeg, const double *__restrict__ part, BScal *__restrict__ sc) {
+    kb_sum_pap(const int *__restrict__ cbeg, const int *__restrict__ pid,
+               const double *__restrict__ part, BScal *__restrict__ sc) {
   __shared__ double sh[T256 / 32];
   const double s = problem_sum(cbeg, part, sh);
-  if (threadIdx.x == 0) sc[blockIdx.x].pap = s;
+  if (threadIdx.x == 0) sc[pid[blockIdx.x]].pap = s;
 }
 
 __global__ void __launch_bounds__(T256)
-    kb_sum_rz(const int *__restrict__ cbeg, const double *__restrict__ part, BScal *__restrict__ sc) {
+    kb_sum_rz(const int *__restrict__ cbeg, const int *__restrict__ pid,
+              const double *__restrict__ part, BScal *__restrict__ sc) {
   __shared__ double sh[T256 / 32];
   const double s = problem_sum(cbeg, part, sh);
-  if (threadIdx.x == 0) sc[blockIdx.x].rz_new = s;
+  if (threadIdx.x == 0) sc[pid[blockIdx.x]].rz_new = s;
 }
 
 // initial residual norms: tol_eff = max(tol, reduce |r0|)
 __global__ void __launch_bounds__(T256)
-    kb_init(const int *__restrict__ cbeg, const double *__restrict__ part, BScal *__restrict__ sc,
-            double tol, double reduce) {
+    kb_init(const int *__restrict__ cbeg, const int *__restrict__ pid,
+            const double *__restrict__ part, BScal *__restrict__ sc, double tol, double reduce) {
   __shared__ double sh[T256 / 32];
   const double rr = problem_sum(cbeg, part, sh);
   if (threadIdx.x == 0) {
-    BScal &q = sc[blockIdx.x];
+    BScal &q = sc[pid[blockIdx.x]];
     const double res = sqrt(rr);
     q.res0 = q.res = res;
     q.tol_eff = fmax(tol, reduce * res);
@@ -257,12 +259,13 @@ __global__ void __launch_bounds__(T256)
 // |r| test per problem (deal.II SolverCG / ReductionControl): converged when
 // |r| <= tol_eff, failed at max_steps or NaN; counts the problems still running
 __global__ void __launch_bounds__(T256)
-    kb_sum_check(const int *__restrict__ cbeg, const double *__restrict__ part,
-                 BScal *__restrict__ sc, int max_steps, int *__restrict__ active) {
+    kb_sum_check(const int *__restrict__ cbeg, const int *__restrict__ pid,
+                 const double *__restrict__ part, BScal *__restrict__ sc, int max_steps,
+                 int *__restrict__ active) {
   __shared__ double sh[T256 / 32];
   const double rr = problem_sum(cbeg, part, sh);
   if (threadIdx.x == 0) {
-    BScal &q = sc[blockIdx.x];
+    BScal &q = sc[pid[blockIdx.x]];
     if (!q.done) {
       const double res = sqrt(rr);
       q.res = res;
@@ -318,6 +321,34 @@ struct PGroup {
   int g = 0;                   // union operator of the fine degree (its map is map_f)
   uint32_t *map_c = nullptr;   // coarse maps of the same cells, depth+1 offsets
   PTransferParams P{};
+};
+
+// What one batched CG iteration launches on one depth, for a set of problems:
+// the union operators, identity rows, chunk tables and transfer tables.
+struct DepthPlan {
+  std::vector<mfgb_operator *> groups;
+  const int64_t *d_cons = nullptr;
+  int64_t n_cons = 0;
+  const Chunk *d_cheb = nullptr, *d_pch = nullptr, *d_hfine = nullptr, *d_hcoarse = nullptr;
+  int n_cheb = 0, n_pch = 0, n_hfine = 0, n_hcoarse = 0;
+  std::vector<PGroup> pgroups;
+  const HPart *d_hp = nullptr;
+};
+
+// A plan: every problem (built at set-up), or the problems still running
+// (gathered from the full plan's arrays while solving: the depth vectors and the
+// maps' offsets into them stay as they are).
+struct Plan {
+  std::vector<DepthPlan> depth;
+  const CoarseDesc *d_coarse = nullptr;
+  int n_coarse = 0, coarse_smem = 0;
+  const Chunk *d_all = nullptr;  // outer CG chunks (depth 0)
+  int n_all = 0;
+  const int *d_cbeg = nullptr, *d_pid = nullptr;
+  int n_prob = 0;
+  int64_t dofs = 0;              // depth-0 DoFs of its problems
+  bool owns = false;             // a gathered plan owns what it points to
+  std::vector<void *> mem;
 };
 
 struct Depth {
@@ -416,14 +447,17 @@ struct mfgb_batch {
   int coarse_smem = 0;
   double *d_Ainv = nullptr;
   int32_t *d_cids = nullptr;
+  std::vector<mfgb::CoarseDesc> coarse_host;  // per problem, for gathered plans
   // outer CG (depth 0, every problem)
   mfgb::Chunk *d_all = nullptr;
   int n_all = 0;
-  int *d_cbeg = nullptr;
+  int *d_cbeg = nullptr, *d_pid = nullptr;
+  mfgb::Plan full;
   double *r = nullptr, *z = nullptr, *p = nullptr, *v = nullptr, *part = nullptr;
   mfgb::BScal *d_scal = nullptr;
   int *d_active = nullptr;
   int *h_active = nullptr;  // pinned
+  int last_replans = 0;     // plans gathered during the last solve
 };
 
 namespace mfgb {
@@ -439,7 +473,7 @@ void free_batch(mfgb_batch *B) {
     cudaFree(D.d_coef); cudaFree(D.d_hp); cudaFree(D.d_hfine); cudaFree(D.d_hcoarse);
   }
   cudaFree(B->d_coarse); cudaFree(B->d_Ainv); cudaFree(B->d_cids);
-  cudaFree(B->d_all); cudaFree(B->d_cbeg);
+  cudaFree(B->d_all); cudaFree(B->d_cbeg); cudaFree(B->d_pid);
   cudaFree(B->r); cudaFree(B->z); cudaFree(B->p); cudaFree(B->v); cudaFree(B->part);
   cudaFree(B->d_scal); cudaFree(B->d_active);
   if (B->h_active) cudaFreeHost(B->h_active);
@@ -456,10 +490,21 @@ mfgb_operator *union_shell(int degree, int64_t n_dofs) {
   return op;
 }
 
+void free_plan(Plan &P) {
+  if (!P.owns) return;
+  for (auto &D : P.depth) {
+    for (auto *op : D.groups) mfgb_operator_destroy(op);
+    for (auto &pg : D.pgroups) cudaFree(pg.map_c);
+  }
+  for (void *m : P.mem) cudaFree(m);
+  P = Plan();
+}
+
 // dst = A src on one depth (FP32, union operators + identity rows)
-mfgb_status apply32(const Depth &D, const float *src, float *dst, cudaStream_t s) {
+mfgb_status apply32(const Depth &V, const DepthPlan &D, const float *src, float *dst,
+                    cudaStream_t s) {
   mfgb_status st;
-  if ((st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(float) * D.n, s), "batch A32: dst = 0")))
+  if ((st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(float) * V.n, s), "batch A32: dst = 0")))
     return st;
   for (const mfgb_operator *op : D.groups)
     if ((st = cuda_status(bk5_f32(op->n, op->n_cells, op->d_map, op->d_G32, src, dst, op->D,
@@ -472,84 +517,249 @@ mfgb_status apply32(const Depth &D, const float *src, float *dst, cudaStream_t s
 }
 
 // dst = A src on depth 0 in FP64 (double-float union operators)
-mfgb_status apply64(const mfgb_batch *B, const double *src, double *dst, cudaStream_t s) {
-  const Depth &D = B->depth[0];
+mfgb_status apply64(const mfgb_batch *B, const Plan &P, const double *src, double *dst,
+                    cudaStream_t s) {
+  const DepthPlan &D = P.depth[0];
   mfgb_status st;
-  if ((st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * D.n, s), "batch A: dst = 0")))
+  if ((st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * B->depth[0].n, s),
+                        "batch A: dst = 0")))
     return st;
   for (mfgb_operator *op : D.groups)
     if ((st = apply_add_impl(op, dst, src, MFGB_ARITH_FP64_DF, s, nullptr))) return st;
   return cuda_status(copy_constrained(D.n_cons, D.d_cons, src, dst, s), "batch A constrained");
 }
 
-mfgb_status chebyshev_b(const mfgb_batch *B, const Depth &D, bool zero_start, cudaStream_t s) {
+mfgb_status chebyshev_b(const mfgb_batch *B, const Depth &V, const DepthPlan &D, bool zero_start,
+                        cudaStream_t s) {
   mfgb_status st;
   if (zero_start) {
-    kb_cheb_first_zero<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, D.b, D.inv_diag, D.x, D.d, D.r,
-                                                 D.d_coef, B->cs);
+    kb_cheb_first_zero<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, V.b, V.inv_diag, V.x, V.d, V.r,
+                                                 V.d_coef, B->cs);
   } else {
-    if ((st = apply32(D, D.x, D.t, s))) return st;
-    kb_cheb_first<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, D.b, D.t, D.inv_diag, D.x, D.d, D.r,
-                                            D.d_coef, B->cs);
+    if ((st = apply32(V, D, V.x, V.t, s))) return st;
+    kb_cheb_first<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, V.b, V.t, V.inv_diag, V.x, V.d, V.r,
+                                            V.d_coef, B->cs);
   }
   for (int j = 1; j < B->cheb_degree; ++j) {
-    if ((st = apply32(D, D.d, D.t, s))) return st;
-    kb_cheb_step<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, D.t, D.inv_diag, D.x, D.d, D.r, D.d_coef,
+    if ((st = apply32(V, D, V.d, V.t, s))) return st;
+    kb_cheb_step<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, V.t, V.inv_diag, V.x, V.d, V.r, V.d_coef,
                                            B->cs, j);
   }
   return cuda_status(cudaGetLastError(), "batch chebyshev");
 }
 
-// depth-0 x = V(b): descend every depth, all coarse solves, ascend
-mfgb_status vcycle_b(const mfgb_batch *B, cudaStream_t s) {
-  const size_t nd = B->depth.size();
+// depth-0 x = V(b): descend every depth the plan's problems reach, all coarse
+// solves, ascend
+mfgb_status vcycle_b(const mfgb_batch *B, const Plan &P, cudaStream_t s) {
+  size_t nd = 1;
+  for (size_t l = 0; l < P.depth.size(); ++l)
+    if (P.depth[l].n_cheb) nd = l + 2;  // depth l smooths, so depth l + 1 exists
+  nd = std::min(nd, P.depth.size());
   mfgb_status st;
   for (size_t l = 0; l + 1 < nd; ++l) {
-    const Depth &D = B->depth[l], &C = B->depth[l + 1];
-    if ((st = chebyshev_b(B, D, true, s))) return st;
-    if ((st = apply32(D, D.x, D.t, s))) return st;
-    kb_residual<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, D.b, D.t, D.r);
+    const Depth &V = B->depth[l], &C = B->depth[l + 1];
+    const DepthPlan &D = P.depth[l];
+    if (!D.n_cheb) continue;
+    if ((st = chebyshev_b(B, V, D, true, s))) return st;
+    if ((st = apply32(V, D, V.x, V.t, s))) return st;
+    kb_residual<<<D.n_cheb, T256, 0, s>>>(D.d_cheb, V.b, V.t, V.r);
     if ((st = cuda_status(cudaMemsetAsync(C.b, 0, sizeof(float) * C.n, s), "batch coarse b = 0")))
       return st;
     for (const PGroup &pg : D.pgroups) {
       const mfgb_operator *op = D.groups[pg.g];
       k_p_restrict_sf<float><<<(unsigned)std::min<int64_t>(op->n_cells, 152 * 16), 128, 0, s>>>(
-          op->n_cells, op->d_map, pg.map_c, D.r, D.inv_val, C.b, pg.P);
+          op->n_cells, op->d_map, pg.map_c, V.r, V.inv_val, C.b, pg.P);
     }
     if (D.n_hcoarse)
-      kb_h_restrict<<<D.n_hcoarse, T256, 0, s>>>(D.d_hcoarse, D.d_hp, D.r, C.b);
+      kb_h_restrict<<<D.n_hcoarse, T256, 0, s>>>(D.d_hcoarse, D.d_hp, V.r, C.b);
     if ((st = cuda_status(cudaGetLastError(), "batch restrict"))) return st;
   }
-  if (B->n_coarse)
-    kb_coarse<<<B->n_coarse, T256, B->coarse_smem, s>>>(B->d_coarse);
+  if (P.n_coarse)
+    kb_coarse<<<P.n_coarse, T256, P.coarse_smem, s>>>(P.d_coarse);
   if ((st = cuda_status(cudaGetLastError(), "batch coarse solves"))) return st;
   for (size_t l = nd - 1; l-- > 0;) {
-    const Depth &D = B->depth[l], &C = B->depth[l + 1];
+    const Depth &V = B->depth[l], &C = B->depth[l + 1];
+    const DepthPlan &D = P.depth[l];
+    if (!D.n_cheb) continue;
     if (!D.pgroups.empty()) {
-      if ((st = cuda_status(cudaMemsetAsync(D.t, 0, sizeof(float) * D.n, s), "batch t = 0")))
+      if ((st = cuda_status(cudaMemsetAsync(V.t, 0, sizeof(float) * V.n, s), "batch t = 0")))
         return st;
       for (const PGroup &pg : D.pgroups) {
         const mfgb_operator *op = D.groups[pg.g];
         k_p_prolongate_sf<float><<<(unsigned)std::min<int64_t>(op->n_cells, 152 * 16), 128, 0, s>>>(
-            op->n_cells, op->d_map, pg.map_c, C.x, D.t, pg.P);
+            op->n_cells, op->d_map, pg.map_c, C.x, V.t, pg.P);
       }
-      kb_add<<<D.n_pch, T256, 0, s>>>(D.d_pch, D.t, D.x);
+      kb_add<<<D.n_pch, T256, 0, s>>>(D.d_pch, V.t, V.x);
     }
-    if (D.n_hfine) kb_h_prolongate_add<<<D.n_hfine, T256, 0, s>>>(D.d_hfine, D.d_hp, C.x, D.x);
+    if (D.n_hfine) kb_h_prolongate_add<<<D.n_hfine, T256, 0, s>>>(D.d_hfine, D.d_hp, C.x, V.x);
     if ((st = cuda_status(cudaGetLastError(), "batch prolongate"))) return st;
-    if ((st = chebyshev_b(B, D, false, s))) return st;
+    if ((st = chebyshev_b(B, V, D, false, s))) return st;
   }
   return MFGB_OK;
 }
 
 // dst = M src (FP64 in and out)
-mfgb_status precondition_b(const mfgb_batch *B, double *dst, const double *src, cudaStream_t s) {
-  const Depth &D = B->depth[0];
-  k_convert<float, double><<<grid1d(D.n), T256, 0, s>>>(D.n, src, D.b);
-  mfgb_status st = vcycle_b(B, s);
+mfgb_status precondition_b(const mfgb_batch *B, const Plan &P, double *dst, const double *src,
+                           cudaStream_t s) {
+  const Depth &V = B->depth[0];
+  k_convert<float, double><<<grid1d(V.n), T256, 0, s>>>(V.n, src, V.b);
+  mfgb_status st = vcycle_b(B, P, s);
   if (st) return st;
-  k_convert<double, float><<<grid1d(D.n), T256, 0, s>>>(D.n, D.x, dst);
+  k_convert<double, float><<<grid1d(V.n), T256, 0, s>>>(V.n, V.x, dst);
   return cuda_status(cudaGetLastError(), "batch precondition");
+}
+
+// A plan for the problems with active[i] != 0, gathered from the full plan:
+// per part, contiguous segments of the union maps and geometric factors, of the
+// identity-row list and of the coarse p-transfer maps are copied; chunk and
+// transfer tables are rebuilt on the host.
+mfgb_status gather_plan(const mfgb_batch *B, const std::vector<char> &active, Plan &out,
+                        cudaStream_t s) {
+  Plan P;
+  P.owns = true;
+  auto track = [&](void *m) { if (m) P.mem.push_back(m); };
+  mfgb_status st = MFGB_OK;
+  auto fail = [&](mfgb_status e) { free_plan(P); return e; };
+  const size_t nd = B->depth.size();
+  P.depth.resize(nd);
+  // index of each problem's part per depth
+  std::vector<std::vector<int>> part_at(B->n_problems, std::vector<int>(nd, -1));
+  for (size_t l = 0; l < nd; ++l)
+    for (size_t k = 0; k < B->depth[l].parts.size(); ++k)
+      part_at[B->depth[l].parts[k].problem][l] = (int)k;
+  for (size_t l = 0; l < nd; ++l) {
+    const Depth &V = B->depth[l];
+    const DepthPlan &F = B->full.depth[l];
+    DepthPlan &D = P.depth[l];
+    std::map<int, int> gidx;
+    std::vector<int64_t> gcells;
+    std::vector<std::vector<int>> gparts;
+    int64_t n_cons = 0;
+    for (size_t k = 0; k < V.parts.size(); ++k) {
+      const Part &Q = V.parts[k];
+      if (!active[Q.problem] || Q.group < 0) continue;
+      auto it = gidx.find(Q.degree);
+      if (it == gidx.end()) {
+        it = gidx.emplace(Q.degree, (int)D.groups.size()).first;
+        D.groups.push_back(union_shell(Q.degree, V.n));
+        gcells.push_back(0);
+        gparts.emplace_back();
+      }
+      gcells[it->second] += Q.n_cells;
+      gparts[it->second].push_back((int)k);
+      n_cons += Q.n_constrained;
+    }
+    int64_t *cons = nullptr;
+    if ((st = dalloc((void **)&cons, sizeof(int64_t) * n_cons))) return fail(st);
+    track(cons);
+    D.d_cons = cons;
+    D.n_cons = n_cons;
+    int64_t cpos = 0;
+    for (size_t g = 0; g < D.groups.size(); ++g) {
+      mfgb_operator *op = D.groups[g];
+      op->n_cells = gcells[g];
+      const int64_t n3 = (int64_t)op->n * op->n * op->n;
+      if ((st = dalloc((void **)&op->d_map, sizeof(uint32_t) * op->n_cells * n3)) ||
+          (st = dalloc((void **)&op->d_G32, sizeof(float) * op->n_cells * 6 * n3)) ||
+          (l == 0 && (st = dalloc((void **)&op->d_Gdf, sizeof(float2) * op->n_cells * 6 * n3))))
+        return fail(st);
+      int64_t c0 = 0;
+      for (int k : gparts[g]) {
+        const Part &Q = V.parts[k];
+        const mfgb_operator *src = F.groups[Q.group];
+        cudaMemcpyAsync(op->d_map + c0 * n3, src->d_map + Q.cell_off * n3,
+                        sizeof(uint32_t) * Q.n_cells * n3, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(op->d_G32 + c0 * 6 * n3, src->d_G32 + Q.cell_off * 6 * n3,
+                        sizeof(float) * Q.n_cells * 6 * n3, cudaMemcpyDeviceToDevice, s);
+        if (l == 0)
+          cudaMemcpyAsync(op->d_Gdf + c0 * 6 * n3, src->d_Gdf + Q.cell_off * 6 * n3,
+                          sizeof(float2) * Q.n_cells * 6 * n3, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(cons + cpos, F.d_cons + Q.cons_off, sizeof(int64_t) * Q.n_constrained,
+                        cudaMemcpyDeviceToDevice, s);
+        cpos += Q.n_constrained;
+        c0 += Q.n_cells;
+      }
+      // p-transfer group of this degree (same cells, same order)
+      const PGroup *fpg = nullptr;
+      for (const PGroup &q : F.pgroups)
+        if (F.groups[q.g]->degree == op->degree) fpg = &q;
+      if (fpg) {
+        PGroup pg;
+        pg.g = (int)g;
+        pg.P = fpg->P;
+        const int64_t nc3 = (int64_t)fpg->P.nc * fpg->P.nc * fpg->P.nc;
+        if ((st = dalloc((void **)&pg.map_c, sizeof(uint32_t) * op->n_cells * nc3))) {
+          return fail(st);
+        }
+        int64_t cc = 0;
+        for (int k : gparts[g]) {
+          const Part &Q = V.parts[k];
+          cudaMemcpyAsync(pg.map_c + cc * nc3, fpg->map_c + Q.cell_off * nc3,
+                          sizeof(uint32_t) * Q.n_cells * nc3, cudaMemcpyDeviceToDevice, s);
+          cc += Q.n_cells;
+        }
+        D.pgroups.push_back(pg);
+      }
+    }
+    // chunk and h-transfer tables
+    std::vector<Chunk> cheb, pch, hfine, hcoarse;
+    std::vector<HPart> hp;
+    for (size_t k = 0; k < V.parts.size(); ++k) {
+      const Part &Q = V.parts[k];
+      if (!active[Q.problem] || Q.kind == 0) continue;
+      append_chunks(cheb, Q.off, Q.n, (int)k);
+      if (Q.kind == 1) append_chunks(pch, Q.off, Q.n, (int)k);
+      if (Q.kind == 2) {
+        const Part &R = B->depth[l + 1].parts[part_at[Q.problem][l + 1]];
+        append_chunks(hfine, Q.off, Q.n, (int)hp.size());
+        append_chunks(hcoarse, R.off, R.n, (int)hp.size());
+        hp.push_back(HPart{hgrid(Q.box, Q.bs, R.box), Q.off, R.off});
+      }
+    }
+    Chunk *c1 = nullptr, *c2 = nullptr, *c3 = nullptr, *c4 = nullptr;
+    HPart *h1 = nullptr;
+    if ((st = upload(&c1, cheb)) || (st = upload(&c2, pch)) || (st = upload(&c3, hfine)) ||
+        (st = upload(&c4, hcoarse)) || (st = upload(&h1, hp)))
+      return fail(st);
+    track(c1); track(c2); track(c3); track(c4); track(h1);
+    D.d_cheb = c1; D.n_cheb = (int)cheb.size();
+    D.d_pch = c2; D.n_pch = (int)pch.size();
+    D.d_hfine = c3; D.n_hfine = (int)hfine.size();
+    D.d_hcoarse = c4; D.n_hcoarse = (int)hcoarse.size();
+    D.d_hp = h1;
+  }
+  // coarse solves, outer CG tables
+  std::vector<CoarseDesc> cd;
+  std::vector<Chunk> all;
+  std::vector<int> cbeg, pid;
+  for (int i = 0; i < B->n_problems; ++i) {
+    if (!active[i]) continue;
+    cd.push_back(B->coarse_host[i]);
+    const Part &Q = B->depth[0].parts[part_at[i][0]];
+    cbeg.push_back((int)all.size());
+    pid.push_back(i);
+    append_chunks(all, Q.off, Q.n, part_at[i][0]);
+    P.dofs += Q.n;
+  }
+  cbeg.push_back((int)all.size());
+  CoarseDesc *dcd = nullptr;
+  Chunk *dall = nullptr;
+  int *dcb = nullptr, *dpid = nullptr;
+  if ((st = upload(&dcd, cd)) || (st = upload(&dall, all)) || (st = upload(&dcb, cbeg)) ||
+      (st = upload(&dpid, pid)))
+    return fail(st);
+  track(dcd); track(dall); track(dcb); track(dpid);
+  P.d_coarse = dcd;
+  P.n_coarse = (int)cd.size();
+  P.coarse_smem = B->full.coarse_smem;
+  P.d_all = dall;
+  P.n_all = (int)all.size();
+  P.d_cbeg = dcb;
+  P.d_pid = dpid;
+  P.n_prob = (int)pid.size();
+  if ((st = cuda_status(cudaStreamSynchronize(s), "batch plan"))) return fail(st);
+  out = P;
+  return MFGB_OK;
 }
 
 mfgb_status check_params(const mfgb_box_desc *boxes, int n, const mfgb_mg_params *prm) {
@@ -839,6 +1049,38 @@ mfgb_status build_batch(mfgb_batch *B, const mfgb_box_desc *boxes, int n,
   B->n_coarse = (int)cd.size();
   B->coarse_smem = (int)(sizeof(double) * std::max(1, max_nc));
   if ((st = upload(&B->d_coarse, cd))) return st;
+  B->coarse_host.assign(n, CoarseDesc{});
+  for (size_t k = 0; k < coarse_h.size(); ++k)
+    B->coarse_host[B->depth[coarse_h[k].depth].parts[coarse_h[k].part].problem] = cd[k];
+  // the full plan views the arrays above
+  Plan &F = B->full;
+  F.depth.resize(B->depth.size());
+  for (size_t l = 0; l < B->depth.size(); ++l) {
+    const Depth &D = B->depth[l];
+    DepthPlan &P = F.depth[l];
+    P.groups = D.groups;
+    P.d_cons = D.d_cons;
+    P.n_cons = D.n_cons;
+    P.d_cheb = D.d_cheb; P.n_cheb = D.n_cheb;
+    P.d_pch = D.d_pch; P.n_pch = D.n_pch;
+    P.d_hfine = D.d_hfine; P.n_hfine = D.n_hfine;
+    P.d_hcoarse = D.d_hcoarse; P.n_hcoarse = D.n_hcoarse;
+    P.d_hp = D.d_hp;
+    P.pgroups = D.pgroups;
+  }
+  std::vector<int> pid(n);
+  for (int i = 0; i < n; ++i) pid[i] = i;
+  if ((st = upload(&B->d_pid, pid))) return st;
+  F.d_coarse = B->d_coarse;
+  F.n_coarse = B->n_coarse;
+  F.coarse_smem = B->coarse_smem;
+  F.d_all = B->d_all;
+  F.n_all = B->n_all;
+  F.d_cbeg = B->d_cbeg;
+  F.d_pid = B->d_pid;
+  F.n_prob = n;
+  F.dofs = B->depth[0].n;
+  F.owns = false;
   return cuda_status(cudaDeviceSynchronize(), "batch set-up");
 }
 
@@ -946,12 +1188,21 @@ mfgb_status mfgb_batch_rhs_uniform(const mfgb_batch *B, const uint64_t *h_seeds,
   return cuda_status(cudaStreamSynchronize(s), "batch rhs");
 }
 
+mfgb_status mfgb_batch_last_solve_stats(const mfgb_batch *B, int *n_replans) {
+  if (!B || !n_replans) {
+    set_error("mfgb_batch_last_solve_stats: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  *n_replans = B->last_replans;
+  return MFGB_OK;
+}
+
 mfgb_status mfgb_batch_vmult(mfgb_batch *B, double *d_dst, const double *d_src, void *stream) {
   if (!B || !d_dst || !d_src || d_dst == d_src) {
     set_error("mfgb_batch_vmult: invalid argument");
     return MFGB_ERR_INVALID_ARG;
   }
-  return apply64(B, d_src, d_dst, (cudaStream_t)stream);
+  return apply64(B, B->full, d_src, d_dst, (cudaStream_t)stream);
 }
 
 mfgb_status mfgb_batch_precondition(mfgb_batch *B, double *d_dst, const double *d_src,
@@ -960,12 +1211,15 @@ mfgb_status mfgb_batch_precondition(mfgb_batch *B, double *d_dst, const double *
     set_error("mfgb_batch_precondition: invalid argument");
     return MFGB_ERR_INVALID_ARG;
   }
-  return precondition_b(B, d_dst, d_src, (cudaStream_t)stream);
+  return precondition_b(B, B->full, d_dst, d_src, (cudaStream_t)stream);
 }
 
 // FP64 CG on every problem at once (deal.II SolverCG / ReductionControl per
 // problem: tol_eff = max(tol, reduce |r0|)), the batched V-cycle as the
-// preconditioner; one iteration of the batch = one CUDA graph launch.
+// preconditioner; one iteration of the batch = one CUDA graph launch.  When the
+// problems still running hold at most 60 % of the current plan's DoFs, the
+// plan is gathered again for them and the graph re-captured, so converged
+// problems stop costing operator and V-cycle work.
 mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
                                 const mfgb_cg_control *ctl, mfgb_solve_info *h_info,
                                 void *stream) {
@@ -979,45 +1233,51 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
   struct J { cudaStream_t s; void *o; ~J() { join_stream(s, o); } } join{s, stream};
   const int np = B->n_problems;
   const unsigned gp = (unsigned)((np + 127) / 128);
+  const Plan &F = B->full;
   // r = b - A x; |r0|; z = M r; p = z; rz
-  if ((st = apply64(B, d_x, B->v, s))) return st;
-  kb_residual64<<<B->n_all, T256, 0, s>>>(B->d_all, d_b, B->v, B->r);
-  kb_dot<<<B->n_all, T256, 0, s>>>(B->d_all, B->r, B->r, B->part);
-  kb_init<<<np, T256, 0, s>>>(B->d_cbeg, B->part, B->d_scal, ctl->tol, ctl->reduce);
-  if ((st = precondition_b(B, B->z, B->r, s))) return st;
-  kb_copy64<<<B->n_all, T256, 0, s>>>(B->d_all, B->z, B->p);
-  kb_dot<<<B->n_all, T256, 0, s>>>(B->d_all, B->r, B->z, B->part);
-  kb_sum_rz<<<np, T256, 0, s>>>(B->d_cbeg, B->part, B->d_scal);
+  if ((st = apply64(B, F, d_x, B->v, s))) return st;
+  kb_residual64<<<F.n_all, T256, 0, s>>>(F.d_all, d_b, B->v, B->r);
+  kb_dot<<<F.n_all, T256, 0, s>>>(F.d_all, B->r, B->r, B->part);
+  kb_init<<<np, T256, 0, s>>>(F.d_cbeg, F.d_pid, B->part, B->d_scal, ctl->tol, ctl->reduce);
+  if ((st = precondition_b(B, F, B->z, B->r, s))) return st;
+  kb_copy64<<<F.n_all, T256, 0, s>>>(F.d_all, B->z, B->p);
+  kb_dot<<<F.n_all, T256, 0, s>>>(F.d_all, B->r, B->z, B->part);
+  kb_sum_rz<<<np, T256, 0, s>>>(F.d_cbeg, F.d_pid, B->part, B->d_scal);
   kb_init_rz<<<gp, 128, 0, s>>>(np, B->d_scal);
   if ((st = cuda_status(cudaGetLastError(), "batch cg init"))) return st;
   std::vector<BScal> hs(np);
-  if ((st = cuda_status(cudaMemcpyAsync(hs.data(), B->d_scal, sizeof(BScal) * np,
-                                        cudaMemcpyDeviceToHost, s),
-                        "batch cg init")) ||
-      (st = cuda_status(cudaStreamSynchronize(s), "batch cg init")))
-    return st;
+  auto read_scalars = [&]() {
+    mfgb_status e = cuda_status(cudaMemcpyAsync(hs.data(), B->d_scal, sizeof(BScal) * np,
+                                                cudaMemcpyDeviceToHost, s),
+                                "batch cg scalars");
+    if (!e) e = cuda_status(cudaStreamSynchronize(s), "batch cg scalars");
+    return e;
+  };
+  if ((st = read_scalars())) return st;
   int running = 0;
   for (const BScal &q : hs) running += q.done == 0;
-  // one iteration as a graph
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  if (running > 0 && ctl->max_steps > 0) {
-    if ((st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture")))
-      return st;
-    mfgb_status cap = apply64(B, B->p, B->v, s);
+
+  // one iteration of the plan's problems as a graph
+  auto capture = [&](const Plan &P, cudaGraphExec_t *exec) -> mfgb_status {
+    cudaGraph_t graph = nullptr;
+    mfgb_status e;
+    if ((e = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture")))
+      return e;
+    const int nb = P.n_prob;
+    mfgb_status cap = apply64(B, P, B->p, B->v, s);
     if (!cap) {
-      kb_dot<<<B->n_all, T256, 0, s>>>(B->d_all, B->p, B->v, B->part);
-      kb_sum_pap<<<np, T256, 0, s>>>(B->d_cbeg, B->part, B->d_scal);
-      kb_update<<<B->n_all, T256, 0, s>>>(B->d_all, d_x, B->r, B->p, B->v, B->d_scal, B->part);
+      kb_dot<<<P.n_all, T256, 0, s>>>(P.d_all, B->p, B->v, B->part);
+      kb_sum_pap<<<nb, T256, 0, s>>>(P.d_cbeg, P.d_pid, B->part, B->d_scal);
+      kb_update<<<P.n_all, T256, 0, s>>>(P.d_all, d_x, B->r, B->p, B->v, B->d_scal, B->part);
       cudaMemsetAsync(B->d_active, 0, sizeof(int), s);
-      kb_sum_check<<<np, T256, 0, s>>>(B->d_cbeg, B->part, B->d_scal, ctl->max_steps,
+      kb_sum_check<<<nb, T256, 0, s>>>(P.d_cbeg, P.d_pid, B->part, B->d_scal, ctl->max_steps,
                                        B->d_active);
-      cap = precondition_b(B, B->z, B->r, s);
+      cap = precondition_b(B, P, B->z, B->r, s);
     }
     if (!cap) {
-      kb_dot<<<B->n_all, T256, 0, s>>>(B->d_all, B->r, B->z, B->part);
-      kb_sum_rz<<<np, T256, 0, s>>>(B->d_cbeg, B->part, B->d_scal);
-      kb_direction<<<B->n_all, T256, 0, s>>>(B->d_all, B->z, B->p, B->d_scal);
+      kb_dot<<<P.n_all, T256, 0, s>>>(P.d_all, B->r, B->z, B->part);
+      kb_sum_rz<<<nb, T256, 0, s>>>(P.d_cbeg, P.d_pid, B->part, B->d_scal);
+      kb_direction<<<P.n_all, T256, 0, s>>>(P.d_all, B->z, B->p, B->d_scal);
       kb_roll<<<gp, 128, 0, s>>>(np, B->d_scal);
       cudaMemcpyAsync(B->h_active, B->d_active, sizeof(int), cudaMemcpyDeviceToHost, s);
     }
@@ -1026,11 +1286,19 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
       if (graph) cudaGraphDestroy(graph);
       return cap;
     }
-    if ((st = cuda_status(ce, "end capture"))) return st;
-    if ((st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "instantiate"))) {
-      cudaGraphDestroy(graph);
-      return st;
-    }
+    if ((e = cuda_status(ce, "end capture"))) return e;
+    e = cuda_status(cudaGraphInstantiate(exec, graph, 0), "instantiate");
+    cudaGraphDestroy(graph);
+    return e;
+  };
+
+  Plan sub;  // the gathered plan in use (owns its arrays), when not the full one
+  struct FreeSub { Plan *p; ~FreeSub() { free_plan(*p); } } free_sub{&sub};
+  const Plan *cur = &F;
+  B->last_replans = 0;
+  if (running > 0 && ctl->max_steps > 0) {
+    cudaGraphExec_t exec = nullptr;
+    if ((st = capture(*cur, &exec))) return st;
     for (int it = 0; it < ctl->max_steps; ++it) {
       cudaError_t e = cudaGraphLaunch(exec, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -1039,16 +1307,31 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
         break;
       }
       if (*B->h_active == 0) break;
+      // re-plan for the running problems once they hold <= 60 % of the plan's DoFs
+      if ((st = read_scalars())) break;
+      std::vector<char> active(np, 0);
+      int64_t dofs = 0;
+      for (int i = 0; i < np; ++i)
+        if (!hs[i].done) {
+          active[i] = 1;
+          dofs += B->depth[0].parts[i].n;
+        }
+      if (dofs <= 0.6 * (double)cur->dofs) {
+        Plan next;
+        if ((st = gather_plan(B, active, next, s))) break;
+        cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        free_plan(sub);
+        sub = next;
+        cur = &sub;
+        ++B->last_replans;
+        if ((st = capture(*cur, &exec))) break;
+      }
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
+    if (exec) cudaGraphExecDestroy(exec);
     if (st) return st;
   }
-  if ((st = cuda_status(cudaMemcpyAsync(hs.data(), B->d_scal, sizeof(BScal) * np,
-                                        cudaMemcpyDeviceToHost, s),
-                        "batch cg result")) ||
-      (st = cuda_status(cudaStreamSynchronize(s), "batch cg result")))
-    return st;
+  if ((st = read_scalars())) return st;
   if ((st = mfgb_check_device_errors(s))) return st;
   int failed = 0, nonfinite = 0;
   for (int i = 0; i < np; ++i) {

@@ -290,9 +290,14 @@ mfgb_status mfgb_batch_vmult(mfgb_batch *batch, double *d_dst, const double *d_s
 mfgb_status mfgb_batch_precondition(mfgb_batch *batch, double *d_dst, const double *d_src,
                                     void *stream);
 /* solves A_i x_i = b_i for every problem; h_info has n_problems entries.
-   MFGB_ERR_NOT_CONVERGED if any problem reached max_steps (infos filled). */
+   MFGB_ERR_NOT_CONVERGED if any problem reached max_steps (infos filled).
+   Once the problems still running hold at most 60 % of the DoFs of the current
+   launch plan, the union operators and tables are gathered again for them
+   (converged problems stop costing work). */
 mfgb_status mfgb_batch_cg_solve(mfgb_batch *batch, const double *d_b, double *d_x,
                                 const mfgb_cg_control *ctl, mfgb_solve_info *h_info, void *stream);
+/* number of launch plans gathered during the last mfgb_batch_cg_solve */
+mfgb_status mfgb_batch_last_solve_stats(const mfgb_batch *batch, int *n_replans);
 
 /* ---- learned part: features, targets, MLP (no counterpart in the reference)
  * features: per cell, dx/dxi at the 8 corner nodes (72 values, scaled by

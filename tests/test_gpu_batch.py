@@ -106,6 +106,7 @@ def test_solve_matches_single_solves(mf, orc, batch):
         assert abs(info["steps"] - ctl.last_step()) <= 1, (i, info, ctl.last_step())
         assert rel(B.split(x)[i].cpu().numpy(), xi.cpu().numpy()) <= 1e-9
     assert B.infos[6]["steps"] == 1  # exact coarse solve as the preconditioner
+    assert B.replans >= 1  # converged problems were dropped from the launches
     # the residual of a solution, checked by the CPU oracle
     m = meshes[2]
     ref = orc.BoxProblem(m.nx, m.ny, m.nz, m.degree, amplitude=m.amplitude)
