@@ -259,26 +259,26 @@ def run_ours(args, rank, world):
     e2e_ms = float("nan")
     if args.no_e2e:
         return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk)
+    # (mfgb_vmult_host: the H2D copy of src, the apply and the D2H copy of dst,
+    # pipelined over slabs of cells inside the library call)
     h_src = src.cpu().pin_memory()
     h_dst = torch.empty_like(h_src).pin_memory()
-    d_a, d_b = A.initialize_dof_vector(), A.initialize_dof_vector()
-    for _ in range(2):
-        d_a.copy_(h_src, non_blocking=True)
-        A.vmult(d_b, d_a)
-        h_dst.copy_(d_b, non_blocking=True)
+    for _ in range(3):
+        A.vmult_host(h_dst, h_src)
     torch.cuda.synchronize()
     e_steps = max(3, min(args.steps, 20))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(e_steps):
-        d_a.copy_(h_src, non_blocking=True)
-        A.vmult(d_b, d_a)
-        h_dst.copy_(d_b, non_blocking=True)
+        A.vmult_host(h_dst, h_src)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e_steps, world)
-    # correctness guard on the timed result
-    assert torch.equal(h_dst.cuda(), d_b)
+    # correctness guard on the timed result: the device apply of the same src
+    A.vmult(dst, src)
+    torch.cuda.synchronize()
+    err = float(torch.linalg.norm(h_dst.cuda() - dst) / torch.linalg.norm(dst))
+    assert err <= 1e-14, err
     return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk)
 
 
@@ -320,7 +320,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
                      "fp64_equiv_tflops": flops / (kernel_ms * 1e-3) / 1e12},
         "e2e": {"value": world * n / (e2e_ms * 1e-3) / 1e9, "unit": "GDoF/s",
                 "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
-                "ms_per_step": e2e_ms},
+                "ms_per_step": e2e_ms, "call": "mfgb_vmult_host (pinned host vectors)"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }

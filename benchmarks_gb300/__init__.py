@@ -182,6 +182,19 @@ class LaplaceOperator:
         self._inv_diag = DiagonalMatrix(inv)
         return d
 
+    def vmult_host(self, dst, src, arith=None):
+        """dst = A src on host (CPU, ideally pinned) float64 tensors; the copies
+        are pipelined with the apply (``mfgb_vmult_host``)."""
+        for v, name in ((dst, "dst"), (src, "src")):
+            if v.is_cuda or v.dtype != _torch().float64 or not v.is_contiguous() or \
+                    v.numel() != self._n_dofs:
+                raise ValueError(f"{name}: contiguous float64 host tensor of {self._n_dofs} entries")
+        _abi.check(lib().mfgb_vmult_host(self._op, ctypes.c_void_p(dst.data_ptr()),
+                                         ctypes.c_void_p(src.data_ptr()),
+                                         self.arith if arith is None else _arith(arith),
+                                         _stream_ptr()))
+        return dst
+
     def get_matrix_diagonal_inverse(self):
         if self._inv_diag is None:
             self.compute_diagonal()

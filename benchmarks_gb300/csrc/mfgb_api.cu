@@ -1,4 +1,5 @@
 // mfgb_api.cu -- C ABI: operator set-up, vmult, kernel seams, diagonal, RHS.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -140,6 +141,25 @@ mfgb_status apply_add_impl(mfgb_operator *op, double *dst, const double *src, in
   return cuda_status(e, "apply: bk5 kernel");
 }
 
+// dst += A src over cells [cell0, cell0 + n): the map keeps global DoF indices
+static cudaError_t apply_cells(mfgb_operator *op, int64_t cell0, int64_t n, double *dst,
+                               const double *src, int arith, cudaStream_t s) {
+  const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  const uint32_t *map = op->d_map + cell0 * n3;
+  if (arith == MFGB_ARITH_FP64)
+    return op->quadrature
+               ? bk5g_f64(op->n, n, map, op->d_G + cell0 * 6 * n3, src, dst, op->DG, op->Bq,
+                          nullptr, nullptr, s, nullptr, op->d_JxW ? op->d_JxW + cell0 * n3 : nullptr)
+               : bk5_f64(op->n, n, map, op->d_G + cell0 * 6 * n3, src, dst, op->D, nullptr,
+                         nullptr, s);
+  return op->quadrature
+             ? bk5g_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->DG, op->Bq,
+                       nullptr, nullptr, s, nullptr,
+                       op->d_JxWdf ? op->d_JxWdf + cell0 * n3 : nullptr)
+             : bk5_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->D, nullptr, nullptr,
+                      s);
+}
+
 static void free_operator(mfgb_operator *op) {
   if (!op) return;
   cudaFree(op->d_map);
@@ -150,6 +170,11 @@ static void free_operator(mfgb_operator *op) {
   cudaFree(op->d_partials);
   cudaFree(op->d_JxW);
   cudaFree(op->d_JxWdf);
+  cudaFree(op->d_hsrc);
+  cudaFree(op->d_hdst);
+  for (cudaStream_t st : op->pipe)
+    if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t e : op->pipe_ev) cudaEventDestroy(e);
   delete op;
 }
 
@@ -287,6 +312,7 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
       }
     }
   op->n_constrained = (int64_t)cons.size();
+  op->h_constrained = cons;
   mfgb_status st;
   if ((st = dev_alloc((void **)&op->d_map, sizeof(uint32_t) * op->n_cells * n3, "dof map")) ||
       (st = dev_alloc((void **)&op->d_G, sizeof(double) * op->n_cells * 6 * n3, "G")) ||
@@ -509,6 +535,99 @@ mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, 
     return MFGB_ERR_INVALID_ARG;
   }
   return cuda_status(e, "mfgb_bk5_evector");
+}
+
+// vmult on host vectors, pipelined over z-slabs of cells on three streams:
+// H2D of the DoF planes a slab adds -> the slab's cells -> D2H of the planes it
+// completes (identity rows applied), while the next slab's planes arrive.
+// Slab k covers cell layers [z0, z1) and DoF planes p z0 .. p z1; plane p z1 is
+// shared with slab k + 1, so it is finished (and copied back) by slab k + 1.
+mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const double *h_src, int arith,
+                            void *stream) {
+  if (!cop || (cop->n_dofs > 0 && (!h_dst || !h_src)) || h_dst == h_src ||
+      (arith != MFGB_ARITH_FP64 && arith != MFGB_ARITH_FP64_DF)) {
+    set_error("mfgb_vmult_host: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  mfgb_operator *op = const_cast<mfgb_operator *>(cop);
+  if (op->n_dofs == 0) return MFGB_OK;
+  mfgb_status st;
+  if (arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if (!op->d_hsrc) {
+    if ((st = dev_alloc((void **)&op->d_hsrc, sizeof(double) * op->n_dofs, "host apply src")) ||
+        (st = dev_alloc((void **)&op->d_hdst, sizeof(double) * op->n_dofs, "host apply dst")))
+      return st;
+  }
+  if (!op->pipe[0])
+    for (auto &ps : op->pipe)
+      if (cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) != cudaSuccess)
+        return cuda_status(cudaErrorUnknown, "mfgb_vmult_host: streams");
+  const int p = op->degree;
+  const int nz = op->is_box ? op->box.nz : 1;
+  const int S = op->is_box ? std::min(nz, 8) : 1;
+  const int Lz = (nz + S - 1) / S;
+  const int n_ev = 3 * S + 1;
+  while ((int)op->pipe_ev.size() < n_ev) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      return cuda_status(cudaErrorUnknown, "mfgb_vmult_host: events");
+    op->pipe_ev.push_back(e);
+  }
+  cudaStream_t s = (cudaStream_t)stream, s_in = op->pipe[0], s_c = op->pipe[1], s_out = op->pipe[2];
+  cudaEvent_t *ev = op->pipe_ev.data();
+  // everything after the caller's prior work on its stream
+  cudaEventRecord(ev[0], s);
+  cudaStreamWaitEvent(s_in, ev[0], 0);
+  cudaStreamWaitEvent(s_c, ev[0], 0);
+  cudaStreamWaitEvent(s_out, ev[0], 0);
+  int64_t plane = op->n_dofs, cells_per_layer = op->n_cells;
+  if (op->is_box) {
+    plane = ((int64_t)p * op->box.nx + 1) * ((int64_t)p * op->box.ny + 1);
+    cells_per_layer = (int64_t)op->box.nx * op->box.ny;
+  }
+  const int64_t *hc = op->h_constrained.data();
+  const int64_t nhc = (int64_t)op->h_constrained.size();
+  int last_out = -1;
+  for (int k = 0, z0 = 0; z0 < nz; ++k, z0 += Lz) {
+    const int z1 = std::min(nz, z0 + Lz);
+    const bool last = z1 == nz;
+    // DoFs [a, b) this slab adds; [c0, c1) it completes
+    int64_t a, b, c0, c1;
+    if (op->is_box) {
+      a = (k == 0 ? 0 : ((int64_t)p * z0 + 1)) * plane;
+      b = ((int64_t)p * z1 + 1) * plane;
+      c0 = (int64_t)p * z0 * plane;
+      c1 = last ? op->n_dofs : (int64_t)p * z1 * plane;
+    } else {
+      a = 0; b = op->n_dofs; c0 = 0; c1 = op->n_dofs;
+    }
+    cudaMemcpyAsync(op->d_hsrc + a, h_src + a, sizeof(double) * (b - a), cudaMemcpyHostToDevice,
+                    s_in);
+    cudaEventRecord(ev[1 + 3 * k], s_in);
+    cudaStreamWaitEvent(s_c, ev[1 + 3 * k], 0);
+    cudaMemsetAsync(op->d_hdst + a, 0, sizeof(double) * (b - a), s_c);
+    const int64_t cell0 = (int64_t)z0 * cells_per_layer, ncell = (int64_t)(z1 - z0) * cells_per_layer;
+    if ((st = cuda_status(apply_cells(op, op->is_box ? cell0 : 0, op->is_box ? ncell : op->n_cells,
+                                      op->d_hdst, op->d_hsrc, arith, s_c),
+                          "mfgb_vmult_host: kernel")))
+      return st;
+    // identity rows among the completed DoFs (the list is ascending)
+    const int64_t i0 = op->is_box ? std::lower_bound(hc, hc + nhc, c0) - hc : 0;
+    const int64_t i1 = op->is_box ? std::lower_bound(hc, hc + nhc, c1) - hc : op->n_constrained;
+    if (i1 > i0 &&
+        (st = cuda_status(copy_constrained(i1 - i0, op->d_constrained + i0, op->d_hsrc, op->d_hdst,
+                                           s_c),
+                          "mfgb_vmult_host: constrained rows")))
+      return st;
+    cudaEventRecord(ev[2 + 3 * k], s_c);
+    cudaStreamWaitEvent(s_out, ev[2 + 3 * k], 0);
+    cudaMemcpyAsync(h_dst + c0, op->d_hdst + c0, sizeof(double) * (c1 - c0),
+                    cudaMemcpyDeviceToHost, s_out);
+    cudaEventRecord(ev[3 + 3 * k], s_out);
+    last_out = 3 + 3 * k;
+  }
+  cudaStreamWaitEvent(s, ev[last_out], 0);
+  return cuda_status(cudaGetLastError(), "mfgb_vmult_host");
 }
 
 mfgb_status mfgb_compute_diagonal(const mfgb_operator *op, double *d_diag, void *stream) {

@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <string>
 
+#include <vector>
+
 #include "mfgb.h"
 
 struct mfgb_operator {
@@ -27,6 +29,12 @@ struct mfgb_operator {
   // workspace for reductions (per-CTA partials)
   double *d_partials = nullptr;
   int partials_cap = 0;
+  // host-buffer apply (mfgb_vmult_host): device copies of the vectors, the
+  // constrained rows on the host (ascending), streams and events of the pipeline
+  double *d_hsrc = nullptr, *d_hdst = nullptr;
+  std::vector<int64_t> h_constrained;
+  cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> pipe_ev;
 };
 
 namespace mfgb {

@@ -188,6 +188,17 @@ mfgb_status mfgb_bk3_evector(int degree, int64_t nelmt, const double *d_basis,
                              const double *d_dbasis, const double *d_G, const double *d_in,
                              double *d_out, int arith, void *stream);
 
+/* vmult on HOST vectors (the call a CPU-side caller of the reference makes):
+   h_dst = A h_src with the copies inside the call.  On box operators the apply
+   is pipelined over z-slabs of cells: the DoF planes a slab needs go up, its
+   cells are applied, and the planes it completes come back while the next
+   slab's planes arrive (three streams, ordered after prior work on `stream`;
+   `stream` waits for the result).  Pinned host buffers are needed for the copies
+   to overlap (pageable ones are copied synchronously by CUDA).  The operator
+   keeps two device vectors for this call after the first use. */
+mfgb_status mfgb_vmult_host(const mfgb_operator *op, double *h_dst, const double *h_src, int arith,
+                            void *stream);
+
 /* ---- diagonal -------------------------------------------------------------
  * compute_diagonal (bp5_kokkos/benchmark.cc:218-251): exact diagonal of the
  * operator (1 on constrained rows), then d -> (d > 0 ? 1/d : 1). */

@@ -292,3 +292,38 @@ def test_autotune_small(mf, tmp_path):
     autotune.save(r, path)
     r2 = autotune.load(path, apply=False)
     assert r2["df"]["3"]["best"] == r["df"][3]["best"]
+
+
+@pytest.mark.parametrize("arith", ["df", "fp64"])
+@pytest.mark.parametrize("form", ["gll", "gauss", "helmholtz"])
+def test_vmult_host_pipeline(mf, orc, form, arith):
+    """The host-buffer apply (slab-pipelined copies) equals the device vmult, with
+    the identity rows copied exactly, for several slab layouts and repeated calls."""
+    import torch
+    for cells in ((3, 2, 9), (2, 3, 1), (4, 4, 16)):
+        A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=3, amplitude=0.06), arith=arith,
+                               quadrature=form)
+        src = torch.from_numpy(np.random.default_rng(sum(cells)).uniform(-1, 1, A.m()))
+        h_src = src.pin_memory()
+        h_dst = torch.empty_like(h_src).pin_memory()
+        want = A.initialize_dof_vector()
+        A.vmult(want, src.cuda())
+        for _ in range(2):
+            h_dst.fill_(float("nan"))
+            A.vmult_host(h_dst, h_src)
+            torch.cuda.synchronize()
+            assert rel(h_dst.numpy(), want.cpu().numpy()) <= 1e-14
+        cons = orc.BoxProblem(*cells, 3).constrained
+        assert np.array_equal(h_dst.numpy()[cons], src.numpy()[cons])
+
+
+def test_vmult_host_array_operator(mf, orc):
+    import torch
+    ref = orc.BoxProblem(3, 2, 2, 2, amplitude=0.05)
+    A = mf.LaplaceOperator(degree=2, n_dofs=ref.n_dofs, dof_map=ref.map, G=ref.G,
+                           constrained=ref.constrained)
+    src = np.random.default_rng(0).uniform(-1, 1, ref.n_dofs)
+    h_dst = torch.empty(ref.n_dofs, dtype=torch.float64).pin_memory()
+    A.vmult_host(h_dst, torch.from_numpy(src).pin_memory())
+    torch.cuda.synchronize()
+    assert rel(h_dst.numpy(), ref.apply(src)) <= 1e-12
