@@ -564,7 +564,7 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
         return cuda_status(cudaErrorUnknown, "mfgb_vmult_host: streams");
   const int p = op->degree;
   const int nz = op->is_box ? op->box.nz : 1;
-  const int S = op->is_box ? std::min(nz, 8) : 1;
+  const int S = op->is_box ? std::max(1, std::min(16, nz / 2)) : 1;  // >= 2 cell layers a slab
   const int Lz = (nz + S - 1) / S;
   const int n_ev = 3 * S + 1;
   while ((int)op->pipe_ev.size() < n_ev) {

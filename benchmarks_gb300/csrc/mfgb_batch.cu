@@ -1217,7 +1217,7 @@ mfgb_status mfgb_batch_precondition(mfgb_batch *B, double *d_dst, const double *
 // FP64 CG on every problem at once (deal.II SolverCG / ReductionControl per
 // problem: tol_eff = max(tol, reduce |r0|)), the batched V-cycle as the
 // preconditioner; one iteration of the batch = one CUDA graph launch.  When the
-// problems still running hold at most 60 % of the current plan's DoFs, the
+// problems still running hold at most 75 % of the current plan's DoFs, the
 // plan is gathered again for them and the graph re-captured, so converged
 // problems stop costing operator and V-cycle work.
 mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
@@ -1316,7 +1316,7 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
           active[i] = 1;
           dofs += B->depth[0].parts[i].n;
         }
-      if (dofs <= 0.6 * (double)cur->dofs) {
+      if (dofs <= 0.75 * (double)cur->dofs) {
         Plan next;
         if ((st = gather_plan(B, active, next, s))) break;
         cudaGraphExecDestroy(exec);

@@ -302,7 +302,7 @@ mfgb_status mfgb_batch_precondition(mfgb_batch *batch, double *d_dst, const doub
                                     void *stream);
 /* solves A_i x_i = b_i for every problem; h_info has n_problems entries.
    MFGB_ERR_NOT_CONVERGED if any problem reached max_steps (infos filled).
-   Once the problems still running hold at most 60 % of the DoFs of the current
+   Once the problems still running hold at most 75 % of the DoFs of the current
    launch plan, the union operators and tables are gathered again for them
    (converged problems stop costing work). */
 mfgb_status mfgb_batch_cg_solve(mfgb_batch *batch, const double *d_b, double *d_x,
