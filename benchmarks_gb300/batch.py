@@ -117,3 +117,4 @@ class BatchSolver:
         self.replans = r.value
         _abi.check(st)
         return x
+
