@@ -567,8 +567,7 @@ mfgb_status vcycle_b(const mfgb_batch *B, const Plan &P, cudaStream_t s) {
       return st;
     for (const PGroup &pg : D.pgroups) {
       const mfgb_operator *op = D.groups[pg.g];
-      k_p_restrict_sf<float><<<(unsigned)std::min<int64_t>(op->n_cells, 152 * 16), 128, 0, s>>>(
-          op->n_cells, op->d_map, pg.map_c, V.r, V.inv_val, C.b, pg.P);
+      p_transfer<float>(true, op->n_cells, op->d_map, pg.map_c, V.r, V.inv_val, C.b, pg.P, s);
     }
     if (D.n_hcoarse)
       kb_h_restrict<<<D.n_hcoarse, T256, 0, s>>>(D.d_hcoarse, D.d_hp, V.r, C.b);
@@ -586,8 +585,7 @@ mfgb_status vcycle_b(const mfgb_batch *B, const Plan &P, cudaStream_t s) {
         return st;
       for (const PGroup &pg : D.pgroups) {
         const mfgb_operator *op = D.groups[pg.g];
-        k_p_prolongate_sf<float><<<(unsigned)std::min<int64_t>(op->n_cells, 152 * 16), 128, 0, s>>>(
-            op->n_cells, op->d_map, pg.map_c, C.x, V.t, pg.P);
+        p_transfer<float>(false, op->n_cells, op->d_map, pg.map_c, C.x, nullptr, V.t, pg.P, s);
       }
       kb_add<<<D.n_pch, T256, 0, s>>>(D.d_pch, V.t, V.x);
     }

@@ -301,8 +301,8 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
   if (L.to_coarse == 1) {
     const PTransferParams P = ptransfer(L.op, C.op);
     if ((st = cuda_status(cudaMemsetAsync(C.b, 0, sizeof(T) * C.n, s), "coarse b = 0"))) return st;
-    k_p_restrict_sf<T><<<(unsigned)std::min<int64_t>(L.op->n_cells, 152 * 16), 128, 0, s>>>(
-        L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)L.r, (const T *)L.inv_val, (T *)C.b, P);
+    p_transfer<T>(true, L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)L.r,
+                  (const T *)L.inv_val, (T *)C.b, P, s);
   } else {
     k_h_restrict<T><<<grid1d(C.n), T256, 0, s>>>(hgrid(L.box, L.bs, C.box), (const T *)L.r, (T *)C.b);
   }
@@ -311,8 +311,8 @@ mfgb_status vcycle(mfgb_mg *mg, size_t l, cudaStream_t s) {
   if (L.to_coarse == 1) {
     const PTransferParams P = ptransfer(L.op, C.op);
     if ((st = cuda_status(cudaMemsetAsync(L.t, 0, sizeof(T) * L.n, s), "t = 0"))) return st;
-    k_p_prolongate_sf<T><<<(unsigned)std::min<int64_t>(L.op->n_cells, 152 * 16), 128, 0, s>>>(
-        L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)C.x, (T *)L.t, P);
+    p_transfer<T>(false, L.op->n_cells, L.op->d_map, C.op->d_map, (const T *)C.x, nullptr,
+                  (T *)L.t, P, s);
     k_axpy<T><<<grid1d(L.n), T256, 0, s>>>(L.n, (T)1, (const T *)L.t, (T *)L.x);
   } else {
     k_h_prolongate_add<T><<<grid1d(L.n), T256, 0, s>>>(hgrid(L.box, L.bs, C.box), (const T *)C.x,

@@ -200,6 +200,149 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Column-layout p-transfers: a CTA holds E cells and thread (e, j, k) owns the
+// fine column i = 0..NF-1 of cell e in registers.  Prolongation reads the
+// cell's NC^3 coarse values from shared memory and writes its fine column
+// (plain writes: shared fine DoFs get the same value from every cell);
+// restriction forms s[a] = sum_i B[i][a] r_i in registers, then one thread per
+// coarse DoF sums B[j][b] B[k][c] s[a][j][k] over the cell and adds atomically.
+template <int NF> struct PtCells {
+  static constexpr int value = NF <= 3 ? 16 : NF <= 5 ? 8 : NF <= 7 ? 4 : 2;
+};
+
+template <class T, int NF, int NC>
+__global__ void __launch_bounds__(NF * NF * PtCells<NF>::value)
+    k_p_prolongate_col(int64_t n_cells, const uint32_t *__restrict__ map_f,
+                       const uint32_t *__restrict__ map_c, const T *__restrict__ xc,
+                       T *__restrict__ tf, PTransferParams P) {
+  constexpr int E = PtCells<NF>::value, NF2 = NF * NF, NF3 = NF2 * NF, NC3 = NC * NC * NC;
+  __shared__ T sB[NF * NC];
+  __shared__ T sc[E * NC3];
+  const int tid = threadIdx.x, el = tid / NF2, jk = tid - el * NF2, j = jk / NF, k = jk - j * NF;
+  for (int t = tid; t < NF * NC; t += blockDim.x) sB[t] = bval<T>(P, t);
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  for (int64_t batch = blockIdx.x; batch < n_batches; batch += gridDim.x) {
+    for (int t = tid; t < E * NC3; t += blockDim.x) {
+      const int64_t c = batch * E + t / NC3;
+      const uint32_t d = c < n_cells ? map_c[c * NC3 + t % NC3] : MFGB_INVALID_DOF;
+      sc[t] = d != MFGB_INVALID_DOF ? xc[d] : T(0);
+    }
+    __syncthreads();
+    const int64_t cell = batch * E + el;
+    if (cell < n_cells) {
+      const T *x = sc + el * NC3;
+      T t2[NC];
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        T acc = 0;
+#pragma unroll
+        for (int b = 0; b < NC; ++b) {
+          T in = 0;
+#pragma unroll
+          for (int c = 0; c < NC; ++c) in += sB[k * NC + c] * x[(a * NC + b) * NC + c];
+          acc += sB[j * NC + b] * in;
+        }
+        t2[a] = acc;
+      }
+#pragma unroll
+      for (int i = 0; i < NF; ++i) {
+        const uint32_t d = map_f[cell * NF3 + i * NF2 + jk];
+        if (d == MFGB_INVALID_DOF) continue;
+        T v = 0;
+#pragma unroll
+        for (int a = 0; a < NC; ++a) v += sB[i * NC + a] * t2[a];
+        tf[d] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <class T, int NF, int NC>
+__global__ void __launch_bounds__(NF * NF * PtCells<NF>::value)
+    k_p_restrict_col(int64_t n_cells, const uint32_t *__restrict__ map_f,
+                     const uint32_t *__restrict__ map_c, const T *__restrict__ rf,
+                     const T *__restrict__ inv_val_f, T *__restrict__ rc, PTransferParams P) {
+  constexpr int E = PtCells<NF>::value, NF2 = NF * NF, NF3 = NF2 * NF, NC3 = NC * NC * NC;
+  __shared__ T sB[NF * NC];
+  __shared__ T ss[E * NC * NF2];
+  const int tid = threadIdx.x, el = tid / NF2, jk = tid - el * NF2;
+  for (int t = tid; t < NF * NC; t += blockDim.x) sB[t] = bval<T>(P, t);
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  for (int64_t batch = blockIdx.x; batch < n_batches; batch += gridDim.x) {
+    __syncthreads();  // sB ready / previous batch's ss consumed
+    const int64_t cell = batch * E + el;
+    T r[NF];
+#pragma unroll
+    for (int i = 0; i < NF; ++i) {
+      const uint32_t d = cell < n_cells ? map_f[cell * NF3 + i * NF2 + jk] : MFGB_INVALID_DOF;
+      r[i] = d != MFGB_INVALID_DOF ? rf[d] * inv_val_f[d] : T(0);
+    }
+#pragma unroll
+    for (int a = 0; a < NC; ++a) {
+      T acc = 0;
+#pragma unroll
+      for (int i = 0; i < NF; ++i) acc += sB[i * NC + a] * r[i];
+      ss[(el * NC + a) * NF2 + jk] = acc;
+    }
+    __syncthreads();
+    for (int t = tid; t < E * NC3; t += blockDim.x) {
+      const int e2 = t / NC3, l = t - e2 * NC3;
+      const int64_t c2 = batch * E + e2;
+      if (c2 >= n_cells) continue;
+      const uint32_t d = map_c[c2 * NC3 + l];
+      if (d == MFGB_INVALID_DOF) continue;
+      const int a = l / (NC * NC), b = (l / NC) % NC, c = l % NC;
+      const T *sa = ss + (e2 * NC + a) * NF2;
+      T acc = 0;
+#pragma unroll
+      for (int jj = 0; jj < NF; ++jj) {
+        T in = 0;
+#pragma unroll
+        for (int kk = 0; kk < NF; ++kk) in += sB[kk * NC + c] * sa[jj * NF + kk];
+        acc += sB[jj * NC + b] * in;
+      }
+      atomicAdd(rc + d, acc);
+    }
+  }
+}
+
+// launch helpers: the (NF, NC) pairs of the halving rule p -> max(1, p/2)
+template <class T, int NF, int NC>
+void p_transfer_col(bool restrict_, int64_t n_cells, const uint32_t *map_f, const uint32_t *map_c,
+                    const T *x, const T *inv_val, T *y, const PTransferParams &P, cudaStream_t s) {
+  constexpr int E = PtCells<NF>::value;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(n_batches, 152 * 8));
+  if (restrict_)
+    k_p_restrict_col<T, NF, NC><<<grid, E * NF * NF, 0, s>>>(n_cells, map_f, map_c, x, inv_val, y, P);
+  else
+    k_p_prolongate_col<T, NF, NC><<<grid, E * NF * NF, 0, s>>>(n_cells, map_f, map_c, x, y, P);
+}
+
+// y = P x (prolongation into a zeroed y) or y += R x (restriction), any (nf, nc)
+template <class T>
+void p_transfer(bool restrict_, int64_t n_cells, const uint32_t *map_f, const uint32_t *map_c,
+                const T *x, const T *inv_val, T *y, const PTransferParams &P, cudaStream_t s) {
+  if (n_cells <= 0) return;
+  const int key = P.nf * 16 + P.nc;
+  switch (key) {
+#define MFGB_PT(NF, NC)                                                              \
+  case NF * 16 + NC:                                                                 \
+    p_transfer_col<T, NF, NC>(restrict_, n_cells, map_f, map_c, x, inv_val, y, P, s); \
+    return;
+    MFGB_PT(3, 2) MFGB_PT(4, 2) MFGB_PT(5, 3) MFGB_PT(6, 3) MFGB_PT(7, 4) MFGB_PT(8, 4)
+    MFGB_PT(9, 5)
+#undef MFGB_PT
+    default: break;
+  }
+  const unsigned grid = (unsigned)std::min<int64_t>(n_cells, 152 * 16);
+  if (restrict_)
+    k_p_restrict_sf<T><<<grid, 128, 0, s>>>(n_cells, map_f, map_c, x, inv_val, y, P);
+  else
+    k_p_prolongate_sf<T><<<grid, 128, 0, s>>>(n_cells, map_f, map_c, x, y, P);
+}
+
 // ---- h-transfer between nested structured Q1 grids -----------------------
 // Level nodes of an axis sit at fine mesh nodes min(k s, nf) (BoxStride); the
 // coarse level (stride 2s) keeps every other node and the last one.  x fastest.

@@ -124,6 +124,7 @@ __device__ __forceinline__ void axis_span(int64_t c, int nf, int s, double &a, d
 __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__restrict__ G,
                                     double *__restrict__ JxW) {
   __shared__ double xyz[729 * 3];
+  __shared__ double s1[3][9];  // sin(2 pi X) of the cell's node coordinates, per axis
   const int n = b.degree + 1, n3 = n * n * n;
   const int ng = gp.ng, ng3 = ng * ng * ng;
   const int64_t e = blockIdx.x;
@@ -135,12 +136,21 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
   axis_span(cy, gp.nf[1], gp.s, ay, wy);
   axis_span(cz, gp.nf[2], gp.s, az, wz);
   const double two_pi = 2.0 * M_PI;
+  // the deformation is separable: 3 ng sines per cell instead of 3 ng^3
+  if (threadIdx.x < 3 * ng) {
+    const int d = threadIdx.x / ng, m = threadIdx.x % ng;
+    const double t = 0.5 * (gp.xg[m] + 1.0);
+    const double c = d == 0 ? b.lo[0] + (ax + t * wx) * hx
+                            : d == 1 ? b.lo[1] + (ay + t * wy) * hy : b.lo[2] + (az + t * wz) * hz;
+    s1[d][m] = sin(two_pi * c);
+  }
+  __syncthreads();
   for (int l = threadIdx.x; l < ng3; l += blockDim.x) {
     const int i = l / (ng * ng), j = (l / ng) % ng, k = l % ng;
     const double X = b.lo[0] + (ax + 0.5 * (gp.xg[k] + 1.0) * wx) * hx;
     const double Y = b.lo[1] + (ay + 0.5 * (gp.xg[j] + 1.0) * wy) * hy;
     const double Z = b.lo[2] + (az + 0.5 * (gp.xg[i] + 1.0) * wz) * hz;
-    const double s = b.amplitude * sin(two_pi * X) * sin(two_pi * Y) * sin(two_pi * Z);
+    const double s = b.amplitude * s1[0][k] * s1[1][j] * s1[2][i];
     xyz[3 * l + 0] = X + s;
     xyz[3 * l + 1] = Y + s;
     xyz[3 * l + 2] = Z + s;
