@@ -379,7 +379,7 @@ def bp5_solves(A):
         from benchmarks_gb300.learned import LearnedSmoother
         S = LearnedSmoother.load(wpath)
         M = mf.MGPreconditioner(mesh, precision=32)
-        (used, its_plain, its_learned), t_cal = timed(
+        (used, its_plain, its_learned, alpha), t_cal = timed(
             lambda: S.attach(M, A, calibrate=True, reduce=1e-10))
         x = A.initialize_dof_vector()
         ctl = mf.ReductionControl(1000, 1e-300, 1e-10)
@@ -387,9 +387,27 @@ def bp5_solves(A):
         out["mg_cg_fp32_learned"] = {
             "seconds": t, "iterations": ctl.last_step(), "used_learned_weights": used,
             "calibration_iterations_plain": its_plain,
-            "calibration_iterations_learned": its_learned, "calibration_seconds": t_cal,
+            "calibration_iterations_learned": its_learned, "exponent": alpha,
+            "calibration_seconds": t_cal,
             "error_vs_fp64_mg": float(torch.linalg.norm(x - sols[64]) / torch.linalg.norm(sols[64]))}
         del M
+        # the same on a strongly deformed cube of the same size (amplitude 0.12,
+        # the largest of the training range), where the smoother weights matter
+        mesh2 = mf.BoxMesh(w["nx"], w["ny"], w["nz"], degree=w["degree"], amplitude=0.12)
+        A2 = mf.LaplaceOperator(mesh2)
+        b2 = A2.rhs_uniform(w["seed"])
+        M2 = mf.MGPreconditioner(mesh2, precision=32)
+        res = {}
+        for name in ("plain", "learned"):
+            if name == "learned":
+                used2, p2, l2, alpha2 = S.attach(M2, A2, calibrate=True, reduce=1e-10)
+            x = A2.initialize_dof_vector()
+            ctl = mf.ReductionControl(1000, 1e-300, 1e-10)
+            _, t = timed(lambda: mf.SolverCG(ctl).solve(A2, x, b2, M2))
+            res[name] = {"seconds": t, "iterations": ctl.last_step()}
+        res["used_learned_weights"], res["exponent"] = used2, alpha2
+        out["mg_cg_fp32_learned_amplitude_0.12"] = res
+        del M2, A2
     x = A.initialize_dof_vector()
     ctl = mf.ReductionControl(100000, 1e-300, 1e-10)
     P = A.get_matrix_diagonal_inverse()

@@ -3,13 +3,16 @@ reference).
 
 A 73-64-64-1 MLP maps a cell's corner Jacobians and degree to
 lambda_e ~ lambda_max(D_e^-1 A_e).  The finest-level Chebyshev smoother then
-uses the positive diagonal D~ = sum_e lambda_e D_e (``mfgb_mg_set_smoother_
-weights``), which keeps the preconditioner linear and SPD, so plain CG stays
-valid.  Training data come from the FP64 operator itself (per-cell power
-iterations, ``mfgb_cell_lambda``); training runs on the GPU with the library's
-own forward/backward/Adam kernels; inference uses BF16 tensor cores.  If a
-calibration solve does not show fewer iterations than the plain smoother, the
-plain smoother is kept (``LearnedSmoother.attach`` returns which one is used).
+uses the positive diagonal D~ = sum_e lambda_e^alpha D_e
+(``mfgb_mg_set_smoother_weights``), which keeps the preconditioner linear and
+SPD, so plain CG stays valid.  Training data come from the FP64 operator itself
+(per-cell power iterations, ``mfgb_cell_lambda``); training runs on the GPU with
+the library's own forward/backward/Adam kernels; inference uses BF16 tensor
+cores.  The exponent alpha is chosen by calibration solves of the multigrid
+itself (on strongly deformed meshes alpha = 1/2 saves an iteration where
+alpha = 1 does not); if no exponent needs fewer iterations than the plain
+smoother, the plain smoother is kept (``LearnedSmoother.attach`` returns which
+one is used).
 """
 from __future__ import annotations
 
@@ -64,7 +67,7 @@ class LearnedSmoother:
         params = np.asarray(params, dtype=np.float32)
         if params.size != n:
             raise ValueError(f"expected {n} parameters, got {params.size}")
-        self.params = torch.from_numpy(params).cuda()
+        self.params = torch.from_numpy(np.array(params, dtype=np.float32)).cuda()
         self.loss_history = []
 
     # ---- data and training -------------------------------------------------
@@ -110,17 +113,20 @@ class LearnedSmoother:
         return y
 
     # ---- use in the multigrid ------------------------------------------------
-    def attach(self, mg, A, calibrate=True, reduce=1e-6, seed=7):
-        """Set the predicted cell weights on the finest level of `mg` (for the
-        operator `A` of the same mesh).  With `calibrate`, one solve with each
-        smoother on a seeded right-hand side decides; the learned weights are
-        kept only if they need fewer iterations.  Returns (used_learned,
-        iterations_plain, iterations_learned)."""
+    def attach(self, mg, A, calibrate=True, reduce=1e-6, seed=7, exponents=(0.25, 0.5, 1.0)):
+        """Set the predicted cell weights lambda^alpha on the finest level of `mg`
+        (for the operator `A` of the same mesh).  With `calibrate`, one solve
+        per exponent and one with the plain smoother on a seeded right-hand side
+        decide; the best learned weights are kept only if they need fewer
+        iterations than the plain smoother.  Returns (used_learned,
+        iterations_plain, iterations_learned, alpha) -- iterations_learned and
+        alpha of the best exponent."""
         import benchmarks_gb300 as mf
-        w = self.predict(cell_features(A))
+        lam = self.predict(cell_features(A))
         if not calibrate:
+            w = (lam ** exponents[0]).contiguous()
             _abi.check(lib().mfgb_mg_set_smoother_weights(mg.handle, _ptr(w)))
-            return True, None, None
+            return True, None, None, exponents[0]
 
         def its():
             b = A.rhs_uniform(seed)
@@ -131,12 +137,19 @@ class LearnedSmoother:
 
         _abi.check(lib().mfgb_mg_set_smoother_weights(mg.handle, None))
         plain = its()
-        _abi.check(lib().mfgb_mg_set_smoother_weights(mg.handle, _ptr(w)))
-        learned = its()
-        if learned < plain:
-            return True, plain, learned
+        best, best_alpha = None, None
+        for alpha in exponents:
+            w = (lam ** alpha).contiguous()
+            _abi.check(lib().mfgb_mg_set_smoother_weights(mg.handle, _ptr(w)))
+            k = its()
+            if best is None or k < best:
+                best, best_alpha = k, alpha
+        if best < plain:
+            w = (lam ** best_alpha).contiguous()
+            _abi.check(lib().mfgb_mg_set_smoother_weights(mg.handle, _ptr(w)))
+            return True, plain, best, best_alpha
         _abi.check(lib().mfgb_mg_set_smoother_weights(mg.handle, None))  # fall back
-        return False, plain, learned
+        return False, plain, best, best_alpha
 
     # ---- persistence: magic, version, count, float32 parameters ----------------
     def save(self, path):
