@@ -333,6 +333,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         line["batched"] = batched_solves()
         line["ceed_bk1_bk3_evector"] = bk1_bk3_rates()
         line["helmholtz_bp5"] = helmholtz_bp5(args)
+        line["bp3"] = bp3_rate(args)
     print(json.dumps(line), flush=True)
 
 
@@ -568,6 +569,31 @@ def helmholtz_bp5(args):
             "cg_seconds": best, "cg_iterations": its, "cg_converged": converged,
             "cg_residual_reduction": reduction, "vmult_seconds": mv,
             "vmult_GDoF/s": mesh.n_dofs / mv / 1e9}
+
+
+def bp3_rate(args):
+    """BP3 (Laplacian at QGauss(p+2), L-vector) apply on the bench mesh, GDoF/s."""
+    import torch
+
+    import benchmarks_gb300 as mf
+    w = WORKLOAD
+    A = mf.LaplaceOperator(mf.BoxMesh(w["nx"], w["ny"], w["nz"], degree=w["degree"],
+                                      amplitude=w["amplitude"]), arith=args.arith, quadrature="bp3")
+    u = A.rhs_uniform(1)
+    y = A.initialize_dof_vector()
+    for _ in range(3):
+        A.vmult(y, u)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        A.vmult(y, u)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    n = A.m()
+    del A
+    return {"GDoF/s": n / ms / 1e6, "ms_per_vmult": ms, "n_q_1d": w["degree"] + 2}
 
 
 def bk6_rate(A, args):

@@ -100,14 +100,15 @@ class LaplaceOperator:
                  G=None, constrained=None, arith="df", quadrature="gll"):
         L = lib()
         self._op = ctypes.c_void_p()
-        if quadrature not in ("gll", "gauss", "helmholtz"):
-            raise ValueError("quadrature must be 'gll' (collocation), 'gauss' (BP5 variant) or "
-                             "'helmholtz' (mass + stiffness at the Gauss points)")
+        if quadrature not in ("gll", "gauss", "helmholtz", "bp3"):
+            raise ValueError("quadrature must be 'gll' (collocation), 'gauss' (BP5 variant, q = p+1), "
+                             "'helmholtz' (mass + stiffness at the Gauss points) or 'bp3' (q = p+2)")
         self.quadrature = quadrature
         if mesh is not None:
             desc = mesh._desc()
             create = {"gll": L.mfgb_operator_create_box, "gauss": L.mfgb_operator_create_box_gauss,
-                      "helmholtz": L.mfgb_operator_create_box_helmholtz}[quadrature]
+                      "helmholtz": L.mfgb_operator_create_box_helmholtz,
+                      "bp3": L.mfgb_operator_create_box_bp3}[quadrature]
             _abi.check(create(ctypes.byref(desc), ctypes.byref(self._op)))
             self.mesh = mesh
         else:

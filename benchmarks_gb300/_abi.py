@@ -70,6 +70,7 @@ def lib():
         "mfgb_operator_create": ([I32, I64, I64, P, P, I64, P, PP], I32),
         "mfgb_operator_create_box_gauss": ([ctypes.POINTER(BoxDesc), PP], I32),
         "mfgb_operator_create_box_helmholtz": ([ctypes.POINTER(BoxDesc), PP], I32),
+        "mfgb_operator_create_box_bp3": ([ctypes.POINTER(BoxDesc), PP], I32),
         "mfgb_operator_destroy": ([P], I32),
         "mfgb_operator_info": ([P, P, P, P, P], I32),
         "mfgb_operator_export": ([P, P, P, P], I32),

@@ -40,7 +40,7 @@ static mfgb_status dev_alloc(void **p, size_t bytes, const char *what) {
 }
 
 mfgb_status ensure_df(mfgb_operator *op) {
-  if (op->d_Gdf) return MFGB_OK;
+  if (op->d_Gdf || op->quadrature == 2) return MFGB_OK;  // BP3 reads FP64 G in both arithmetics
   const int64_t ng = op->n_cells * 6 * (int64_t)op->n * op->n * op->n;
   mfgb_status st = dev_alloc((void **)&op->d_Gdf, sizeof(float2) * ng, "G (double-float)");
   if (st) return st;
@@ -55,32 +55,47 @@ mfgb_status ensure_df(mfgb_operator *op) {
   return cuda_status(cudaDeviceSynchronize(), "G -> double-float");
 }
 
+// dst += A src over cells [cell0, cell0 + n) (the map keeps global DoF indices);
+// partials/grid (the energy form) are supported by the GLL and Gauss p+1 kernels
+static cudaError_t apply_range(mfgb_operator *op, int64_t cell0, int64_t n, double *dst,
+                               const double *src, int arith, double *partials, int *grid,
+                               cudaStream_t s, const int *done) {
+  const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  const int64_t q3 = (int64_t)op->nq * op->nq * op->nq;
+  const uint32_t *map = op->d_map + cell0 * n3;
+  if (op->quadrature == 2) {
+    if (partials || done) return cudaErrorNotSupported;
+    return bp3_apply(op->degree, n, map, op->d_Bq, op->d_DGq, op->d_G + cell0 * 6 * q3, src, dst,
+                     arith, s);
+  }
+  if (arith == MFGB_ARITH_FP64)
+    return op->quadrature
+               ? bk5g_f64(op->n, n, map, op->d_G + cell0 * 6 * n3, src, dst, op->DG, op->Bq,
+                          partials, grid, s, done, op->d_JxW ? op->d_JxW + cell0 * n3 : nullptr)
+               : bk5_f64(op->n, n, map, op->d_G + cell0 * 6 * n3, src, dst, op->D, partials, grid,
+                         s, done);
+  return op->quadrature
+             ? bk5g_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->DG, op->Bq,
+                       partials, grid, s, done, op->d_JxWdf ? op->d_JxWdf + cell0 * n3 : nullptr)
+             : bk5_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->D, partials, grid, s,
+                      done);
+}
+
 mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int arith,
                        double *partials, int *grid, cudaStream_t s, const int *done) {
   const bool full = partials == nullptr;
   mfgb_status st;
-  if (full && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
-                                "vmult: dst = 0")))
-    return st;
-  cudaError_t e;
-  if (arith == MFGB_ARITH_FP64) {
-    e = op->quadrature
-            ? bk5g_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->DG, op->Bq, partials,
-                       grid, s, done, op->d_JxW)
-            : bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s,
-                      done);
-  } else if (arith == MFGB_ARITH_FP64_DF) {
-    if ((st = ensure_df(op))) return st;
-    e = op->quadrature
-            ? bk5g_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->DG, op->Bq, partials,
-                      grid, s, done, op->d_JxWdf)
-            : bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s,
-                     done);
-  } else {
+  if (arith != MFGB_ARITH_FP64 && arith != MFGB_ARITH_FP64_DF) {
     set_error("vmult: unknown arith mode");
     return MFGB_ERR_INVALID_ARG;
   }
-  if ((st = cuda_status(e, "vmult: bk5 kernel"))) return st;
+  if (arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if (full && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
+                                "vmult: dst = 0")))
+    return st;
+  if ((st = cuda_status(apply_range(op, 0, op->n_cells, dst, src, arith, partials, grid, s, done),
+                        "vmult: operator kernel")))
+    return st;
   if (full)
     return cuda_status(copy_constrained(op->n_constrained, op->d_constrained, src, dst, s),
                        "vmult: constrained rows");
@@ -122,42 +137,14 @@ int kernel_shape(int arith_class, int N) {
 mfgb_status apply_add_impl(mfgb_operator *op, double *dst, const double *src, int arith,
                            cudaStream_t s, const int *done) {
   mfgb_status st;
-  cudaError_t e;
-  if (arith == MFGB_ARITH_FP64) {
-    e = op->quadrature ? bk5g_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->DG, op->Bq,
-                                  nullptr, nullptr, s, done, op->d_JxW)
-                       : bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, nullptr,
-                                 nullptr, s, done);
-  } else if (arith == MFGB_ARITH_FP64_DF) {
-    if ((st = ensure_df(op))) return st;
-    e = op->quadrature ? bk5g_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->DG,
-                                 op->Bq, nullptr, nullptr, s, done, op->d_JxWdf)
-                       : bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D,
-                                nullptr, nullptr, s, done);
-  } else {
+  if (arith != MFGB_ARITH_FP64 && arith != MFGB_ARITH_FP64_DF) {
     set_error("apply: unknown arith mode");
     return MFGB_ERR_INVALID_ARG;
   }
-  return cuda_status(e, "apply: bk5 kernel");
-}
-
-// dst += A src over cells [cell0, cell0 + n): the map keeps global DoF indices
-static cudaError_t apply_cells(mfgb_operator *op, int64_t cell0, int64_t n, double *dst,
-                               const double *src, int arith, cudaStream_t s) {
-  const int64_t n3 = (int64_t)op->n * op->n * op->n;
-  const uint32_t *map = op->d_map + cell0 * n3;
-  if (arith == MFGB_ARITH_FP64)
-    return op->quadrature
-               ? bk5g_f64(op->n, n, map, op->d_G + cell0 * 6 * n3, src, dst, op->DG, op->Bq,
-                          nullptr, nullptr, s, nullptr, op->d_JxW ? op->d_JxW + cell0 * n3 : nullptr)
-               : bk5_f64(op->n, n, map, op->d_G + cell0 * 6 * n3, src, dst, op->D, nullptr,
-                         nullptr, s);
-  return op->quadrature
-             ? bk5g_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->DG, op->Bq,
-                       nullptr, nullptr, s, nullptr,
-                       op->d_JxWdf ? op->d_JxWdf + cell0 * n3 : nullptr)
-             : bk5_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->D, nullptr, nullptr,
-                      s);
+  if (arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if (done && op->quadrature == 2) done = nullptr;  // the BP3 kernel runs every time
+  return cuda_status(apply_range(op, 0, op->n_cells, dst, src, arith, nullptr, nullptr, s, done),
+                     "apply: operator kernel");
 }
 
 static void free_operator(mfgb_operator *op) {
@@ -172,6 +159,8 @@ static void free_operator(mfgb_operator *op) {
   cudaFree(op->d_JxWdf);
   cudaFree(op->d_hsrc);
   cudaFree(op->d_hdst);
+  cudaFree(op->d_Bq);
+  cudaFree(op->d_DGq);
   for (cudaStream_t st : op->pipe)
     if (st) cudaStreamDestroy(st);
   for (cudaEvent_t e : op->pipe_ev) cudaEventDestroy(e);
@@ -181,6 +170,7 @@ static void free_operator(mfgb_operator *op) {
 static void init_basis(mfgb_operator *op, int degree) {
   op->degree = degree;
   op->n = degree + 1;
+  op->nq = op->n;
   gll_nodes(op->n, op->gll_x, op->gll_w);
   derivative_matrix(op->n, op->gll_x, op->D);
 }
@@ -263,6 +253,10 @@ mfgb_status mfgb_operator_create_box_helmholtz(const mfgb_box_desc *box, mfgb_op
   return create_box_impl(box, 1, out, nullptr, true);
 }
 
+mfgb_status mfgb_operator_create_box_bp3(const mfgb_box_desc *box, mfgb_operator **out) {
+  return create_box_impl(box, 2, out);
+}
+
 static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfgb_operator **out,
                                    const BoxStride *bs, bool mass) {
   if (!box || !out) {
@@ -286,11 +280,12 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
   mfgb_operator *op = new mfgb_operator();
   init_basis(op, box->degree);
   op->quadrature = quadrature;
-  if (quadrature) {  // Gauss points = GLL count (BP5 variant, q = p + 1)
-    double xq[9], wq[9];
-    gauss_nodes(op->n, xq, wq);
-    derivative_matrix(op->n, xq, op->DG);
-    for (int q = 0; q < op->n; ++q)
+  if (quadrature) {  // Gauss points: n (BP5 variant, q = p + 1) or n + 1 (BP3, q = p + 2)
+    op->nq = quadrature == 2 ? op->n + 1 : op->n;
+    double xq[10], wq[10];
+    gauss_nodes(op->nq, xq, wq);
+    derivative_matrix(op->nq, xq, op->DG);
+    for (int q = 0; q < op->nq; ++q)
       for (int i = 0; i < op->n; ++i) op->Bq[q * op->n + i] = lagrange_value(op->n, op->gll_x, i, xq[q]);
   }
   op->is_box = true;
@@ -298,6 +293,7 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
   op->n_dofs = n_dofs;
   op->n_cells = (int64_t)box->nx * box->ny * box->nz;
   const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  const int64_t q3 = (int64_t)op->nq * op->nq * op->nq;  // points per cell of G
   // constrained list: every boundary DoF, ascending
   std::vector<int64_t> cons;
   cons.reserve(2 * (Nx * Ny + Ny * Nz + Nx * Nz));
@@ -315,9 +311,12 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
   op->h_constrained = cons;
   mfgb_status st;
   if ((st = dev_alloc((void **)&op->d_map, sizeof(uint32_t) * op->n_cells * n3, "dof map")) ||
-      (st = dev_alloc((void **)&op->d_G, sizeof(double) * op->n_cells * 6 * n3, "G")) ||
+      (st = dev_alloc((void **)&op->d_G, sizeof(double) * op->n_cells * 6 * q3, "G")) ||
       (st = dev_alloc((void **)&op->d_constrained, sizeof(int64_t) * cons.size(), "constraints")) ||
-      (mass && (st = dev_alloc((void **)&op->d_JxW, sizeof(double) * op->n_cells * n3, "JxW")))) {
+      (mass && (st = dev_alloc((void **)&op->d_JxW, sizeof(double) * op->n_cells * n3, "JxW"))) ||
+      (quadrature == 2 &&
+       ((st = dev_alloc((void **)&op->d_Bq, sizeof(double) * op->nq * op->n, "BP3 basis")) ||
+        (st = dev_alloc((void **)&op->d_DGq, sizeof(double) * op->nq * op->nq, "BP3 derivative"))))) {
     free_operator(op);
     return st;
   }
@@ -326,8 +325,13 @@ static mfgb_status create_box_impl(const mfgb_box_desc *box, int quadrature, mfg
                         "constraints copy")) ||
       (st = cuda_status(box_map(*box, op->d_map, nullptr), "box map")) ||
       (st = cuda_status(box_geometry(*box, op->gll_x, op->gll_w, op->D, op->d_G, nullptr,
-                                     quadrature != 0, bs, op->d_JxW),
+                                     quadrature != 0, bs, op->d_JxW, op->nq),
                         "box geometry")) ||
+      (quadrature == 2 &&
+       ((st = cuda_status(cudaMemcpy(op->d_Bq, op->Bq, sizeof(double) * op->nq * op->n,
+                                     cudaMemcpyHostToDevice), "BP3 basis")) ||
+        (st = cuda_status(cudaMemcpy(op->d_DGq, op->DG, sizeof(double) * op->nq * op->nq,
+                                     cudaMemcpyHostToDevice), "BP3 derivative")))) ||
       (st = cuda_status(cudaDeviceSynchronize(), "box set-up"))) {
     free_operator(op);
     return st;
@@ -414,6 +418,7 @@ mfgb_status mfgb_operator_export(const mfgb_operator *op, uint32_t *h_dof_map, d
     return MFGB_ERR_INVALID_ARG;
   }
   const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  const int64_t q3 = (int64_t)op->nq * op->nq * op->nq;  // G points per cell
   mfgb_status st;
   if (h_dof_map && op->n_cells > 0 &&
       (st = cuda_status(cudaMemcpy(h_dof_map, op->d_map, sizeof(uint32_t) * op->n_cells * n3,
@@ -421,7 +426,7 @@ mfgb_status mfgb_operator_export(const mfgb_operator *op, uint32_t *h_dof_map, d
                         "export map")))
     return st;
   if (h_G && op->n_cells > 0 &&
-      (st = cuda_status(cudaMemcpy(h_G, op->d_G, sizeof(double) * op->n_cells * 6 * n3,
+      (st = cuda_status(cudaMemcpy(h_G, op->d_G, sizeof(double) * op->n_cells * 6 * q3,
                                    cudaMemcpyDeviceToHost),
                         "export G")))
     return st;
@@ -449,26 +454,8 @@ mfgb_status mfgb_vmult_add(const mfgb_operator *op, double *d_dst, const double 
     set_error("mfgb_vmult_add: invalid argument (dst and src must be distinct device vectors)");
     return MFGB_ERR_INVALID_ARG;
   }
-  cudaStream_t s = (cudaStream_t)stream;
-  mfgb_operator *o = const_cast<mfgb_operator *>(op);
-  cudaError_t e;
-  mfgb_status st;
-  if (arith == MFGB_ARITH_FP64) {
-    e = o->quadrature ? bk5g_f64(o->n, o->n_cells, o->d_map, o->d_G, d_src, d_dst, o->DG, o->Bq,
-                                 nullptr, nullptr, s)
-                      : bk5_f64(o->n, o->n_cells, o->d_map, o->d_G, d_src, d_dst, o->D, nullptr,
-                                nullptr, s);
-  } else if (arith == MFGB_ARITH_FP64_DF) {
-    if ((st = ensure_df(o))) return st;
-    e = o->quadrature ? bk5g_df(o->n, o->n_cells, o->d_map, o->d_Gdf, d_src, d_dst, o->DG, o->Bq,
-                                nullptr, nullptr, s)
-                      : bk5_df(o->n, o->n_cells, o->d_map, o->d_Gdf, d_src, d_dst, o->D, nullptr,
-                               nullptr, s);
-  } else {
-    set_error("mfgb_vmult_add: unknown arith mode");
-    return MFGB_ERR_INVALID_ARG;
-  }
-  return cuda_status(e, "mfgb_vmult_add");
+  return apply_add_impl(const_cast<mfgb_operator *>(op), d_dst, d_src, arith, (cudaStream_t)stream,
+                        nullptr);
 }
 
 mfgb_status mfgb_copy_constrained(const mfgb_operator *op, double *d_dst, const double *d_src,
@@ -607,8 +594,9 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
     cudaStreamWaitEvent(s_c, ev[1 + 3 * k], 0);
     cudaMemsetAsync(op->d_hdst + a, 0, sizeof(double) * (b - a), s_c);
     const int64_t cell0 = (int64_t)z0 * cells_per_layer, ncell = (int64_t)(z1 - z0) * cells_per_layer;
-    if ((st = cuda_status(apply_cells(op, op->is_box ? cell0 : 0, op->is_box ? ncell : op->n_cells,
-                                      op->d_hdst, op->d_hsrc, arith, s_c),
+    if ((st = cuda_status(apply_range(op, op->is_box ? cell0 : 0, op->is_box ? ncell : op->n_cells,
+                                      op->d_hdst, op->d_hsrc, arith, nullptr, nullptr, s_c,
+                                      nullptr),
                           "mfgb_vmult_host: kernel")))
       return st;
     // identity rows among the completed DoFs (the list is ascending)
@@ -640,8 +628,8 @@ mfgb_status mfgb_compute_diagonal(const mfgb_operator *op, double *d_diag, void 
   if ((st = cuda_status(cudaMemsetAsync(d_diag, 0, sizeof(double) * op->n_dofs, s), "diag = 0")))
     return st;
   if (op->quadrature)
-    st = cuda_status(diagonal_gauss(op->n, op->n_cells, op->d_map, op->d_G, op->d_JxW, op->Bq,
-                                    op->DG, d_diag, s),
+    st = cuda_status(diagonal_gauss(op->n, op->nq, op->n_cells, op->d_map, op->d_G, op->d_JxW,
+                                    op->Bq, op->DG, d_diag, s),
                      "diagonal kernel (Gauss points)");
   else
     st = cuda_status(diagonal_f64(op->n, op->n_cells, op->d_map, op->d_G, op->D, d_diag, s),

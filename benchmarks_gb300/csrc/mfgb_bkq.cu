@@ -10,7 +10,7 @@ namespace {
 
 template <int NM, int NQ, class A, bool LAPLACE>
 cudaError_t bkq_launch(int64_t nelmt, const double *basis, const double *dbasis, const double *coef,
-                       const double *in, double *out, cudaStream_t s) {
+                       const double *in, double *out, cudaStream_t s, const uint32_t *map) {
   constexpr int E = BkqElems<NQ>::value;
   constexpr int threads = E * NQ * NQ;
   static int per_sm = -1;
@@ -26,22 +26,24 @@ cudaError_t bkq_launch(int64_t nelmt, const double *basis, const double *dbasis,
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t batches = (nelmt + E - 1) / E;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(batches, (int64_t)per_sm * sms));
-  bkq_kernel<NM, NQ, A, LAPLACE><<<grid, threads, 0, s>>>(nelmt, basis, dbasis, coef, in, out);
+  bkq_kernel<NM, NQ, A, LAPLACE><<<grid, threads, 0, s>>>(nelmt, basis, dbasis, coef, in, out,
+                                                           map);
   return cudaGetLastError();
 }
 
 template <class A, bool LAPLACE>
 cudaError_t bkq_dispatch(int degree, int64_t nelmt, const double *basis, const double *dbasis,
-                         const double *coef, const double *in, double *out, cudaStream_t s) {
+                         const double *coef, const double *in, double *out, cudaStream_t s,
+                         const uint32_t *map = nullptr) {
   switch (degree) {
-    case 1: return bkq_launch<2, 3, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
-    case 2: return bkq_launch<3, 4, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
-    case 3: return bkq_launch<4, 5, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
-    case 4: return bkq_launch<5, 6, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
-    case 5: return bkq_launch<6, 7, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
-    case 6: return bkq_launch<7, 8, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
-    case 7: return bkq_launch<8, 9, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
-    case 8: return bkq_launch<9, 10, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s);
+    case 1: return bkq_launch<2, 3, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
+    case 2: return bkq_launch<3, 4, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
+    case 3: return bkq_launch<4, 5, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
+    case 4: return bkq_launch<5, 6, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
+    case 5: return bkq_launch<6, 7, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
+    case 6: return bkq_launch<7, 8, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
+    case 7: return bkq_launch<8, 9, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
+    case 8: return bkq_launch<9, 10, A, LAPLACE>(nelmt, basis, dbasis, coef, in, out, s, map);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -68,6 +70,17 @@ mfgb_status bkq_entry(const char *name, bool laplace, int degree, int64_t nelmt,
 }
 
 }  // namespace
+
+// BP3 operator apply: dst += A src over n_cells cells (gather / scatter through map)
+cudaError_t bp3_apply(int degree, int64_t n_cells, const uint32_t *map, const double *B,
+                      const double *DG, const double *G, const double *src, double *dst, int arith,
+                      cudaStream_t s) {
+  if (n_cells <= 0) return cudaSuccess;
+  return arith == MFGB_ARITH_FP64
+             ? bkq_dispatch<ArithF64, true>(degree, n_cells, B, DG, G, src, dst, s, map)
+             : bkq_dispatch<ArithDF, true>(degree, n_cells, B, DG, G, src, dst, s, map);
+}
+
 }  // namespace mfgb
 
 using namespace mfgb;

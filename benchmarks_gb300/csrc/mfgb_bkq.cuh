@@ -10,7 +10,8 @@
 // Layouts (point and mode indices with direction 0 slowest, like BK5):
 // basis[q*NM + i], dbasis[q*NQ + m], JxW[e][NQ^3], G[e][6][NQ^3] (rr rs rt ss st
 // tt; the reference CUDA BK3 kernel's layout, templated_cuda_kernels.cuh:156-161),
-// in/out[e][NM^3].
+// in/out[e][NM^3].  With a dof map (L-vector mode, the BP3 operator) the input
+// is gathered through map[e][NM^3] and the output scatter-added atomically.
 //
 // GB300 structure: a CTA holds E elements, NQ^2 threads per element.  The
 // interpolation passes run one 1D line per thread through shared memory; the
@@ -28,7 +29,8 @@ template <int NM, int NQ, class A, bool LAPLACE>
 __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
     bkq_kernel(const int64_t nelmt, const double *__restrict__ basis,
                const double *__restrict__ dbasis, const double *__restrict__ coef,
-               const double *__restrict__ in, double *__restrict__ out) {
+               const double *__restrict__ in, double *__restrict__ out,
+               const uint32_t *__restrict__ map) {
   using V = typename A::V;
   using Acc = typename A::Acc;
   constexpr int E = BkqElems<NQ>::value;
@@ -53,7 +55,17 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
   for (int64_t batch = blockIdx.x; batch < n_batches; batch += gridDim.x) {
     const int64_t e = batch * E + el;
     const bool valid = e < nelmt;
-    for (int t = lt; t < NM3; t += NQ2) a0[t] = valid ? A::load_vec(in[e * NM3 + t]) : A::zero_v();
+    // E-vector: in[e][NM^3]; L-vector (map != nullptr): gather through the map
+    for (int t = lt; t < NM3; t += NQ2) {
+      if (!valid) {
+        a0[t] = A::zero_v();
+      } else if (map) {
+        const uint32_t d = __ldg(map + e * NM3 + t);
+        a0[t] = d != MFGB_INVALID_DOF ? A::load_vec(__ldg(in + d)) : A::zero_v();
+      } else {
+        a0[t] = A::load_vec(in[e * NM3 + t]);
+      }
+    }
     __syncthreads();
     // ---- interpolate: direction 0 (i -> p), lines (j, k)
     for (int t = lt; t < NM2; t += NQ2) {
@@ -203,7 +215,13 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
         A::zero(a);
 #pragma unroll
         for (int p = 0; p < NQ; ++p) A::fma(a, sB[p * NM + i], r[p]);
-        if (valid) out[e * NM3 + i * NM2 + t] = A::store_vec(A::finish(a));
+        if (!valid) continue;
+        if (map) {  // scatter-add (atomic: DoFs shared between cells)
+          const uint32_t d = __ldg(map + e * NM3 + i * NM2 + t);
+          if (d != MFGB_INVALID_DOF) atomicAdd(out + d, A::store_vec(A::finish(a)));
+        } else {
+          out[e * NM3 + i * NM2 + t] = A::store_vec(A::finish(a));
+        }
       }
     }
     __syncthreads();

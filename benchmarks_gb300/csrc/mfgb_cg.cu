@@ -485,6 +485,10 @@ extern "C" mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const doub
     set_error("mfgb_cg_solve_noalloc: unknown arith");
     return MFGB_ERR_INVALID_ARG;
   }
+  if (op->quadrature != 0) {
+    set_error("mfgb_cg_solve_noalloc: GLL-collocated operators only (use mfgb_cg_solve)");
+    return MFGB_ERR_UNSUPPORTED;
+  }
   const int64_t n = op->n_dofs;
   if (n > (int64_t)MFGB_CG_NOALLOC_MAX_DOFS) {
     set_error("mfgb_cg_solve_noalloc: " + std::to_string(n) + " DoFs exceed the fixed scratch of " +

@@ -19,11 +19,13 @@ struct mfgb_operator {
   int64_t *d_constrained = nullptr;
   double D[81] = {0};             // derivative matrix D[q*n + b]
   double gll_x[9] = {0}, gll_w[9] = {0};
-  int quadrature = 0;             // 0: GLL collocation, 1: Gauss (p+1 points, BP5 variant)
+  int quadrature = 0;             // 0: GLL collocation, 1: Gauss p+1 (BP5 variant), 2: Gauss p+2 (BP3)
+  int nq = 0;                     // quadrature points per direction (n, or n + 1 for BP3)
+  double *d_Bq = nullptr, *d_DGq = nullptr;  // BP3: the two matrices below on the device
   double *d_JxW = nullptr;        // Gauss form with a mass term (Helmholtz): [n_cells][n^3]
   float2 *d_JxWdf = nullptr;      // same, double-float pairs
-  double DG[81] = {0};            // Gauss form: collocation derivative on the Gauss points
-  double Bq[81] = {0};            // Gauss form: GLL basis at the Gauss points, Bq[q*n + i]
+  double DG[100] = {0};           // Gauss forms: collocation derivative on the Gauss points
+  double Bq[100] = {0};           // Gauss forms: GLL basis at the Gauss points, Bq[q*n + i]
   bool is_box = false;
   mfgb_box_desc box{};
   // workspace for reductions (per-CTA partials)
@@ -99,12 +101,17 @@ struct BoxStride {
 };
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
                          const double *D, double *d_G, cudaStream_t s, bool at_gauss = false,
-                         const BoxStride *bs = nullptr, double *d_JxW = nullptr);
+                         const BoxStride *bs = nullptr, double *d_JxW = nullptr,
+                         int n_gauss = 0);  // Gauss points per direction (0: degree + 1)
 // exact diagonal of the Gauss-point operator (Laplacian, plus mass when JxW is
 // given) on a box, accumulated into diag (not zeroed; constrained rows untouched)
-cudaError_t diagonal_gauss(int N, int64_t n_cells, const uint32_t *map, const double *G,
+cudaError_t diagonal_gauss(int N, int NQ, int64_t n_cells, const uint32_t *map, const double *G,
                            const double *JxW, const double *B, const double *DG, double *diag,
                            cudaStream_t s);
+// BP3 operator (mfgb_bkq.cu): dst += A src, q = p + 2 Gauss points, G[cell][6][nq^3]
+cudaError_t bp3_apply(int degree, int64_t n_cells, const uint32_t *map, const double *B,
+                      const double *DG, const double *G, const double *src, double *dst, int arith,
+                      cudaStream_t s);
 cudaError_t g_to_df(int64_t n, const double *G, float2 *Gdf, cudaStream_t s);
 cudaError_t g_to_f32(int64_t n, const double *G, float *G32, cudaStream_t s);
 cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const double *G,

@@ -102,9 +102,10 @@ cudaError_t box_map(const mfgb_box_desc &b, uint32_t *d_map, cudaStream_t s) {
 }
 
 struct GeomParams {
-  double x[9], w[9];      // GLL points / weights of the operator degree
+  double x[10], w[10];    // target points / weights (GLL of the degree, or Gauss)
   double xg[9];           // GLL points of the geometry degree
-  double V[81], Dv[81];   // V[i*ng+a] = l_a(x_i), Dv[i*ng+a] = l_a'(x_i) (geometry basis)
+  double V[90], Dv[90];   // V[i*ng+a] = l_a(x_i), Dv[i*ng+a] = l_a'(x_i) (geometry basis)
+  int nt;                 // target points per direction
   int ng;                 // geometry points per direction
   int general;            // 0: targets are the geometry nodes (J by the square D)
   int nf[3], s;           // axis spans in fine-mesh units (BoxStride)
@@ -125,7 +126,7 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
                                     double *__restrict__ JxW) {
   __shared__ double xyz[729 * 3];
   __shared__ double s1[3][9];  // sin(2 pi X) of the cell's node coordinates, per axis
-  const int n = b.degree + 1, n3 = n * n * n;
+  const int n = gp.nt, n3 = n * n * n;
   const int ng = gp.ng, ng3 = ng * ng * ng;
   const int64_t e = blockIdx.x;
   const int64_t cx = e % b.nx, cy = (e / b.nx) % b.ny, cz = e / ((int64_t)b.nx * b.ny);
@@ -241,7 +242,7 @@ void gauss_nodes(int n, double *x, double *w) {
 
 cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const double *gll_w,
                          const double *D, double *d_G, cudaStream_t s, bool at_gauss,
-                         const BoxStride *bs, double *d_JxW) {
+                         const BoxStride *bs, double *d_JxW, int n_gauss) {
   GeomParams gp{};
   if (bs && bs->s > 1) {
     for (int d = 0; d < 3; ++d) gp.nf[d] = bs->nf[d];
@@ -253,11 +254,12 @@ cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const doub
     gp.nf[0] = b.nx; gp.nf[1] = b.ny; gp.nf[2] = b.nz;
     gp.s = 1;
   }
-  const int n = b.degree + 1;
+  const int n = at_gauss && n_gauss > 0 ? n_gauss : b.degree + 1;
   const int g = b.geometry_degree > 0 ? b.geometry_degree : b.degree;
-  if (g < 1 || g > 8) return cudaErrorInvalidValue;
+  if (g < 1 || g > 8 || n > 10) return cudaErrorInvalidValue;
   gp.ng = g + 1;
-  double tx[9], tw[9];  // target points: the GLL points, or the Gauss points
+  gp.nt = n;
+  double tx[10], tw[10];  // target points: the GLL points, or the Gauss points
   if (at_gauss) gauss_nodes(n, tx, tw);
   else for (int i = 0; i < n; ++i) { tx[i] = gll_x[i]; tw[i] = gll_w[i]; }
   for (int i = 0; i < n; ++i) { gp.x[i] = tx[i]; gp.w[i] = tw[i]; }
@@ -362,61 +364,60 @@ cudaError_t diagonal_f64(int N, int64_t n_cells, const uint32_t *map, const doub
 // d phi / d xi_0 = (DG B)[i][a] B[j][b] B[k][c], etc.  One CTA per cell, one
 // thread per local DoF; G and JxW of the cell staged in shared memory.
 struct GaussDiagParams {
-  double B[81], DB[81];  // B[q*n + a], DB = DG B
+  double B[100], DB[100];  // B[q*n + a], DB = DG B  (q < nq, a < n)
 };
 
 __global__ void __launch_bounds__(256)
-    diagonal_gauss_kernel(int N, int64_t n_cells, const uint32_t *__restrict__ map,
+    diagonal_gauss_kernel(int N, int NQ, int64_t n_cells, const uint32_t *__restrict__ map,
                           const double *__restrict__ G, const double *__restrict__ JxW,
                           GaussDiagParams gp, double *__restrict__ diag) {
-  __shared__ double sG[6 * 729];
-  __shared__ double sW[729];
-  const int N2 = N * N, N3 = N2 * N;
+  const int N2 = N * N, N3 = N2 * N, NQ3 = NQ * NQ * NQ;
   for (int64_t e = blockIdx.x; e < n_cells; e += gridDim.x) {
-    for (int t = threadIdx.x; t < 6 * N3; t += blockDim.x) sG[t] = G[e * 6 * N3 + t];
-    for (int t = threadIdx.x; t < N3; t += blockDim.x) sW[t] = JxW ? JxW[e * N3 + t] : 0.0;
-    __syncthreads();
+    // every thread of the cell reads the same G and JxW entries (broadcast loads)
+    const double *Gc = G + e * 6 * NQ3;
+    const double *Wc = JxW ? JxW + e * NQ3 : nullptr;
     for (int l = threadIdx.x; l < N3; l += blockDim.x) {
       const uint32_t dof = map[e * N3 + l];
       if (dof == MFGB_INVALID_DOF) continue;
       const int a = l / N2, b = (l / N) % N, c = l % N;
       double acc = 0.0;
-      for (int i = 0; i < N; ++i) {
+      for (int i = 0; i < NQ; ++i) {
         const double bi = gp.B[i * N + a], di = gp.DB[i * N + a];
-        for (int j = 0; j < N; ++j) {
+        for (int j = 0; j < NQ; ++j) {
           const double bj = gp.B[j * N + b], dj = gp.DB[j * N + b];
-          for (int k = 0; k < N; ++k) {
+          for (int k = 0; k < NQ; ++k) {
             const double bk = gp.B[k * N + c], dk = gp.DB[k * N + c];
-            const int q = (i * N + j) * N + k;
+            const int q = (i * NQ + j) * NQ + k;
             const double r = di * bj * bk, s = bi * dj * bk, t = bi * bj * dk, ph = bi * bj * bk;
-            acc += sG[0 * N3 + q] * r * r + sG[3 * N3 + q] * s * s + sG[5 * N3 + q] * t * t +
-                   2.0 * (sG[1 * N3 + q] * r * s + sG[2 * N3 + q] * r * t + sG[4 * N3 + q] * s * t) +
-                   sW[q] * ph * ph;
+            acc += __ldg(Gc + q) * r * r + __ldg(Gc + 3 * NQ3 + q) * s * s +
+                   __ldg(Gc + 5 * NQ3 + q) * t * t +
+                   2.0 * (__ldg(Gc + NQ3 + q) * r * s + __ldg(Gc + 2 * NQ3 + q) * r * t +
+                          __ldg(Gc + 4 * NQ3 + q) * s * t) +
+                   (Wc ? __ldg(Wc + q) * ph * ph : 0.0);
           }
         }
       }
       atomicAdd(diag + dof, acc);
     }
-    __syncthreads();
   }
 }
 
-cudaError_t diagonal_gauss(int N, int64_t n_cells, const uint32_t *map, const double *G,
+cudaError_t diagonal_gauss(int N, int NQ, int64_t n_cells, const uint32_t *map, const double *G,
                            const double *JxW, const double *B, const double *DG, double *diag,
                            cudaStream_t s) {
-  if (N < 2 || N > 9) return cudaErrorInvalidValue;
+  if (N < 2 || N > 9 || NQ < N || NQ > 10) return cudaErrorInvalidValue;
   GaussDiagParams gp{};
-  for (int q = 0; q < N; ++q)
+  for (int q = 0; q < NQ; ++q)
     for (int a = 0; a < N; ++a) {
       gp.B[q * N + a] = B[q * N + a];
       double d = 0.0;
-      for (int m = 0; m < N; ++m) d += DG[q * N + m] * B[m * N + a];
+      for (int m = 0; m < NQ; ++m) d += DG[q * NQ + m] * B[m * N + a];
       gp.DB[q * N + a] = d;
     }
   if (n_cells == 0) return cudaSuccess;
   const int threads = std::min(256, ((N * N * N + 31) / 32) * 32);
   const unsigned grid = (unsigned)std::min<int64_t>(n_cells, 152 * 16);
-  diagonal_gauss_kernel<<<grid, threads, 0, s>>>(N, n_cells, map, G, JxW, gp, diag);
+  diagonal_gauss_kernel<<<grid, threads, 0, s>>>(N, NQ, n_cells, map, G, JxW, gp, diag);
   return cudaGetLastError();
 }
 

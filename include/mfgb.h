@@ -109,6 +109,12 @@ mfgb_status mfgb_operator_create_box_gauss(const mfgb_box_desc *box, mfgb_operat
    (the compute_diagonal of :218-251). */
 mfgb_status mfgb_operator_create_box_helmholtz(const mfgb_box_desc *box, mfgb_operator **op);
 
+/* BP3 on the same box mesh: the Laplacian at QGauss(p+2) on GLL nodal values
+   (the CEED BP3 quadrature; CEED_bp/include/bk3_kokkos_kernel.h:146-354 is the
+   reference's L-vector kernel for it, CEED_BK/include/kernels/BK3 its E-vector
+   form), G[cell][6][(p+2)^3].  mfgb_compute_diagonal gives its exact diagonal. */
+mfgb_status mfgb_operator_create_box_bp3(const mfgb_box_desc *box, mfgb_operator **op);
+
 /* Same, from caller-provided host arrays (the deal.II set-up path):
    h_dof_map[cell*(p+1)^3 + l] (0xFFFFFFFF = constrained), h_G[cell][6][(p+1)^3]
    in the order rr, rs, rt, ss, st, tt, and the list of constrained DoFs. */

@@ -105,3 +105,40 @@ def test_helmholtz_jacobi_pcg_counts(mf, orc):
     xr, info = ref.cg(b.cpu().numpy(), diag_inv=dinv)
     assert ctl.last_step() == info["steps"]
     assert rel(x.cpu().numpy(), xr) <= 1e-9
+
+
+@pytest.mark.parametrize("arith", ["fp64", "df"])
+@pytest.mark.parametrize("p", range(1, 9))
+def test_bp3_operator_matches_oracle(mf, orc, p, arith):
+    """BP3: the Laplacian at QGauss(p+2) (L-vector, gather/scatter through the
+    dof map) on a deformed box, against the oracle's Gauss problem with
+    nq = p + 2; the exact diagonal too."""
+    cells = (3, 2, 3) if p <= 5 else (2, 2, 2)
+    A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.07), arith=arith,
+                           quadrature="bp3")
+    ref = orc.GaussProblem(*cells, p, nq=p + 2, amplitude=0.07)
+    src = np.random.default_rng(p).uniform(-1, 1, ref.n_dofs)
+    y = A.initialize_dof_vector()
+    A.vmult(y, torch_from(src))
+    assert rel(y.cpu().numpy(), ref.apply(src)) <= 1e-12
+    if arith == "fp64":
+        dr = np.zeros(ref.n_dofs)
+        orc._gauss_sigs().orc_gauss_diagonal(ref.n, ref.nq, orc._p(ref.B), orc._p(ref.DG),
+                                             ref.n_cells, orc._p(ref.map), orc._p(ref.Gg), None,
+                                             ref.n_dofs, ref.constrained.size,
+                                             orc._p(ref.constrained), orc._p(dr))
+        assert rel(A.compute_diagonal().cpu().numpy(), dr) <= 1e-13
+
+
+def test_bp3_cg_counts_match_oracle(mf, orc):
+    mesh = mf.BoxMesh(4, 3, 3, degree=3, amplitude=0.05)
+    A = mf.LaplaceOperator(mesh, quadrature="bp3")
+    ref = orc.GaussProblem(4, 3, 3, 3, nq=5, amplitude=0.05)
+    b = A.rhs_uniform(4)
+    x = A.initialize_dof_vector()
+    ctl = mf.ReductionControl(1000, 1e-300, 1e-10)
+    mf.SolverCG(ctl).solve(A, x, b, A.get_matrix_diagonal_inverse())
+    dinv = 1.0 / A.compute_diagonal().cpu().numpy()
+    xr, info = ref.cg(b.cpu().numpy(), diag_inv=dinv, tol=1e-300, reduce=1e-10)
+    assert ctl.last_step() == info["steps"]
+    assert rel(x.cpu().numpy(), xr) <= 1e-9

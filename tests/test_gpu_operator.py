@@ -295,7 +295,7 @@ def test_autotune_small(mf, tmp_path):
 
 
 @pytest.mark.parametrize("arith", ["df", "fp64"])
-@pytest.mark.parametrize("form", ["gll", "gauss", "helmholtz"])
+@pytest.mark.parametrize("form", ["gll", "gauss", "helmholtz", "bp3"])
 def test_vmult_host_pipeline(mf, orc, form, arith):
     """The host-buffer apply (slab-pipelined copies) equals the device vmult, with
     the identity rows copied exactly, for several slab layouts and repeated calls."""
