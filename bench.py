@@ -149,6 +149,27 @@ def traffic_from_profile(arith: str):
     return None
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def cpu_reference_apply_rate(prob, steps, warmup, src):
     """Time the oracle's OpenMP vmult on the host cores; returns GDoF/s."""
     for _ in range(warmup):
@@ -180,6 +201,7 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded U[-1,1] src, deformed unit-cube mesh)",
         "config": config_dict(args, prob.n_dofs, prob.n_cells),
         "cpu_baseline": {"value": rate, "unit": "GDoF/s", "cores": cores, "kind": "port",
+                         "cpu_model": cpu_model(),
                          "sample": f"full workload, {steps} vmult on {prob.n_dofs} DoFs"},
         "e2e": {"value": rate, "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -301,6 +323,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         s_src = sample.rhs(w["seed"])
         rate, dt = cpu_reference_apply_rate(sample, 5, 1, s_src)
         cpu = {"value": rate, "unit": "GDoF/s", "cores": oracle.num_threads(), "kind": "port",
+               "cpu_model": cpu_model(),
                "sample": f"5 vmult of the oracle (OpenMP) on a {sample.nx}x{sample.ny}x{sample.nz}-"
                          f"cell p={w['degree']} mesh of the same deformed cube, "
                          f"{sample.n_dofs} DoFs"}

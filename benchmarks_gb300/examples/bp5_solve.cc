@@ -5,7 +5,10 @@
 // of vmult and a CG solve, print one row of the reference's convergence table
 // (cells dofs matvec CG_tot_time CG_time/iters cg_its cg_reduction).
 //
-// usage: bp5_solve nx ny nz [precond: none|jacobi|mg32|mg64] [reduce]
+// usage: bp5_solve nx ny nz [precond: none|jacobi|mg32|mg64|helmholtz] [reduce]
+//   helmholtz: bp5_kokkos's Helmholtz operator with Jacobi-PCG
+//   (bp5_kokkos/benchmark.cc:296-410); the table then describes that operator.
+// A last line compares the host-buffer apply (vmult_host) with the device one.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -47,12 +50,17 @@ int main(int argc, char **argv) {
     mfgb::ReductionControl control(1000000, 1e-300, reduce);
     mfgb::SolverCG cg(control);
     cudaDeviceSynchronize();
-    const auto t0 = Clock::now();
+    auto t0 = Clock::now();
     if (precond == "none") {
       cg.solve(A, x, b, mfgb::PreconditionIdentity());
     } else if (precond == "jacobi") {
       A.compute_diagonal();
       cg.solve(A, x, b, *A.get_matrix_diagonal_inverse());
+    } else if (precond == "helmholtz") {
+      mfgb::HelmholtzOperator<3, 4, double> H(box);
+      H.compute_diagonal();
+      t0 = Clock::now();
+      cg.solve(H, x, b, *H.get_matrix_diagonal_inverse());
     } else {
       mfgb::MGPreconditioner mg(box, precond == "mg32" ? 32 : 64);
       cg.solve(A, x, b, mg);
@@ -65,6 +73,24 @@ int main(int argc, char **argv) {
     std::printf("%lld %lld %.3e %.3e %.3e %d %.3e\n", (long long)A.n_cells(), (long long)A.m(),
                 best_mv, t_cg, its ? t_cg / its : 0.0, its, red);
     std::printf("GDoF/s %.3f\n", A.m() / best_mv * 1e-9);
+    // the host-buffer apply against the device apply (pinned host vectors)
+    double *hs = nullptr, *hd = nullptr;
+    const size_t bytes = sizeof(double) * A.m();
+    if (cudaMallocHost((void **)&hs, bytes) != cudaSuccess ||
+        cudaMallocHost((void **)&hd, bytes) != cudaSuccess)
+      throw mfgb::Error(MFGB_ERR_OUT_OF_MEMORY, "pinned host vectors");
+    cudaMemcpy(hs, b.get_values(), bytes, cudaMemcpyDeviceToHost);
+    A.vmult(y, b);
+    A.vmult_host(hd, hs);
+    cudaMemcpy(hs, y.get_values(), bytes, cudaMemcpyDeviceToHost);
+    double num = 0.0, den = 0.0;
+    for (int64_t i = 0; i < A.m(); ++i) {
+      num += (hd[i] - hs[i]) * (hd[i] - hs[i]);
+      den += hs[i] * hs[i];
+    }
+    std::printf("host_apply_rel_diff %.3e\n", std::sqrt(num / den));
+    cudaFreeHost(hs);
+    cudaFreeHost(hd);
   } catch (const mfgb::Error &e) {
     std::fprintf(stderr, "mfgb error %d: %s\n", e.status, e.what());
     return 2;

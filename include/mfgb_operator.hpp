@@ -125,6 +125,12 @@ class LaplaceOperatorBK35 {
     check(mfgb_vmult(op_.get(), dst.get_values(), src.get_values(), arith_, nullptr));
   }
   void Tvmult(DeviceVector &dst, const DeviceVector &src) const { vmult(dst, src); }
+  // host vectors (pinned for overlap): copies pipelined with the apply; returns
+  // after the result is in dst
+  void vmult_host(double *dst, const double *src) const {
+    check(mfgb_vmult_host(op_.get(), dst, src, arith_, nullptr));
+    check(mfgb_check_device_errors(nullptr));
+  }
   void initialize_dof_vector(DeviceVector &v) const { v.reinit(n_dofs_); }
   int64_t m() const { return n_dofs_; }
   int64_t n() const { return n_dofs_; }
@@ -142,6 +148,20 @@ class LaplaceOperatorBK35 {
   const mfgb_operator *handle() const { return op_.get(); }
   int arith() const { return arith_; }
 
+ protected:
+  struct FromHandle {};
+  LaplaceOperatorBK35(FromHandle, mfgb_operator *op, int arith) : arith_(arith) {
+    op_.reset(op);
+    check(mfgb_operator_info(op, &n_dofs_, &n_cells_, nullptr, nullptr));
+  }
+  static mfgb_operator *create(mfgb_status (*fn)(const mfgb_box_desc *, mfgb_operator **),
+                               mfgb_box_desc box) {
+    box.degree = fe_degree;
+    mfgb_operator *op = nullptr;
+    check(fn(&box, &op));
+    return op;
+  }
+
  private:
   struct Deleter {
     void operator()(mfgb_operator *p) const { mfgb_operator_destroy(p); }
@@ -150,6 +170,29 @@ class LaplaceOperatorBK35 {
   int64_t n_dofs_ = 0, n_cells_ = 0;
   int arith_;
   std::shared_ptr<DiagonalMatrix> inverse_diagonal_;
+};
+
+// Step64::HelmholtzOperator of bp5_kokkos (benchmark.cc:141-251): mass +
+// stiffness at QGauss(p+1), same interface (vmult, compute_diagonal,
+// get_matrix_diagonal_inverse, ...)
+template <int dim, int fe_degree, typename number = double>
+class HelmholtzOperator : public LaplaceOperatorBK35<dim, fe_degree, number> {
+  using Base = LaplaceOperatorBK35<dim, fe_degree, number>;
+
+ public:
+  explicit HelmholtzOperator(mfgb_box_desc box, int arith = MFGB_ARITH_FP64_DF)
+      : Base(typename Base::FromHandle{}, Base::create(mfgb_operator_create_box_helmholtz, box),
+             arith) {}
+};
+
+// The BP3 Laplacian (QGauss(p+2) on GLL nodal values)
+template <int dim, int fe_degree, typename number = double>
+class LaplaceOperatorBP3 : public LaplaceOperatorBK35<dim, fe_degree, number> {
+  using Base = LaplaceOperatorBK35<dim, fe_degree, number>;
+
+ public:
+  explicit LaplaceOperatorBP3(mfgb_box_desc box, int arith = MFGB_ARITH_FP64_DF)
+      : Base(typename Base::FromHandle{}, Base::create(mfgb_operator_create_box_bp3, box), arith) {}
 };
 
 // V-cycle preconditioner (mfgb_mg_*), FP32 or FP64

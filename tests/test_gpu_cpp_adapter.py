@@ -44,6 +44,26 @@ def test_cpp_adapter_matches_python_api(example):
     assert 0 < its_mg < 30
 
 
+def test_cpp_adapter_helmholtz_and_host_apply(example):
+    """mfgb::HelmholtzOperator (bp5_kokkos's operator) with Jacobi-PCG through the
+    adapter gives the Python API's iteration count; the host-buffer apply
+    equals the device apply."""
+    import benchmarks_gb300 as mf
+    out = subprocess.run([example, "6", "6", "4", "helmholtz", "1e-8"], capture_output=True,
+                         text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    its = int(lines[1].split()[5])
+    diff = float(lines[-1].split()[1])
+    assert lines[-1].startswith("host_apply_rel_diff") and diff <= 1e-14
+    H = mf.HelmholtzOperator(mf.BoxMesh(6, 6, 4, degree=4, amplitude=0.05))
+    b = H.rhs_uniform(1)
+    x = H.initialize_dof_vector()
+    ctl = mf.ReductionControl(1000000, 1e-300, 1e-8)
+    mf.SolverCG(ctl).solve(H, x, b, H.get_matrix_diagonal_inverse())
+    assert its == ctl.last_step()
+
+
 def test_cpp_adapter_reports_errors(example):
     out = subprocess.run([example, "0", "1", "1"], capture_output=True, text=True, timeout=60)
     assert out.returncode == 2 and "invalid argument" in out.stderr
