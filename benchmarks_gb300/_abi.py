@@ -78,6 +78,7 @@ def lib():
         "mfgb_vmult_add": ([P, P, P, I32, P], I32),
         "mfgb_vmult_f32": ([P, P, P, P], I32),
         "mfgb_vmult_host": ([P, P, P, I32, P], I32),
+        "mfgb_set_host_pipeline": ([I32], I32),
         "mfgb_vmult_vector": ([P, P, P, I32, I32, P], I32),
         "mfgb_copy_constrained": ([P, P, P, P], I32),
         "mfgb_bk5_lvector": ([I32, I64, P, P, P, P, P, I32, P], I32),

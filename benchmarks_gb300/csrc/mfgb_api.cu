@@ -524,6 +524,17 @@ mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, 
   return cuda_status(e, "mfgb_bk5_evector");
 }
 
+static int g_host_slabs = 0;  // slabs of the host-buffer pipeline (0: automatic)
+
+mfgb_status mfgb_set_host_pipeline(int slabs) {
+  if (slabs < 0 || slabs > 64) {
+    set_error("mfgb_set_host_pipeline: slabs must be 0 (automatic) .. 64");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  g_host_slabs = slabs;
+  return MFGB_OK;
+}
+
 // vmult on host vectors, pipelined over z-slabs of cells on three streams:
 // H2D of the DoF planes a slab adds -> the slab's cells -> D2H of the planes it
 // completes (identity rows applied), while the next slab's planes arrive.
@@ -551,9 +562,11 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
         return cuda_status(cudaErrorUnknown, "mfgb_vmult_host: streams");
   const int p = op->degree;
   const int nz = op->is_box ? op->box.nz : 1;
-  const int S = op->is_box ? std::max(1, std::min(16, nz / 2)) : 1;  // >= 2 cell layers a slab
+  // >= 2 cell layers a slab; 16 slabs unless set by mfgb_set_host_pipeline
+  const int want = g_host_slabs > 0 ? g_host_slabs : 16;
+  const int S = op->is_box ? std::max(1, std::min(want, nz / 2)) : 1;
   const int Lz = (nz + S - 1) / S;
-  const int n_ev = 3 * S + 1;
+  const int n_ev = 3 * S + 1;  // S <= 64
   while ((int)op->pipe_ev.size() < n_ev) {
     cudaEvent_t e;
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)

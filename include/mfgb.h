@@ -204,6 +204,9 @@ mfgb_status mfgb_bk3_evector(int degree, int64_t nelmt, const double *d_basis,
    keeps two device vectors for this call after the first use. */
 mfgb_status mfgb_vmult_host(const mfgb_operator *op, double *h_dst, const double *h_src, int arith,
                             void *stream);
+/* number of z-slabs of that pipeline (1..64; 0 = automatic: 16, each slab at
+   least two cell layers) */
+mfgb_status mfgb_set_host_pipeline(int slabs);
 
 /* ---- diagonal -------------------------------------------------------------
  * compute_diagonal (bp5_kokkos/benchmark.cc:218-251): exact diagonal of the
