@@ -183,6 +183,21 @@ class LaplaceOperator:
         self._inv_diag = DiagonalMatrix(inv)
         return d
 
+    def vmult_dummy(self, dst, src, ghost_exchange_on=True, computation_on=True):
+        """``vmult_dummy`` of the reference operator (portable_laplace_operator_bk35.h:
+        170-225): ``computation_on`` runs dst = 0 and the cell loop,
+        ``ghost_exchange_on`` the identity rows (the exchange itself is a no-op on
+        one GPU)."""
+        n = self._n_dofs
+        if computation_on:
+            dst.zero_()
+            _abi.check(lib().mfgb_vmult_add(self._op, _check_vec(dst, n, "dst"),
+                                            _check_vec(src, n, "src"), self.arith, _stream_ptr()))
+        if ghost_exchange_on:
+            _abi.check(lib().mfgb_copy_constrained(self._op, _check_vec(dst, n, "dst"),
+                                                   _check_vec(src, n, "src"), _stream_ptr()))
+        return dst
+
     def vmult_host(self, dst, src, arith=None):
         """dst = A src on host (CPU, ideally pinned) float64 tensors; the copies
         are pipelined with the apply (``mfgb_vmult_host``)."""
@@ -271,15 +286,24 @@ class MGPreconditioner:
     CG), 64 in FP64."""
 
     def __init__(self, mesh: BoxMesh, precision=32, chebyshev_degree=5, smoothing_range=15.0,
-                 eig_iterations=20, coarse_cells=4, coarse_tol=1e-12):
+                 eig_iterations=20, coarse_cells=4, coarse_tol=1e-12, operator=None):
+        """``operator``: the LaplaceOperator of the same mesh; the finest level then
+        borrows it (no second geometry set-up) and keeps a reference to it."""
         self.mesh = mesh
         self.precision = precision
         self._mg = ctypes.c_void_p()
         prm = _abi.MgParams(precision, chebyshev_degree, smoothing_range, eig_iterations,
                             coarse_cells, coarse_tol)
-        desc = mesh._desc()
-        _abi.check(lib().mfgb_mg_setup(ctypes.byref(desc), ctypes.byref(prm),
-                                       ctypes.byref(self._mg)))
+        if operator is not None:
+            if operator.mesh is None or operator.mesh != mesh or operator.quadrature != "gll":
+                raise ValueError("operator must be the GLL LaplaceOperator of the same mesh")
+            self._operator = operator  # outlives the hierarchy
+            _abi.check(lib().mfgb_mg_setup_shared(operator.handle, ctypes.byref(prm),
+                                                  ctypes.byref(self._mg)))
+        else:
+            desc = mesh._desc()
+            _abi.check(lib().mfgb_mg_setup(ctypes.byref(desc), ctypes.byref(prm),
+                                           ctypes.byref(self._mg)))
         nl = ctypes.c_int()
         _abi.check(lib().mfgb_mg_info(self._mg, ctypes.byref(nl), None, None, None))
         dofs = (ctypes.c_int64 * nl.value)()

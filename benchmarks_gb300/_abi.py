@@ -100,6 +100,7 @@ def lib():
         "mfgb_mlp_forward_f32": ([P, P, I32, P], I32),
         "mfgb_mlp_infer": ([P, P, I64, P, P], I32),
         "mfgb_mg_setup": ([ctypes.POINTER(BoxDesc), ctypes.POINTER(MgParams), PP], I32),
+        "mfgb_mg_setup_shared": ([P, ctypes.POINTER(MgParams), PP], I32),
         "mfgb_mg_destroy": ([P], I32),
         "mfgb_mg_info": ([P, P, P, P, P], I32),
         "mfgb_mg_vmult": ([P, P, P, P], I32),

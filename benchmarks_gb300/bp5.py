@@ -65,7 +65,7 @@ def main(argv=None):
     else:
         A, t_setup = timed(lambda: mf.LaplaceOperator(mesh, arith=a.arith))
     if a.solver in ("mg32", "mg64"):
-        P, t_pre = timed(lambda: mf.MGPreconditioner(mesh, precision=int(a.solver[2:])))
+        P, t_pre = timed(lambda: mf.MGPreconditioner(mesh, precision=int(a.solver[2:]), operator=A))
     elif a.solver in ("jacobi", "helmholtz"):
         P, t_pre = timed(A.get_matrix_diagonal_inverse)
     else:

@@ -408,7 +408,7 @@ void free_mg(mfgb_mg *mg) {
   for (auto &L : mg->levels) {
     cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.d); cudaFree(L.t);
     cudaFree(L.inv_diag); cudaFree(L.inv_val);
-    if (L.op) mfgb_operator_destroy(L.op);
+    if (L.op && !L.borrowed) mfgb_operator_destroy(L.op);
   }
   cudaFree(mg->coarse.A); cudaFree(mg->coarse.dinv); cudaFree(mg->coarse.work);
   cudaFree(mg->coarse.ids);
@@ -422,8 +422,30 @@ void free_mg(mfgb_mg *mg) {
 
 using namespace mfgb;
 
+static mfgb_status mg_setup_impl(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
+                                 mfgb_mg **out, mfgb_operator *fine_op);
+
 extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
                                      mfgb_mg **out) {
+  return mg_setup_impl(fine, prm, out, nullptr);
+}
+
+// The finest level borrows the caller's operator (its geometric factors are
+// not computed a second time); the operator must outlive the hierarchy.
+extern "C" mfgb_status mfgb_mg_setup_shared(const mfgb_operator *fine_op,
+                                            const mfgb_mg_params *prm, mfgb_mg **out) {
+  if (!fine_op || !fine_op->is_box || fine_op->quadrature != 0 ||
+      fine_op->n_dofs != ((int64_t)fine_op->degree * fine_op->box.nx + 1) *
+                             ((int64_t)fine_op->degree * fine_op->box.ny + 1) *
+                             ((int64_t)fine_op->degree * fine_op->box.nz + 1)) {
+    set_error("mfgb_mg_setup_shared: needs a GLL-collocated box operator");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return mg_setup_impl(&fine_op->box, prm, out, const_cast<mfgb_operator *>(fine_op));
+}
+
+static mfgb_status mg_setup_impl(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
+                                 mfgb_mg **out, mfgb_operator *fine_op) {
   if (!fine || !prm || !out || (prm->precision != 32 && prm->precision != 64) ||
       prm->chebyshev_degree < 1 || prm->smoothing_range <= 1.0 || prm->eig_iterations < 1 ||
       prm->coarse_cells < 1) {
@@ -447,7 +469,13 @@ extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_pa
     L.box = boxes[l];
     L.to_coarse = kinds[l];
     L.bs = BoxStride{{fine->nx, fine->ny, fine->nz}, strides[l]};
-    st = create_box_strided(&boxes[l], &L.bs, &L.op);
+    if (l == 0 && fine_op && (fine_op->box.geometry_degree == 0 ||
+                              fine_op->box.geometry_degree == boxes[0].geometry_degree)) {
+      L.op = fine_op;  // the same box, degree and geometry interpolant
+      L.borrowed = true;
+    } else {
+      st = create_box_strided(&boxes[l], &L.bs, &L.op);
+    }
     if (st) break;
     L.n = L.op->n_dofs;
     mg->levels.push_back(L);

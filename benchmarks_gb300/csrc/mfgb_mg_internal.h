@@ -17,6 +17,7 @@ struct MgLevel {
   void *inv_val = nullptr;   // 1/valence (precision T), for p-restriction from this level
   double lmax = 0;
   int to_coarse = 0;  // 1 = p-transfer, 2 = h-transfer, 0 = coarsest
+  bool borrowed = false;  // op belongs to the caller (mfgb_mg_setup_shared)
 };
 
 struct MgCoarse {

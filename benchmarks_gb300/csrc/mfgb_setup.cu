@@ -191,15 +191,16 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
     const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
     const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
     double Ji[3][3];
-    Ji[0][0] = c00 / det;
-    Ji[1][0] = c01 / det;
-    Ji[2][0] = c02 / det;
-    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
-    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
-    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
-    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
-    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
-    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    const double id = 1.0 / det;  // one FP64 division per point
+    Ji[0][0] = c00 * id;
+    Ji[1][0] = c01 * id;
+    Ji[2][0] = c02 * id;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
     const double jxw = fabs(det) * gp.w[i] * gp.w[j] * gp.w[k];
     if (JxW) JxW[e * n3 + l] = jxw;
     double *Gc = G + e * 6 * n3 + l;

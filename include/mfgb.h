@@ -266,6 +266,11 @@ typedef struct {
 } mfgb_mg_params;
 
 mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_params *params, mfgb_mg **mg);
+/* the same, with the finest level borrowing the caller's box operator (created
+   by mfgb_operator_create_box; no second geometry set-up); the operator must
+   outlive the hierarchy */
+mfgb_status mfgb_mg_setup_shared(const mfgb_operator *fine_op, const mfgb_mg_params *params,
+                                 mfgb_mg **mg);
 mfgb_status mfgb_mg_destroy(mfgb_mg *mg);
 /* level sizes (h_* arrays of n_levels entries, any may be NULL) */
 mfgb_status mfgb_mg_info(const mfgb_mg *mg, int *n_levels, int64_t *h_dofs, int *h_degree,

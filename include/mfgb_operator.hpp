@@ -125,6 +125,19 @@ class LaplaceOperatorBK35 {
     check(mfgb_vmult(op_.get(), dst.get_values(), src.get_values(), arith_, nullptr));
   }
   void Tvmult(DeviceVector &dst, const DeviceVector &src) const { vmult(dst, src); }
+  // vmult_dummy (portable_laplace_operator_bk35.h:170-225): computation_on runs
+  // dst = 0 and the cell loop; ghost_exchange_on does the single-GPU part of the
+  // exchange, the identity rows (compress and the ghost update are no-ops here)
+  void vmult_dummy(DeviceVector &dst, const DeviceVector &src, bool ghost_exchange_on,
+                   bool computation_on) const {
+    if (computation_on) {
+      if (cudaMemset(dst.get_values(), 0, sizeof(double) * dst.locally_owned_size()) != cudaSuccess)
+        throw Error(MFGB_ERR_CUDA, "vmult_dummy: dst = 0");
+      check(mfgb_vmult_add(op_.get(), dst.get_values(), src.get_values(), arith_, nullptr));
+    }
+    if (ghost_exchange_on)
+      check(mfgb_copy_constrained(op_.get(), dst.get_values(), src.get_values(), nullptr));
+  }
   // host vectors (pinned for overlap): copies pipelined with the apply; returns
   // after the result is in dst
   void vmult_host(double *dst, const double *src) const {

@@ -138,3 +138,32 @@ def test_odd_mesh_mg_cg_converges_fast(mf, n):
     mf.SolverCG(ctl).solve(A, x, b, M)
     assert ctl.last_value() <= 1e-10 * ctl.initial_value()
     assert ctl.last_step() <= 25
+
+
+def test_shared_fine_operator(mf):
+    """mfgb_mg_setup_shared: the finest level borrows the caller's operator; the
+    hierarchy, the V-cycle and the solve match the stand-alone set-up."""
+    mesh = mf.BoxMesh(8, 8, 4, degree=4, amplitude=0.1)
+    A = mf.LaplaceOperator(mesh)
+    M0 = mf.MGPreconditioner(mesh, precision=32)
+    M1 = mf.MGPreconditioner(mesh, precision=32, operator=A)
+    assert [l["dofs"] for l in M0.levels] == [l["dofs"] for l in M1.levels]
+    for a, b in zip(M0.levels, M1.levels):
+        assert a["lambda_max"] == pytest.approx(b["lambda_max"], rel=1e-6)
+    r = A.rhs_uniform(9)
+    z0, z1 = A.initialize_dof_vector(), A.initialize_dof_vector()
+    M0.vmult(z0, r)
+    M1.vmult(z1, r)
+    assert rel(z1.cpu().numpy(), z0.cpu().numpy()) <= 1e-5
+    its = []
+    for M in (M0, M1):
+        x = A.initialize_dof_vector()
+        ctl = mf.ReductionControl(200, 1e-300, 1e-10)
+        mf.SolverCG(ctl).solve(A, x, r, M)
+        its.append(ctl.last_step())
+    assert its[0] == its[1]
+    del M1
+    y = A.initialize_dof_vector()
+    A.vmult(y, r)  # the operator survives the hierarchy
+    with pytest.raises(ValueError):
+        mf.MGPreconditioner(mf.BoxMesh(8, 8, 2, degree=4), operator=A)

@@ -327,3 +327,20 @@ def test_vmult_host_array_operator(mf, orc):
     A.vmult_host(h_dst, torch.from_numpy(src).pin_memory())
     torch.cuda.synchronize()
     assert rel(h_dst.numpy(), ref.apply(src)) <= 1e-12
+
+
+def test_vmult_dummy(mf):
+    """vmult_dummy(ghost_on, compute_on) composes to vmult; compute alone leaves
+    the constrained rows at the cell-loop value, ghost alone only sets them."""
+    import torch
+    A = mf.LaplaceOperator(mf.BoxMesh(3, 3, 3, degree=2, amplitude=0.05))
+    src = A.rhs_uniform(2) + 1.0
+    want = A.initialize_dof_vector()
+    A.vmult(want, src)
+    y = A.initialize_dof_vector()
+    A.vmult_dummy(y, src, True, True)
+    assert torch.equal(y, want) or float(torch.linalg.norm(y - want)) <= 1e-14 * float(torch.linalg.norm(want))
+    z = A.initialize_dof_vector()
+    A.vmult_dummy(z, src, False, True)
+    A.vmult_dummy(z, src, True, False)
+    assert float(torch.linalg.norm(z - want)) <= 1e-14 * float(torch.linalg.norm(want))
