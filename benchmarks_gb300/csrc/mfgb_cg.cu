@@ -459,11 +459,8 @@ static mfgb_status noalloc_apply(const mfgb_operator *op, double *dst, const dou
     e = bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s, done);
   else if (op->d_Gdf)
     e = bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s, done);
-  else if (partials)
-    e = bk5_df_g64_energy(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid,
-                          s, done);
   else
-    e = bk5_df_g64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, s);
+    e = bk5_df_g64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, s, done);
   if ((st = cuda_status(e, "bk5 kernel"))) return st;
   if (full)
     return cuda_status(copy_constrained(op->n_constrained, op->d_constrained, src, dst, s),

@@ -58,11 +58,8 @@ cudaError_t bk5_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G,
                    double *dst, const double *D, double *partials, int *grid, cudaStream_t s,
                     const int *done = nullptr);
 cudaError_t bk5_df_g64(int N, int64_t n_cells, const uint32_t *map, const double *G,
-                       const double *src, double *dst, const double *D, cudaStream_t s);
-// double-float on FP64 G with per-CTA energy partials (no double-float copy of G needed)
-cudaError_t bk5_df_g64_energy(int N, int64_t n_cells, const uint32_t *map, const double *G,
-                              const double *src, double *dst, const double *D, double *partials,
-                              int *grid, cudaStream_t s, const int *done);
+                       const double *src, double *dst, const double *D, cudaStream_t s,
+                       const int *done = nullptr);
 cudaError_t bk5_f32(int N, int64_t n_cells, const uint32_t *map, const float *G, const float *src,
                     float *dst, const double *D, double *partials, int *grid, cudaStream_t s,
                     const int *done = nullptr);
