@@ -16,6 +16,11 @@ template <> struct ElemsPerCta<7> { static constexpr int value = 4; };
 template <> struct ElemsPerCta<8> { static constexpr int value = 2; };
 template <> struct ElemsPerCta<9> { static constexpr int value = 2; };
 
+// bulk-TMA column kernel: elements per CTA, per arithmetic (default: as the
+// column kernel)
+template <int N, class A> struct ElemsPerCtaTma { static constexpr int value = ElemsPerCta<N>::value; };
+template <> struct ElemsPerCtaTma<5, ArithF32> { static constexpr int value = 6; };
+
 // point-per-thread kernel: elements per CTA (CTA = E * N^3 threads)
 template <int N> struct ElemsPerCtaPt;
 template <> struct ElemsPerCtaPt<2> { static constexpr int value = 32; };
@@ -72,7 +77,7 @@ int bk5_grid(int64_t n_cells, int shape) {
     E = ElemsPerCtaPt<N>::value;
     if (ps < 0) ps = ctas_per_sm(bk5_pt_kernel<N, ElemsPerCtaPt<N>::value, A, EVEC, EN>, E * N * N * N, 0);
   } else if (shape == SHAPE_TMA) {
-    constexpr int ET = ElemsPerCta<N>::value;
+    constexpr int ET = ElemsPerCtaTma<N, A>::value;
     E = ET;
     if (ps < 0)
       ps = ctas_per_sm(bk5_tma_kernel<N, ET, A, EN>, ET * N * N, TmaLayout<N, ET, A>::total);
@@ -111,7 +116,7 @@ cudaError_t bk5_launch(int64_t n_cells, const uint32_t *map, const typename A::G
         n_cells, map, G, src, dst, basis, partials, done_flag);
   } else if (shape == SHAPE_TMA) {
     if constexpr (!EVEC) {
-      constexpr int E = ElemsPerCta<N>::value;
+      constexpr int E = ElemsPerCtaTma<N, A>::value;
       bk5_tma_kernel<N, E, A, EN><<<grid, E * N * N, TmaLayout<N, E, A>::total, stream>>>(
           n_cells, map, G, src, dst, basis, partials, done_flag, device_error_flag());
     }
