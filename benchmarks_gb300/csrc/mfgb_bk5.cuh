@@ -316,9 +316,12 @@ struct TmaLayout {
 // err_flag (may be null) records a TMA wait that exceeded its time limit.
 template <int N, class A> struct TmaMinBlocks { static constexpr int value = N <= 6 ? 2 : 1; };
 // FP32 at N = 4, 5: the compiler's 86 / 107 registers leave 2-3 CTAs per SM
-// (N = 5 runs 6 cells per CTA, ElemsPerCtaTma: 0.62 -> 0.54 ms at 2.95e7 DoFs)
+// (N = 5 runs 6 cells per CTA, ElemsPerCtaTma: 0.62 -> 0.54 ms at 2.95e7 DoFs).
+// Double-float at N = 5 runs 5 cells per CTA (125 threads, 4 CTAs per SM by
+// registers and shared memory): 3.76 -> 3.06 ms at 67.6M DoFs.
 template <> struct TmaMinBlocks<4, ArithF32> { static constexpr int value = 4; };
 template <> struct TmaMinBlocks<5, ArithF32> { static constexpr int value = 6; };
+template <> struct TmaMinBlocks<5, ArithDF> { static constexpr int value = 4; };
 
 template <int N, int E, class A, bool WITH_ENERGY>
 __global__ void __launch_bounds__(E * N * N, (TmaMinBlocks<N, A>::value))

@@ -20,6 +20,7 @@ template <> struct ElemsPerCta<9> { static constexpr int value = 2; };
 // column kernel)
 template <int N, class A> struct ElemsPerCtaTma { static constexpr int value = ElemsPerCta<N>::value; };
 template <> struct ElemsPerCtaTma<5, ArithF32> { static constexpr int value = 6; };
+template <> struct ElemsPerCtaTma<5, ArithDF> { static constexpr int value = 5; };
 
 // point-per-thread kernel: elements per CTA (CTA = E * N^3 threads)
 template <int N> struct ElemsPerCtaPt;
