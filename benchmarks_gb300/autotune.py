@@ -2,7 +2,9 @@
 launch shape is a compile-time choice: CEED_BK/src/BK5/templated_cuda_benchmark.cc:114-124).
 
 For each (arithmetic, degree) it times every thread layout the library has
-(0 column, 1 point-per-thread, 2 column with bulk-TMA prefetch) on a
+(0 column, 1 point-per-thread, 2 column with bulk-TMA prefetch, 3 and 4 the
+column and bulk-TMA kernels at an alternative number of cells per thread block,
+i.e. the elements-per-block choice) on a
 representative deformed box mesh with CUDA events, and installs the fastest in
 the library's shape table (``mfgb_set_kernel_shape``).  Results can be saved
 to and loaded from a small JSON file.
@@ -16,7 +18,7 @@ from . import _abi
 from ._abi import lib
 
 ARITHS = {"fp64": 0, "df": 1, "fp32": 2}
-SHAPES = (0, 1, 2)
+SHAPES = (0, 1, 2, 3, 4)
 
 
 def _mesh_for(degree, target_dofs):

@@ -103,12 +103,13 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
 }
 
 // kernel shape per (arithmetic class, N): 0 column, 1 point-per-thread,
-// 2 column with TMA-prefetched geometric factors.  Defaults are the fastest
+// 2 column with TMA-prefetched geometric factors, 3 / 4 the column / TMA
+// kernels at the alternative cells per CTA (AltElems).  Defaults are the fastest
 // shape per degree measured on a GB300 at ~3e7 DoFs (autotune.py re-measures).
 static int g_shape[3][10] = {
-    {0, 0, 2, 2, 2, 1, 2, 1, 2, 1},  // FP64
-    {2, 2, 2, 2, 2, 2, 0, 2, 2, 2},  // double-float
-    {0, 0, 0, 0, 0, 0, 2, 0, 2, 2},  // FP32
+    {0, 0, 4, 3, 2, 4, 2, 1, 2, 1},  // FP64
+    {2, 2, 2, 4, 2, 4, 0, 2, 2, 2},  // double-float
+    {0, 0, 3, 3, 0, 3, 2, 4, 4, 2},  // FP32
 };
 
 // device-side error word (a TMA wait that ran out of time), one per device
@@ -200,7 +201,7 @@ const char *mfgb_last_error(void) { return g_last_error.c_str(); }
 int mfgb_version(void) { return 1; }
 
 mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape) {
-  if (arith < 0 || arith > 2 || degree < 1 || degree > 8 || shape < 0 || shape > 2) {
+  if (arith < 0 || arith > 2 || degree < 1 || degree > 8 || shape < 0 || shape > 4) {
     set_error("mfgb_set_kernel_shape: invalid argument");
     return MFGB_ERR_INVALID_ARG;
   }

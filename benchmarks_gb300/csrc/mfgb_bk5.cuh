@@ -158,6 +158,17 @@ __global__ void __launch_bounds__(E * N * N)
                                               done_flag);
 }
 
+// the same with an explicit residency (register cap) of MB CTAs per SM
+template <int N, int E, class A, bool EVEC, bool WITH_ENERGY, int MB>
+__global__ void __launch_bounds__(E * N * N, MB)
+    bk5_kernel_mb(const int64_t n_cells, const uint32_t *__restrict__ map,
+                  const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+                  typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
+                  double *__restrict__ energy_partials, const int *__restrict__ done_flag) {
+  bk5_column_body<N, E, A, EVEC, WITH_ENERGY>(n_cells, map, G, src, dst, basis, energy_partials,
+                                              done_flag);
+}
+
 // the same with the register cap of ColumnMinBlocks
 template <int N, int E, class A, bool EVEC, bool WITH_ENERGY>
 __global__ void __launch_bounds__(E * N * N, (ColumnMinBlocks<N, A>::value > 0
@@ -301,7 +312,10 @@ struct TmaLayout {
   static constexpr size_t map_bytes = ((size_t)E * N3 * 4 + 15) / 16 * 16;
   static constexpr size_t work_bytes = 3 * sizeof(typename A::V) * E * N3;
   static constexpr size_t total = g_bytes + map_bytes + work_bytes + 16;
+  // tiles start at batch * (full tile): bulk copies only when every full tile
+  // is a 16-byte multiple (then every batch's start is 16-byte aligned)
   static constexpr bool map_tma = (E * N3 * 4) % 16 == 0;
+  static constexpr bool g_tma = g_bytes % 16 == 0;
 };
 
 // Column kernel with bulk-TMA prefetch.  Per batch b of E cells:
@@ -323,8 +337,8 @@ template <> struct TmaMinBlocks<4, ArithF32> { static constexpr int value = 4; }
 template <> struct TmaMinBlocks<5, ArithF32> { static constexpr int value = 6; };
 template <> struct TmaMinBlocks<5, ArithDF> { static constexpr int value = 4; };
 
-template <int N, int E, class A, bool WITH_ENERGY>
-__global__ void __launch_bounds__(E * N * N, (TmaMinBlocks<N, A>::value))
+template <int N, int E, class A, bool WITH_ENERGY, int MB = TmaMinBlocks<N, A>::value>
+__global__ void __launch_bounds__(E * N * N, MB)
     bk5_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
                    const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
                    typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
@@ -366,9 +380,12 @@ __global__ void __launch_bounds__(E * N * N, (TmaMinBlocks<N, A>::value))
 
   auto cells_of = [&](int64_t b) { return (int)min((int64_t)E, n_cells - b * E); };
   auto map_by_tma = [&](int cells) { return L::map_tma && ((cells * N3 * 4) % 16 == 0); };
-  // a bulk copy needs a 16-byte multiple: 4-byte G tiles of an odd number of
-  // cells with odd N^3 (possible only in the last batch) are loaded by plain loads
-  auto g_by_tma = [&](int cells) { return (sizeof(GT) * cells * 6 * N3) % 16 == 0; };
+  // a bulk copy needs a 16-byte aligned start and a 16-byte multiple: 4-byte G
+  // tiles of an odd number of cells with odd N^3 (an odd E, or the last batch)
+  // are loaded by plain loads
+  auto g_by_tma = [&](int cells) {
+    return L::g_tma && (sizeof(GT) * cells * 6 * N3) % 16 == 0;
+  };
   auto issue_g = [&](int64_t b) {  // one thread; completes the phase either way
     const int cells = cells_of(b);
     const uint32_t gb = g_by_tma(cells) ? (uint32_t)(sizeof(GT) * cells * 6 * N3) : 0u;

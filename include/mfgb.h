@@ -73,8 +73,10 @@ typedef struct {
 
 /* Thread layout of the operator kernel for (arith, degree): 0 = one thread per
    (j,k) column of an element, 1 = one thread per quadrature point, 2 = columns
-   with the geometric factors prefetched by bulk TMA copies.  The
-   library starts from a built-in table; the autotuner overrides it.  No
+   with the geometric factors prefetched by bulk TMA copies, 3 / 4 = shapes 0 /
+   2 at an alternative number of cells per thread block (the autotuner's
+   elements-per-block choice).  The library starts from a built-in table; the
+   autotuner overrides it.  No
    counterpart in the reference (its launch shape is a compile-time choice,
    CEED_BK/src/BK5/templated_cuda_benchmark.cc:114-124). */
 mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape);

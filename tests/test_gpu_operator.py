@@ -190,7 +190,7 @@ def test_full_size_properties(mf):
     torch.cuda.empty_cache()
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2])
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("arith", ["fp64", "df"])
 @pytest.mark.parametrize("p", [1, 2, 4, 5, 7, 8])
 def test_every_kernel_shape_matches_oracle(mf, orc, shape, arith, p):
@@ -248,8 +248,9 @@ def torch_zeros(n):
     return torch.zeros(n, dtype=torch.float64, device="cuda")
 
 
-@pytest.mark.parametrize("p", [2, 4, 8])
-def test_fp32_tma_tail_batch(mf, orc, p):
+@pytest.mark.parametrize("shape", [0, 2, 3, 4])
+@pytest.mark.parametrize("p", [2, 4, 5, 8])
+def test_fp32_tma_tail_batch(mf, orc, p, shape):
     """FP32 geometric factors in an odd last batch (a 4-byte tile that is not a
     16-byte multiple) go through plain loads: correct result, no timeout."""
     import ctypes
@@ -259,7 +260,7 @@ def test_fp32_tma_tail_batch(mf, orc, p):
     old = ctypes.c_int()
     _abi.check(L.mfgb_get_kernel_shape(2, p, ctypes.byref(old)))
     try:
-        _abi.check(L.mfgb_set_kernel_shape(2, p, 2))
+        _abi.check(L.mfgb_set_kernel_shape(2, p, shape))
         cells = (3, 3, 3)  # 27 cells: odd last batch for every batch size
         A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.1))
         ref = orc.BoxProblem(*cells, p, amplitude=0.1)
@@ -287,7 +288,7 @@ def test_autotune_small(mf, tmp_path):
     assert after.value == before.value
     for name in ("df", "fp32"):
         e = r[name][3]
-        assert e["best"] in autotune.SHAPES and len(e["ms"]) == 3 and min(e["ms"]) > 0
+        assert e["best"] in autotune.SHAPES and len(e["ms"]) == len(autotune.SHAPES) and min(e["ms"]) > 0
     path = tmp_path / "tune.json"
     autotune.save(r, path)
     r2 = autotune.load(path, apply=False)
