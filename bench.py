@@ -208,6 +208,10 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# operator kernel thread layouts (mfgb_set_kernel_shape)
+SHAPE_CODES = {"column": 0, "point": 1, "tma": 2, "column_alt": 3, "tma_alt": 4}
+
+
 def is_headline():
     return (WORKLOAD["nx"], WORKLOAD["ny"], WORKLOAD["nz"], WORKLOAD["degree"]) == (128, 128, 64, 4)
 
@@ -236,7 +240,7 @@ def run_ours(args, rank, world):
     w = WORKLOAD
     if args.shape != "auto":
         _abi.check(L.mfgb_set_kernel_shape(mf._arith(args.arith), w["degree"],
-                                           {"column": 0, "point": 1, "tma": 2}[args.shape]))
+                                           SHAPE_CODES[args.shape]))
     A = mf.LaplaceOperator(mf.BoxMesh(w["nx"], w["ny"], w["nz"], degree=w["degree"],
                                       amplitude=w["amplitude"]), arith=args.arith)
     n, n_cells = A.m(), A.n_cells
@@ -699,7 +703,7 @@ def main():
     ap.add_argument("--cells", type=int, nargs=3, default=None,
                     help="override the mesh (cells per direction) for sweeps and profiling")
     ap.add_argument("--degree", type=int, default=None, help="override the degree p")
-    ap.add_argument("--shape", choices=["auto", "column", "point", "tma"], default="auto",
+    ap.add_argument("--shape", choices=["auto", *SHAPE_CODES], default="auto",
                     help="operator kernel thread layout (default: the library's table)")
     args = ap.parse_args()
     if args.cells:
