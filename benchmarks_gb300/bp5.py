@@ -9,6 +9,8 @@ python -m benchmarks_gb300.bp5 --cells 128 128 64 --degree 4 --solver mg32
              helmholtz (bp5_kokkos's Helmholtz operator with Jacobi-PCG),
              batch (the seeded --problems mix solved together; --cells and
              --degree unused)
+    --quadrature gll | gauss | bp3: the operator form (BP3: CEED_bp's
+             q = p + 2 Laplacian, CEED_bp/include/bk3_kokkos_kernel.h:146-354)
 """
 from __future__ import annotations
 
@@ -31,6 +33,8 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=2, help="solves (best time reported)")
     ap.add_argument("--seed", type=int, default=1, help="right-hand side U[-1,1] seed")
     ap.add_argument("--arith", choices=["df", "fp64"], default="df")
+    ap.add_argument("--quadrature", choices=["gll", "gauss", "bp3"], default="gll",
+                    help="operator form: GLL collocation (BK5), Gauss p+1, BP3 (Gauss p+2)")
     a = ap.parse_args(argv)
     import torch
 
@@ -63,7 +67,8 @@ def main(argv=None):
     if a.solver == "helmholtz":
         A, t_setup = timed(lambda: mf.HelmholtzOperator(mesh, arith=a.arith))
     else:
-        A, t_setup = timed(lambda: mf.LaplaceOperator(mesh, arith=a.arith))
+        A, t_setup = timed(lambda: mf.LaplaceOperator(mesh, arith=a.arith,
+                                                      quadrature=a.quadrature))
     if a.solver in ("mg32", "mg64"):
         P, t_pre = timed(lambda: mf.MGPreconditioner(mesh, precision=int(a.solver[2:]), operator=A))
     elif a.solver in ("jacobi", "helmholtz"):

@@ -40,8 +40,9 @@ static mfgb_status dev_alloc(void **p, size_t bytes, const char *what) {
 }
 
 mfgb_status ensure_df(mfgb_operator *op) {
-  if (op->d_Gdf || op->quadrature == 2) return MFGB_OK;  // BP3 reads FP64 G in both arithmetics
-  const int64_t ng = op->n_cells * 6 * (int64_t)op->n * op->n * op->n;
+  if (op->d_Gdf) return MFGB_OK;
+  const int64_t nq = op->nq > 0 ? op->nq : op->n;  // G points per direction
+  const int64_t ng = op->n_cells * 6 * nq * nq * nq;
   mfgb_status st = dev_alloc((void **)&op->d_Gdf, sizeof(float2) * ng, "G (double-float)");
   if (st) return st;
   st = cuda_status(g_to_df(ng, op->d_G, op->d_Gdf, nullptr), "G -> double-float");
@@ -65,8 +66,9 @@ static cudaError_t apply_range(mfgb_operator *op, int64_t cell0, int64_t n, doub
   const uint32_t *map = op->d_map + cell0 * n3;
   if (op->quadrature == 2) {
     if (partials || done) return cudaErrorNotSupported;
-    return bp3_apply(op->degree, n, map, op->d_Bq, op->d_DGq, op->d_G + cell0 * 6 * q3, src, dst,
-                     arith, s);
+    return bp3_apply(op->degree, n, map, op->d_Bq, op->d_DGq, op->Bq, op->DG,
+                     op->d_G + cell0 * 6 * q3, op->d_Gdf ? op->d_Gdf + cell0 * 6 * q3 : nullptr,
+                     src, dst, arith, s);
   }
   if (arith == MFGB_ARITH_FP64)
     return op->quadrature

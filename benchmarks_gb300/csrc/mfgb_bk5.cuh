@@ -305,18 +305,90 @@ __global__ void __launch_bounds__(E * N * N * N)
 
 namespace mfgb {
 
-template <int N, int E, class A>
-struct TmaLayout {
-  static constexpr int N3 = N * N * N;
-  static constexpr size_t g_bytes = sizeof(typename A::GType) * E * 6 * N3;
-  static constexpr size_t map_bytes = ((size_t)E * N3 * 4 + 15) / 16 * 16;
-  static constexpr size_t work_bytes = 3 * sizeof(typename A::V) * E * N3;
+// Shared-memory layout of a bulk-TMA kernel's batch of E cells: G tile (6
+// components at NQ^3 points per cell), dof-map tile (NM^3 per cell), three
+// work arrays of NQ^3 values per cell, two mbarriers.
+template <int NM, int NQ, int E, class A>
+struct TmaLayoutQ {
+  static constexpr int M3 = NM * NM * NM, Q3 = NQ * NQ * NQ;
+  static constexpr size_t g_bytes = sizeof(typename A::GType) * E * 6 * Q3;
+  static constexpr size_t map_bytes = ((size_t)E * M3 * 4 + 15) / 16 * 16;
+  static constexpr size_t work_bytes = 3 * sizeof(typename A::V) * E * Q3;
   static constexpr size_t total = g_bytes + map_bytes + work_bytes + 16;
   // tiles start at batch * (full tile): bulk copies only when every full tile
   // is a 16-byte multiple (then every batch's start is 16-byte aligned)
-  static constexpr bool map_tma = (E * N3 * 4) % 16 == 0;
+  static constexpr bool map_tma = (E * M3 * 4) % 16 == 0;
   static constexpr bool g_tma = g_bytes % 16 == 0;
 };
+template <int N, int E, class A> using TmaLayout = TmaLayoutQ<N, N, E, A>;
+
+// One CTA's bulk-TMA staging of a batch's G tile and dof-map tile into shared
+// memory, each completing on its own mbarrier; used by the collocation, the
+// Gauss-point and the BP3 kernels.  issue_* run on one thread and complete the
+// mbarrier phase whether or not a copy is issued.
+template <int NM, int NQ, int E, class A>
+struct TmaTilesQ {
+  using GT = typename A::GType;
+  using VT = typename A::VecT;
+  using L = TmaLayoutQ<NM, NQ, E, A>;
+  static constexpr int M2 = NM * NM, M3 = NM * NM * NM, Q3 = NQ * NQ * NQ;
+  int64_t n_cells;
+  const uint32_t *__restrict__ map;
+  const GT *__restrict__ G;
+  const VT *__restrict__ src;
+  GT *sG;
+  uint32_t *sMap;
+  uint64_t *mbar_g, *mbar_m;
+
+  __device__ __forceinline__ int cells_of(int64_t b) const {
+    return (int)min((int64_t)E, n_cells - b * E);
+  }
+  __device__ __forceinline__ bool map_by_tma(int cells) const {
+    return L::map_tma && ((cells * M3 * 4) % 16 == 0);
+  }
+  // a bulk copy needs a 16-byte aligned start and a 16-byte multiple: 4-byte G
+  // tiles of an odd number of cells with odd NQ^3 (an odd E, or the last batch)
+  // are loaded by plain loads (load_g_plain)
+  __device__ __forceinline__ bool g_by_tma(int cells) const {
+    return L::g_tma && (sizeof(GT) * cells * 6 * Q3) % 16 == 0;
+  }
+  __device__ __forceinline__ void issue_g(int64_t b) const {
+    const int cells = cells_of(b);
+    const uint32_t gb = g_by_tma(cells) ? (uint32_t)(sizeof(GT) * cells * 6 * Q3) : 0u;
+    mbar_arrive_expect_tx(mbar_g, gb);
+    if (gb) bulk_g2s(sG, G + b * E * 6 * Q3, gb, mbar_g);
+  }
+  __device__ __forceinline__ void issue_map(int64_t b) const {
+    const int cells = cells_of(b);
+    const uint32_t mb = map_by_tma(cells) ? (uint32_t)(cells * M3 * 4) : 0u;
+    mbar_arrive_expect_tx(mbar_m, mb);
+    if (mb) bulk_g2s(sMap, map + b * E * M3, mb, mbar_m);
+  }
+  // after the G wait: the tile of a batch that had no bulk copy, by plain loads
+  // (to be ordered before its readers by a barrier)
+  __device__ __forceinline__ void load_g_plain(int64_t b, int tid, int nthreads) const {
+    if (g_by_tma(cells_of(b))) return;
+    const int64_t nG = (int64_t)cells_of(b) * 6 * Q3;
+    const GT *Gb = G + b * E * 6 * Q3;
+    for (int64_t t = tid; t < nG; t += nthreads) sG[t] = __ldg(Gb + t);
+  }
+  // node column (el, jk), jk = j * NM + k, of batch b: dof indices (from the
+  // map tile or global) and the raw source values, into registers; threads
+  // without a column (has_col false) get invalid indices
+  __device__ __forceinline__ void gather(int64_t b, int el, int jk, uint32_t *idx, VT *raw,
+                                         bool has_col = true) const {
+    const int cells = cells_of(b);
+    const bool valid = has_col && el < cells;
+    const bool mt = map_by_tma(cells);
+#pragma unroll
+    for (int i = 0; i < NM; ++i) {
+      idx[i] = valid ? (mt ? sMap[el * M3 + i * M2 + jk] : __ldg(map + (b * E + el) * M3 + i * M2 + jk))
+                     : MFGB_INVALID_DOF;
+      raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + idx[i]) : VT(0);
+    }
+  }
+};
+template <int N, int E, class A> using TmaTiles = TmaTilesQ<N, N, E, A>;
 
 // Column kernel with bulk-TMA prefetch.  Per batch b of E cells:
 //   barrier A   wait for G(b) (mbarrier 0); the u(b) gather was prefetched
@@ -378,38 +450,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
     Dtk[m] = basis.D[m * N + k];
   }
 
-  auto cells_of = [&](int64_t b) { return (int)min((int64_t)E, n_cells - b * E); };
-  auto map_by_tma = [&](int cells) { return L::map_tma && ((cells * N3 * 4) % 16 == 0); };
-  // a bulk copy needs a 16-byte aligned start and a 16-byte multiple: 4-byte G
-  // tiles of an odd number of cells with odd N^3 (an odd E, or the last batch)
-  // are loaded by plain loads
-  auto g_by_tma = [&](int cells) {
-    return L::g_tma && (sizeof(GT) * cells * 6 * N3) % 16 == 0;
-  };
-  auto issue_g = [&](int64_t b) {  // one thread; completes the phase either way
-    const int cells = cells_of(b);
-    const uint32_t gb = g_by_tma(cells) ? (uint32_t)(sizeof(GT) * cells * 6 * N3) : 0u;
-    mbar_arrive_expect_tx(mbar_g, gb);
-    if (gb) bulk_g2s(sG, G + b * E * 6 * N3, gb, mbar_g);
-  };
-  auto issue_map = [&](int64_t b) {  // one thread; completes the phase either way
-    const int cells = cells_of(b);
-    const uint32_t mb = map_by_tma(cells) ? (uint32_t)(cells * N3 * 4) : 0u;
-    mbar_arrive_expect_tx(mbar_m, mb);
-    if (mb) bulk_g2s(sMap, map + b * E * N3, mb, mbar_m);
-  };
-  // gather of one batch into registers (idx from the map tile or global)
-  auto gather = [&](int64_t b, uint32_t *idx, VT *raw) {
-    const int cells = cells_of(b);
-    const bool valid = el < cells;
-    const bool mt = map_by_tma(cells);
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      idx[i] = valid ? (mt ? sMap[el * N3 + i * N2 + jk] : __ldg(map + (b * E + el) * N3 + i * N2 + jk))
-                     : MFGB_INVALID_DOF;
-      raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + idx[i]) : VT(0);
-    }
-  };
+  const TmaTiles<N, E, A> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
   auto fail = [&](uint32_t pg, uint32_t pm) {
     if (tid == 0 && err_flag) atomicExch(err_flag, 1);
     mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
@@ -423,8 +464,8 @@ __global__ void __launch_bounds__(E * N * N, MB)
   }
   __syncthreads();
   if (tid == 0) {
-    issue_g(batch);
-    issue_map(batch);
+    T.issue_g(batch);
+    T.issue_map(batch);
   }
   uint32_t ph_g = 0, ph_m = 0;
   uint32_t idx[N];
@@ -433,7 +474,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
     const bool ok = mbar_wait(mbar_m, ph_m);
     if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
     ph_m ^= 1u;
-    gather(batch, idx, raw);
+    T.gather(batch, el, jk, idx, raw);
   }
   double energy = 0.0;
 
@@ -443,11 +484,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
     const bool okg = mbar_wait(mbar_g, ph_g);
     if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
     ph_g ^= 1u;
-    if (!g_by_tma(cells_of(batch))) {  // tail tile not 16-byte sized: plain loads
-      const int64_t nG = (int64_t)cells_of(batch) * 6 * N3;
-      const GT *Gb = G + batch * E * 6 * N3;
-      for (int64_t t = tid; t < nG; t += blockDim.x) sG[t] = __ldg(Gb + t);
-    }  // ordered before the metric phase by barrier B
+    T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase by barrier B
     V u[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -457,10 +494,10 @@ __global__ void __launch_bounds__(E * N * N, MB)
     __syncthreads();  // barrier B: s_u ready; the map tile is free
     if (tid == 0 && has_next) {
       fence_proxy_async_smem();
-      issue_map(next);
+      T.issue_map(next);
     }
 
-    const bool valid = el < cells_of(batch);
+    const bool valid = el < T.cells_of(batch);
     V vr[N];
     const GT *Gc = sG + el * 6 * N3 + jk;
 #pragma unroll
@@ -499,7 +536,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
     __syncthreads();  // barrier C: G tile consumed, s_vs / s_vt ready
     if (tid == 0 && has_next) {
       fence_proxy_async_smem();
-      issue_g(next);
+      T.issue_g(next);
     }
 
     // this batch's scatter targets; then prefetch the next batch's gather
@@ -512,11 +549,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
     }
     if (has_next) {
       const bool okm = mbar_wait(mbar_m, ph_m);
-      if (!okm) {  // per-thread: fall back to the global map (always valid)
-        if (err_flag) atomicExch(err_flag, 1);
-      }
+      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
       ph_m ^= 1u;
-      if (okm) gather(next, idx, raw);
+      if (okm) T.gather(next, el, jk, idx, raw);
       else
         for (int i = 0; i < N; ++i) { idx[i] = MFGB_INVALID_DOF; raw[i] = VT(0); }
     }
@@ -747,6 +782,247 @@ __global__ void __launch_bounds__(E * N * N)
 }  // namespace mfgb
 
 namespace mfgb {
+
+// The Gauss-point form with the bulk-TMA pipeline of bk5_tma_kernel: the next
+// batch's G and dof-map tiles stream into shared memory while this batch is
+// computed, and the next batch's gather is prefetched into registers during
+// the integrate phase.  Per batch of E cells (W0, W1, W2 the work arrays):
+//   A  wait G(b); W0 = u (prefetched gather); B; TMA map(b+next)
+//      W1 = B_k W0; barrier; u = B_i B_j W1 (registers), W0 = u; barrier
+//      gradient + metric (W0, G tile) -> vr (registers), W1, W2
+//   C  TMA G(b+next); wait map(b+next), prefetch u(b+next)
+//      integrate (+ JxW u for the mass term), back along i (registers); barrier
+//      W0 = that; barrier; W1 = B_j^T W0; barrier; dst += B_k^T W1 (atomic)
+// A JxW array (mass term) is read with plain loads.  Waits are bounded as in
+// bk5_tma_kernel.
+template <int N, int E, class A, int MB>
+__global__ void __launch_bounds__(E * N * N, MB)
+    bk5g_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                    const typename A::GType *__restrict__ G,
+                    const typename A::VecT *__restrict__ src, typename A::VecT *__restrict__ dst,
+                    const BasisG<N, A> basis, const int *__restrict__ done_flag,
+                    const typename A::GType *__restrict__ jxw, int *__restrict__ err_flag) {
+  if (done_flag != nullptr && *done_flag) return;
+  using V = typename A::V;
+  using Acc = typename A::Acc;
+  using GT = typename A::GType;
+  using VT = typename A::VecT;
+  using L = TmaLayout<N, E, A>;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  extern __shared__ __align__(128) unsigned char smem[];
+  GT *sG = reinterpret_cast<GT *>(smem);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *w0 = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
+  V *w1 = w0 + E * N3;
+  V *w2 = w1 + E * N3;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+  uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
+
+  const int tid = threadIdx.x;
+  const int el = tid / N2;
+  const int jk = tid - el * N2;
+  const int j = jk / N;
+  const int k = jk - j * N;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  int64_t batch = blockIdx.x;
+  if (batch >= n_batches) return;  // uniform across the CTA
+  V *a0 = w0 + el * N3, *a1 = w1 + el * N3, *a2 = w2 + el * N3;
+  // B and D in shared memory: each phase loads the rows / columns its thread
+  // needs (indexed by j or k) into registers; rows indexed by the unrolled i
+  // stay constant-bank operands
+  __shared__ V sB[N * N], sD[N * N];
+  for (int q = tid; q < N * N; q += blockDim.x) {
+    sB[q] = basis.B[q];
+    sD[q] = basis.D[q];
+  }
+  auto row = [&](const V *M, int r, V *out) {
+#pragma unroll
+    for (int m = 0; m < N; ++m) out[m] = M[r * N + m];
+  };
+  auto col = [&](const V *M, int c, V *out) {
+#pragma unroll
+    for (int m = 0; m < N; ++m) out[m] = M[m * N + c];
+  };
+
+  const TmaTiles<N, E, A> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
+  auto fail = [&](uint32_t pg, uint32_t pm) {
+    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
+    mbar_wait(mbar_m, pm);
+  };
+  if (tid == 0) {
+    mbar_init(mbar_g, 1);
+    mbar_init(mbar_m, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    T.issue_g(batch);
+    T.issue_map(batch);
+  }
+  uint32_t ph_g = 0, ph_m = 0;
+  uint32_t idx[N];
+  VT raw[N];
+  {
+    const bool ok = mbar_wait(mbar_m, ph_m);
+    if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
+    ph_m ^= 1u;
+    T.gather(batch, el, jk, idx, raw);
+  }
+
+  for (; batch < n_batches; batch += gridDim.x) {
+    const int64_t next = batch + gridDim.x;
+    const bool has_next = next < n_batches;
+    const bool okg = mbar_wait(mbar_g, ph_g);
+    if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
+    ph_g ^= 1u;
+    T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase
+    const bool valid = el < T.cells_of(batch);
+    const int64_t cell = batch * E + el;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      a0[i * N2 + jk] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(raw[i]) : A::zero_v();
+    __syncthreads();  // barrier B: W0 ready; the map tile is free
+    if (tid == 0 && has_next) {
+      fence_proxy_async_smem();
+      T.issue_map(next);
+    }
+    // ---- interpolate to the Gauss points: along k (W0 -> W1), then j and i
+    V t[N], u[N], c0[N], c1[N];
+    row(sB, k, c0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a0[i * N2 + j * N + m]);
+      a1[i * N2 + jk] = A::finish(a);
+    }
+    __syncthreads();
+    row(sB, j, c0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a1[i * N2 + m * N + k]);
+      t[i] = A::finish(a);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[i * N + m], t[m]);
+      u[i] = A::finish(a);
+      a0[i * N2 + jk] = u[i];
+    }
+    __syncthreads();
+    // ---- collocation gradient at the Gauss points + metric (G tile in shared)
+    V vr[N];
+    const GT *Gc = sG + el * 6 * N3 + jk;
+    row(sD, j, c0);
+    row(sD, k, c1);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc ar, as, at;
+      A::zero(ar);
+      A::zero(as);
+      A::zero(at);
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        A::fma(ar, basis.D[i * N + m], u[m]);
+        A::fma(as, c0[m], a0[i * N2 + m * N + k]);
+        A::fma(at, c1[m], a0[i * N2 + j * N + m]);
+      }
+      const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+      V grr = A::zero_v(), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+      if (valid) {
+        grr = A::load_g(Gc[0 * N3 + i * N2]);
+        grs = A::load_g(Gc[1 * N3 + i * N2]);
+        grt = A::load_g(Gc[2 * N3 + i * N2]);
+        gss = A::load_g(Gc[3 * N3 + i * N2]);
+        gst = A::load_g(Gc[4 * N3 + i * N2]);
+        gtt = A::load_g(Gc[5 * N3 + i * N2]);
+      }
+      Acc br, bs, bt;
+      A::zero(br);
+      A::zero(bs);
+      A::zero(bt);
+      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      vr[i] = A::finish(br);
+      a1[i * N2 + jk] = A::finish(bs);
+      a2[i * N2 + jk] = A::finish(bt);
+    }
+    __syncthreads();  // barrier C: G tile consumed, W1 / W2 ready
+    if (tid == 0 && has_next) {
+      fence_proxy_async_smem();
+      T.issue_g(next);
+    }
+    // this batch's scatter targets; then prefetch the next batch's gather
+    uint32_t cur[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cur[i] = idx[i];
+    if (has_next) {
+      const bool okm = mbar_wait(mbar_m, ph_m);
+      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+      ph_m ^= 1u;
+      if (okm) T.gather(next, el, jk, idx, raw);
+      else
+        for (int i = 0; i < N; ++i) { idx[i] = MFGB_INVALID_DOF; raw[i] = VT(0); }
+    }
+    // ---- transpose gradient (+ JxW u), then back to the GLL nodes along i
+    col(sD, j, c0);
+    col(sD, k, c1);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        A::fma(a, basis.D[m * N + i], vr[m]);
+        A::fma(a, c0[m], a1[i * N2 + m * N + k]);
+        A::fma(a, c1[m], a2[i * N2 + j * N + m]);
+      }
+      if (jxw != nullptr && valid) A::fma(a, A::load_g(__ldg(jxw + cell * N3 + i * N2 + jk)), u[i]);
+      t[i] = A::finish(a);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + i], t[m]);
+      u[i] = A::finish(a);
+    }
+    __syncthreads();  // W0 (gradient input) and W1 / W2 consumed
+#pragma unroll
+    for (int i = 0; i < N; ++i) a0[i * N2 + jk] = u[i];
+    __syncthreads();
+    col(sB, j, c0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a0[i * N2 + m * N + k]);
+      a1[i * N2 + jk] = A::finish(a);
+    }
+    __syncthreads();
+    col(sB, k, c0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Acc a;
+      A::zero(a);
+#pragma unroll
+      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a1[i * N2 + j * N + m]);
+      if (cur[i] != MFGB_INVALID_DOF) atomicAdd(dst + cur[i], A::store_vec(A::finish(a)));
+    }
+    // W1 is read above until barrier A of the next batch; W0 is rewritten only after it
+  }
+}
 
 // BK6: the vector Laplacian with NC interleaved components (vec[NC*dof + c]),
 // every component through the same scalar operator.  A batch's G tile is

@@ -3,6 +3,7 @@
 #include <string>
 
 #include "mfgb_bkq.cuh"
+#include "mfgb_dispatch.cuh"
 #include "mfgb_internal.h"
 
 namespace mfgb {
@@ -71,14 +72,66 @@ mfgb_status bkq_entry(const char *name, bool laplace, int degree, int64_t nelmt,
 
 }  // namespace
 
-// BP3 operator apply: dst += A src over n_cells cells (gather / scatter through map)
-cudaError_t bp3_apply(int degree, int64_t n_cells, const uint32_t *map, const double *B,
-                      const double *DG, const double *G, const double *src, double *dst, int arith,
+namespace {
+
+// cells per CTA of the BP3 TMA kernel: about 7 warps of NQ^2-thread cells
+template <int NQ> struct Bp3Elems {
+  static constexpr int value =
+      NQ == 3 ? 24 : NQ == 4 ? 14 : NQ == 5 ? 9 : NQ == 6 ? 6 : NQ == 7 ? 4 : NQ <= 9 ? 2 : 1;
+};
+// residency: 2 CTAs per SM (128 registers a thread) up to NQ = 6, else 1
+template <int NQ> struct Bp3MinBlocks { static constexpr int value = NQ <= 6 ? 2 : 1; };
+
+template <int NM, int NQ, class A>
+cudaError_t bp3_tma_launch(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
+                           const double *src, double *dst, const double *hB, const double *hDG,
+                           cudaStream_t s) {
+  constexpr int E = Bp3Elems<NQ>::value;
+  constexpr int MB = Bp3MinBlocks<NQ>::value;
+  constexpr int threads = E * NQ * NQ;
+  constexpr size_t smem = TmaLayoutQ<NM, NQ, E, A>::total;
+  BasisQ<NM, NQ, A> basis;
+  for (int q = 0; q < NQ * NM; ++q) basis.B[q] = BasisValue<A>::from(hB[q]);
+  for (int q = 0; q < NQ * NQ; ++q) basis.D[q] = BasisValue<A>::from(hDG[q]);
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bp3_tma_kernel<NM, NQ, E, A, MB>, threads, smem));
+  const int64_t batches = (n_cells + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(batches, (int64_t)per_sm * num_sms()));
+  bp3_tma_kernel<NM, NQ, E, A, MB><<<grid, threads, smem, s>>>(n_cells, map, G, src, dst, basis,
+                                                                 device_error_flag());
+  return cudaGetLastError();
+}
+
+template <class A>
+cudaError_t bp3_tma_dispatch(int degree, int64_t n_cells, const uint32_t *map,
+                             const typename A::GType *G, const double *src, double *dst,
+                             const double *hB, const double *hDG, cudaStream_t s) {
+  switch (degree) {
+#define MFGB_BP3(P) \
+  case P: return bp3_tma_launch<P + 1, P + 2, A>(n_cells, map, G, src, dst, hB, hDG, s);
+    MFGB_BP3(1) MFGB_BP3(2) MFGB_BP3(3) MFGB_BP3(4) MFGB_BP3(5) MFGB_BP3(6) MFGB_BP3(7) MFGB_BP3(8)
+#undef MFGB_BP3
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+// BP3 operator apply: dst += A src over n_cells cells (gather / scatter through
+// map).  16-byte aligned G and map run the bulk-TMA kernel (G as FP64 or as
+// double-float pairs, Gdf); otherwise the line kernel bkq_kernel with FP64 G.
+cudaError_t bp3_apply(int degree, int64_t n_cells, const uint32_t *map, const double *d_B,
+                      const double *d_DG, const double *h_B, const double *h_DG, const double *G,
+                      const float2 *Gdf, const double *src, double *dst, int arith,
                       cudaStream_t s) {
   if (n_cells <= 0) return cudaSuccess;
-  return arith == MFGB_ARITH_FP64
-             ? bkq_dispatch<ArithF64, true>(degree, n_cells, B, DG, G, src, dst, s, map)
-             : bkq_dispatch<ArithDF, true>(degree, n_cells, B, DG, G, src, dst, s, map);
+  const bool f64 = arith == MFGB_ARITH_FP64;
+  const uintptr_t g = f64 ? reinterpret_cast<uintptr_t>(G) : reinterpret_cast<uintptr_t>(Gdf);
+  if (g != 0 && ((g | reinterpret_cast<uintptr_t>(map)) & 15u) == 0)
+    return f64 ? bp3_tma_dispatch<ArithF64>(degree, n_cells, map, G, src, dst, h_B, h_DG, s)
+               : bp3_tma_dispatch<ArithDF>(degree, n_cells, map, Gdf, src, dst, h_B, h_DG, s);
+  return f64 ? bkq_dispatch<ArithF64, true>(degree, n_cells, d_B, d_DG, G, src, dst, s, map)
+             : bkq_dispatch<ArithDF, true>(degree, n_cells, d_B, d_DG, G, src, dst, s, map);
 }
 
 }  // namespace mfgb

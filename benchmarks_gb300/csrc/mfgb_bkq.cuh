@@ -19,7 +19,7 @@
 // (q, r) keeps the direction-0 column of its points in registers).  Arithmetic
 // is FP64 or double-float (policy A).
 #pragma once
-#include "mfgb_common.cuh"
+#include "mfgb_bk5.cuh"
 
 namespace mfgb {
 
@@ -225,6 +225,262 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
       }
     }
     __syncthreads();
+  }
+}
+
+// BP3 operator (L-vector, NM = p + 1 GLL nodes interpolated to NQ Gauss points
+// per direction; CEED_bp/include/bk3_kokkos_kernel.h:146-354) with the bulk-TMA
+// pipeline of the BK5 kernels: G (6 x NQ^3 per cell, A::GType) and the dof map
+// of the next batch stream into shared memory while this batch is computed,
+// and the next gather is prefetched into registers.  A CTA holds E cells with
+// NQ^2 threads per cell, thread (a, b) of a cell:
+//   gather          (a, b) < NM: node column u[i][a][b]           -> W0
+//   interp k        a < NM:  W1[i][a][q3 = b] = sum_m B[b][m] W0[i][a][m]
+//   interp j, i     all:     t[i] = sum_m B[a][m] W1[i][m][b]; u[q1] = sum_i B[q1][i] t[i]
+//                            -> W0 (Gauss layout [q1][a][b])
+//   gradient, metric         column (a, b) at the Gauss points: vr (registers), W1, W2
+//   integrate, back i        t[q1] = D^T...; y[i] = sum_q1 B[q1][i] t[q1] -> W0 [i][a][b]
+//   back j          a < NM:  W1[i][a][b] = sum_q2 B[q2][a] W0[i][q2][b]
+//   back k, scatter (a, b) < NM: dst[map] += sum_q3 B[q3][b] W1[i][a][q3]
+// Every wait is bounded (a timeout sets err_flag and the CTA returns).
+template <int NM, int NQ, class A>
+struct BasisQ {
+  typename A::V B[NQ * NM];  // B[q * NM + i] = l_i(g_q)
+  typename A::V D[NQ * NQ];  // collocation derivative at the Gauss points
+};
+
+template <int NM, int NQ, int E, class A, int MB>
+__global__ void __launch_bounds__(E * NQ * NQ, MB)
+    bp3_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                   const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+                   typename A::VecT *__restrict__ dst, const BasisQ<NM, NQ, A> basis,
+                   int *__restrict__ err_flag) {
+  using V = typename A::V;
+  using Acc = typename A::Acc;
+  using GT = typename A::GType;
+  using VT = typename A::VecT;
+  using L = TmaLayoutQ<NM, NQ, E, A>;
+  constexpr int M2 = NM * NM, Q2 = NQ * NQ, Q3 = NQ * NQ * NQ, MQ = NM * NQ;
+  extern __shared__ __align__(128) unsigned char smem[];
+  GT *sG = reinterpret_cast<GT *>(smem);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *w0 = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+  uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
+  __shared__ V sB[NQ * NM], sD[NQ * NQ];
+
+  const int tid = threadIdx.x;
+  const int el = tid / Q2;
+  const int ab = tid - el * Q2;
+  const int a = ab / NQ;
+  const int b = ab - a * NQ;
+  const bool node_col = a < NM && b < NM;  // owns a node column (gather / scatter)
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  int64_t batch = blockIdx.x;
+  if (batch >= n_batches) return;  // uniform across the CTA
+  V *W0 = w0 + el * Q3, *W1 = w0 + (E + el) * Q3, *W2 = w0 + (2 * E + el) * Q3;
+  for (int q = tid; q < NQ * NM; q += blockDim.x) sB[q] = basis.B[q];
+  for (int q = tid; q < NQ * NQ; q += blockDim.x) sD[q] = basis.D[q];
+
+  const TmaTilesQ<NM, NQ, E, A> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
+  auto fail = [&](uint32_t pg, uint32_t pm) {
+    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
+    mbar_wait(mbar_m, pm);
+  };
+  if (tid == 0) {
+    mbar_init(mbar_g, 1);
+    mbar_init(mbar_m, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    T.issue_g(batch);
+    T.issue_map(batch);
+  }
+  uint32_t ph_g = 0, ph_m = 0;
+  uint32_t idx[NM];
+  VT raw[NM];
+  const int jk = node_col ? a * NM + b : 0;
+  {
+    const bool ok = mbar_wait(mbar_m, ph_m);
+    if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
+    ph_m ^= 1u;
+    T.gather(batch, el, jk, idx, raw, node_col);
+  }
+
+  for (; batch < n_batches; batch += gridDim.x) {
+    const int64_t next = batch + gridDim.x;
+    const bool has_next = next < n_batches;
+    const bool okg = mbar_wait(mbar_g, ph_g);
+    if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
+    ph_g ^= 1u;
+    T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase
+    const bool valid = el < T.cells_of(batch);
+    if (node_col) {
+#pragma unroll
+      for (int i = 0; i < NM; ++i)
+        W0[i * M2 + jk] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(raw[i]) : A::zero_v();
+    }
+    __syncthreads();  // barrier B: nodal values ready; the map tile is free
+    if (tid == 0 && has_next) {
+      fence_proxy_async_smem();
+      T.issue_map(next);
+    }
+    V c0[NQ], c1[NQ];
+    // ---- interpolate along k: W1[i][a][b] (a < NM, b < NQ)
+    if (a < NM) {
+#pragma unroll
+      for (int m = 0; m < NM; ++m) c0[m] = sB[b * NM + m];
+#pragma unroll
+      for (int i = 0; i < NM; ++i) {
+        Acc s;
+        A::zero(s);
+#pragma unroll
+        for (int m = 0; m < NM; ++m) A::fma(s, c0[m], W0[i * M2 + a * NM + m]);
+        W1[i * MQ + a * NQ + b] = A::finish(s);
+      }
+    }
+    __syncthreads();
+    // ---- along j (shared) and i (registers): u at the Gauss points of column (a, b)
+    V t[NQ], u[NQ];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) c0[m] = sB[a * NM + m];
+#pragma unroll
+    for (int i = 0; i < NM; ++i) {
+      Acc s;
+      A::zero(s);
+#pragma unroll
+      for (int m = 0; m < NM; ++m) A::fma(s, c0[m], W1[i * MQ + m * NQ + b]);
+      t[i] = A::finish(s);
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      Acc s;
+      A::zero(s);
+#pragma unroll
+      for (int i = 0; i < NM; ++i) A::fma(s, basis.B[q * NM + i], t[i]);
+      u[q] = A::finish(s);
+      W0[q * Q2 + ab] = u[q];
+    }
+    __syncthreads();
+    // ---- collocation gradient + metric (G tile in shared memory)
+    V vr[NQ];
+    const GT *Gc = sG + el * 6 * Q3 + ab;
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      c0[m] = sD[a * NQ + m];
+      c1[m] = sD[b * NQ + m];
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      Acc ar, as, at;
+      A::zero(ar);
+      A::zero(as);
+      A::zero(at);
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) {
+        A::fma(ar, basis.D[q * NQ + m], u[m]);
+        A::fma(as, c0[m], W0[q * Q2 + m * NQ + b]);
+        A::fma(at, c1[m], W0[q * Q2 + a * NQ + m]);
+      }
+      const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+      V grr = A::zero_v(), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+      if (valid) {
+        grr = A::load_g(Gc[0 * Q3 + q * Q2]);
+        grs = A::load_g(Gc[1 * Q3 + q * Q2]);
+        grt = A::load_g(Gc[2 * Q3 + q * Q2]);
+        gss = A::load_g(Gc[3 * Q3 + q * Q2]);
+        gst = A::load_g(Gc[4 * Q3 + q * Q2]);
+        gtt = A::load_g(Gc[5 * Q3 + q * Q2]);
+      }
+      Acc br, bs, bt;
+      A::zero(br);
+      A::zero(bs);
+      A::zero(bt);
+      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      vr[q] = A::finish(br);
+      W1[q * Q2 + ab] = A::finish(bs);
+      W2[q * Q2 + ab] = A::finish(bt);
+    }
+    __syncthreads();  // barrier C: G tile consumed, W1 / W2 ready
+    if (tid == 0 && has_next) {
+      fence_proxy_async_smem();
+      T.issue_g(next);
+    }
+    // this batch's scatter targets; then prefetch the next batch's gather
+    uint32_t cur[NM];
+#pragma unroll
+    for (int i = 0; i < NM; ++i) cur[i] = idx[i];
+    if (has_next) {
+      const bool okm = mbar_wait(mbar_m, ph_m);
+      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+      ph_m ^= 1u;
+      if (okm) T.gather(next, el, jk, idx, raw, node_col);
+      else
+        for (int i = 0; i < NM; ++i) { idx[i] = MFGB_INVALID_DOF; raw[i] = VT(0); }
+    }
+    // ---- integrate (D^T, sum of three) and back to the nodes along i
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      c0[m] = sD[m * NQ + a];
+      c1[m] = sD[m * NQ + b];
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      Acc s;
+      A::zero(s);
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) {
+        A::fma(s, basis.D[m * NQ + q], vr[m]);
+        A::fma(s, c0[m], W1[q * Q2 + m * NQ + b]);
+        A::fma(s, c1[m], W2[q * Q2 + a * NQ + m]);
+      }
+      t[q] = A::finish(s);
+    }
+    V y[NM];
+#pragma unroll
+    for (int i = 0; i < NM; ++i) {
+      Acc s;
+      A::zero(s);
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) A::fma(s, basis.B[q * NM + i], t[q]);
+      y[i] = A::finish(s);
+    }
+    __syncthreads();  // W0 (gradient input), W1, W2 consumed
+#pragma unroll
+    for (int i = 0; i < NM; ++i) W0[i * Q2 + ab] = y[i];
+    __syncthreads();
+    // ---- back along j: W1[i][a][b] (a < NM)
+    if (a < NM) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) c0[q] = sB[q * NM + a];
+#pragma unroll
+      for (int i = 0; i < NM; ++i) {
+        Acc s;
+        A::zero(s);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) A::fma(s, c0[q], W0[i * Q2 + q * NQ + b]);
+        W1[i * MQ + a * NQ + b] = A::finish(s);
+      }
+    }
+    __syncthreads();
+    // ---- back along k and scatter-add (node columns)
+    if (node_col) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) c0[q] = sB[q * NM + b];
+#pragma unroll
+      for (int i = 0; i < NM; ++i) {
+        Acc s;
+        A::zero(s);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) A::fma(s, c0[q], W1[i * MQ + a * NQ + q]);
+        if (cur[i] != MFGB_INVALID_DOF) atomicAdd(dst + cur[i], A::store_vec(A::finish(s)));
+      }
+    }
+    // W1 is read above until barrier A of the next batch; W0 is rewritten only after it
   }
 }
 

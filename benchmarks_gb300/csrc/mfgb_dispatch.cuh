@@ -49,6 +49,15 @@ cudaError_t bk5_dispatch(int N, int64_t n_cells, const uint32_t *map, const type
 
 namespace mfgb {
 
+// cells per CTA of the Gauss-point TMA kernel: whole warps at n = 5 (250
+// threads), else as the column kernel
+template <int N> struct GaussTmaElems { static constexpr int value = N == 5 ? 10 : ElemsPerCta<N>::value; };
+// residency of the Gauss-point TMA kernel: the register budget of the
+// arithmetic up to n = 5 (as AltMinBlocks), one CTA per SM's worth above
+template <int N, int E, class A> struct GaussTmaMinBlocks {
+  static constexpr int value = N <= 5 ? AltMinBlocks<N, E, A>::value : 1;
+};
+
 template <int N, class A, bool EN>
 cudaError_t bk5g_with_basis(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
                             const typename A::VecT *src, typename A::VecT *dst, const double *DG64,
@@ -60,9 +69,27 @@ cudaError_t bk5g_with_basis(int64_t n_cells, const uint32_t *map, const typename
     b.D[q] = BasisValue<A>::from(DG64[q]);
     b.B[q] = BasisValue<A>::from(B64[q]);
   }
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  // L-vector mode with 16-byte aligned G and map: the bulk-TMA pipeline
+  const bool tma = !EN && map != nullptr &&
+                   ((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(map)) & 15u) == 0;
+  if (tma) {
+    constexpr int ET = GaussTmaElems<N>::value;
+    constexpr int MB = GaussTmaMinBlocks<N, ET, A>::value;
+    constexpr size_t smem = TmaLayout<N, ET, A>::total;
+    static int per_sm_tma = -1;
+    if (per_sm_tma < 0)
+      per_sm_tma = std::max(1, ctas_per_sm(bk5g_tma_kernel<N, ET, A, MB>, ET * N * N, smem));
+    const int64_t nb = (n_cells + ET - 1) / ET;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)per_sm_tma * num_sms()));
+    if (grid) *grid = g;
+    if (n_cells <= 0) return cudaSuccess;
+    bk5g_tma_kernel<N, ET, A, MB><<<g, ET * N * N, smem, s>>>(n_cells, map, G, src, dst, b, done,
+                                                              jxw, device_error_flag());
+    return cudaGetLastError();
+  }
   static int per_sm = -1;
   if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk5g_kernel<N, E, A, EN>, E * N * N, 0));
-  const int64_t n_batches = (n_cells + E - 1) / E;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>(n_batches, (int64_t)per_sm * num_sms()));
   if (grid) *grid = g;
   if (n_cells <= 0) return cudaSuccess;

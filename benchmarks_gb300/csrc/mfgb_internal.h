@@ -106,8 +106,11 @@ cudaError_t diagonal_gauss(int N, int NQ, int64_t n_cells, const uint32_t *map, 
                            const double *JxW, const double *B, const double *DG, double *diag,
                            cudaStream_t s);
 // BP3 operator (mfgb_bkq.cu): dst += A src, q = p + 2 Gauss points, G[cell][6][nq^3]
-cudaError_t bp3_apply(int degree, int64_t n_cells, const uint32_t *map, const double *B,
-                      const double *DG, const double *G, const double *src, double *dst, int arith,
+// in FP64 (G) and, for double-float arithmetic, as pairs (Gdf); the bases on the
+// device (d_B, d_DG) and on the host (h_B, h_DG)
+cudaError_t bp3_apply(int degree, int64_t n_cells, const uint32_t *map, const double *d_B,
+                      const double *d_DG, const double *h_B, const double *h_DG, const double *G,
+                      const float2 *Gdf, const double *src, double *dst, int arith,
                       cudaStream_t s);
 cudaError_t g_to_df(int64_t n, const double *G, float2 *Gdf, cudaStream_t s);
 cudaError_t g_to_f32(int64_t n, const double *G, float *G32, cudaStream_t s);
