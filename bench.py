@@ -620,7 +620,10 @@ def bp3_rate(args):
     ms = e0.elapsed_time(e1) / 10
     n = A.m()
     del A
-    return {"GDoF/s": n / ms / 1e6, "ms_per_vmult": ms, "n_q_1d": w["degree"] + 2}
+    # published: 9.396e-3 s a vmult at 67,634,433 DoFs on one GH200 (FP64 on an
+    # affine cube; CEED_bp/results/1xGH200_P4.txt:648)
+    return {"GDoF/s": n / ms / 1e6, "ms_per_vmult": ms, "n_q_1d": w["degree"] + 2,
+            "published_gh200": 7.20, "ratio_vs_published": n / ms / 1e6 / 7.20}
 
 
 def bk6_rate(A, args):

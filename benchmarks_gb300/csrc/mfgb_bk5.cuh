@@ -306,14 +306,14 @@ __global__ void __launch_bounds__(E * N * N * N)
 namespace mfgb {
 
 // Shared-memory layout of a bulk-TMA kernel's batch of E cells: G tile (6
-// components at NQ^3 points per cell), dof-map tile (NM^3 per cell), three
-// work arrays of NQ^3 values per cell, two mbarriers.
-template <int NM, int NQ, int E, class A>
+// components at NQ^3 points per cell), dof-map tile (NM^3 per cell), NW work
+// arrays of NQ^3 values per cell, two mbarriers.
+template <int NM, int NQ, int E, class A, int NW = 3>
 struct TmaLayoutQ {
   static constexpr int M3 = NM * NM * NM, Q3 = NQ * NQ * NQ;
   static constexpr size_t g_bytes = sizeof(typename A::GType) * E * 6 * Q3;
   static constexpr size_t map_bytes = ((size_t)E * M3 * 4 + 15) / 16 * 16;
-  static constexpr size_t work_bytes = 3 * sizeof(typename A::V) * E * Q3;
+  static constexpr size_t work_bytes = NW * sizeof(typename A::V) * E * Q3;
   static constexpr size_t total = g_bytes + map_bytes + work_bytes + 16;
   // tiles start at batch * (full tile): bulk copies only when every full tile
   // is a 16-byte multiple (then every batch's start is 16-byte aligned)
@@ -791,8 +791,8 @@ namespace mfgb {
 //      W1 = B_k W0; barrier; u = B_i B_j W1 (registers), W0 = u; barrier
 //      gradient + metric (W0, G tile) -> vr (registers), W1, W2
 //   C  TMA G(b+next); wait map(b+next), prefetch u(b+next)
-//      integrate (+ JxW u for the mass term), back along i (registers); barrier
-//      W0 = that; barrier; W1 = B_j^T W0; barrier; dst += B_k^T W1 (atomic)
+//      integrate (+ JxW u for the mass term), back along i (registers); W0 = that
+//      barrier; W1 = B_j^T W0; barrier; dst += B_k^T W1 (atomic)
 // A JxW array (mass term) is read with plain loads.  Waits are bounded as in
 // bk5_tma_kernel.
 template <int N, int E, class A, int MB>
@@ -997,10 +997,10 @@ __global__ void __launch_bounds__(E * N * N, MB)
       for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + i], t[m]);
       u[i] = A::finish(a);
     }
-    __syncthreads();  // W0 (gradient input) and W1 / W2 consumed
+    // W0's last readers (the gradient) finished before barrier C
 #pragma unroll
     for (int i = 0; i < N; ++i) a0[i * N2 + jk] = u[i];
-    __syncthreads();
+    __syncthreads();  // W0 ready; W1 / W2 consumed
     col(sB, j, c0);
 #pragma unroll
     for (int i = 0; i < N; ++i) {

@@ -89,7 +89,7 @@ cudaError_t bp3_tma_launch(int64_t n_cells, const uint32_t *map, const typename 
   constexpr int E = Bp3Elems<NQ>::value;
   constexpr int MB = Bp3MinBlocks<NQ>::value;
   constexpr int threads = E * NQ * NQ;
-  constexpr size_t smem = TmaLayoutQ<NM, NQ, E, A>::total;
+  constexpr size_t smem = TmaLayoutQ<NM, NQ, E, A, 4>::total;
   BasisQ<NM, NQ, A> basis;
   for (int q = 0; q < NQ * NM; ++q) basis.B[q] = BasisValue<A>::from(hB[q]);
   for (int q = 0; q < NQ * NQ; ++q) basis.D[q] = BasisValue<A>::from(hDG[q]);

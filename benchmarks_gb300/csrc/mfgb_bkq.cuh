@@ -236,12 +236,14 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 // NQ^2 threads per cell, thread (a, b) of a cell:
 //   gather          (a, b) < NM: node column u[i][a][b]           -> W0
 //   interp k        a < NM:  W1[i][a][q3 = b] = sum_m B[b][m] W0[i][a][m]
-//   interp j, i     all:     t[i] = sum_m B[a][m] W1[i][m][b]; u[q1] = sum_i B[q1][i] t[i]
-//                            -> W0 (Gauss layout [q1][a][b])
-//   gradient, metric         column (a, b) at the Gauss points: vr (registers), W1, W2
-//   integrate, back i        t[q1] = D^T...; y[i] = sum_q1 B[q1][i] t[q1] -> W0 [i][a][b]
+//   interp j, i     all:     t[i] = sum_m B[a][m] W1[i][m][b]; W0[q1][a][b] = sum_i B[q1][i] t[i]
+//   gradient, metric         column (a, b), one Gauss point per step -> W3 (r), W1 (s), W2 (t)
+//   integrate, back i        y[i] = sum_q1 B[q1][i] (D^T...)[q1]      -> W0 [i][a][b]
 //   back j          a < NM:  W1[i][a][b] = sum_q2 B[q2][a] W0[i][q2][b]
 //   back k, scatter (a, b) < NM: dst[map] += sum_q3 B[q3][b] W1[i][a][q3]
+// The loops over the Gauss points of a column are not unrolled (values in
+// shared memory, not registers): fully unrolled, the double-float code
+// outgrew the instruction cache (warps stalled on instruction fetch).
 // Every wait is bounded (a timeout sets err_flag and the CTA returns).
 template <int NM, int NQ, class A>
 struct BasisQ {
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
   using Acc = typename A::Acc;
   using GT = typename A::GType;
   using VT = typename A::VecT;
-  using L = TmaLayoutQ<NM, NQ, E, A>;
+  using L = TmaLayoutQ<NM, NQ, E, A, 4>;
   constexpr int M2 = NM * NM, Q2 = NQ * NQ, Q3 = NQ * NQ * NQ, MQ = NM * NQ;
   extern __shared__ __align__(128) unsigned char smem[];
   GT *sG = reinterpret_cast<GT *>(smem);
@@ -278,7 +280,8 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
   const int64_t n_batches = (n_cells + E - 1) / E;
   int64_t batch = blockIdx.x;
   if (batch >= n_batches) return;  // uniform across the CTA
-  V *W0 = w0 + el * Q3, *W1 = w0 + (E + el) * Q3, *W2 = w0 + (2 * E + el) * Q3;
+  V *W0 = w0 + el * Q3, *W1 = w0 + (E + el) * Q3, *W2 = w0 + (2 * E + el) * Q3,
+    *W3 = w0 + (3 * E + el) * Q3;
   for (int q = tid; q < NQ * NM; q += blockDim.x) sB[q] = basis.B[q];
   for (int q = tid; q < NQ * NQ; q += blockDim.x) sD[q] = basis.D[q];
 
@@ -342,37 +345,37 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
       }
     }
     __syncthreads();
-    // ---- along j (shared) and i (registers): u at the Gauss points of column (a, b)
-    V t[NQ], u[NQ];
+    // ---- along j (shared) and i: the column's values at the Gauss points -> W0
+    {
+      V t[NM];
 #pragma unroll
-    for (int m = 0; m < NM; ++m) c0[m] = sB[a * NM + m];
+      for (int m = 0; m < NM; ++m) c0[m] = sB[a * NM + m];
 #pragma unroll
-    for (int i = 0; i < NM; ++i) {
-      Acc s;
-      A::zero(s);
+      for (int i = 0; i < NM; ++i) {
+        Acc s;
+        A::zero(s);
 #pragma unroll
-      for (int m = 0; m < NM; ++m) A::fma(s, c0[m], W1[i * MQ + m * NQ + b]);
-      t[i] = A::finish(s);
-    }
+        for (int m = 0; m < NM; ++m) A::fma(s, c0[m], W1[i * MQ + m * NQ + b]);
+        t[i] = A::finish(s);
+      }
+#pragma unroll 1
+      for (int q = 0; q < NQ; ++q) {
+        Acc s;
+        A::zero(s);
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      Acc s;
-      A::zero(s);
-#pragma unroll
-      for (int i = 0; i < NM; ++i) A::fma(s, basis.B[q * NM + i], t[i]);
-      u[q] = A::finish(s);
-      W0[q * Q2 + ab] = u[q];
+        for (int i = 0; i < NM; ++i) A::fma(s, sB[q * NM + i], t[i]);
+        W0[q * Q2 + ab] = A::finish(s);
+      }
     }
     __syncthreads();
     // ---- collocation gradient + metric (G tile in shared memory)
-    V vr[NQ];
     const GT *Gc = sG + el * 6 * Q3 + ab;
 #pragma unroll
     for (int m = 0; m < NQ; ++m) {
       c0[m] = sD[a * NQ + m];
       c1[m] = sD[b * NQ + m];
     }
-#pragma unroll
+#pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       Acc ar, as, at;
       A::zero(ar);
@@ -380,7 +383,7 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
       A::zero(at);
 #pragma unroll
       for (int m = 0; m < NQ; ++m) {
-        A::fma(ar, basis.D[q * NQ + m], u[m]);
+        A::fma(ar, sD[q * NQ + m], W0[m * Q2 + ab]);
         A::fma(as, c0[m], W0[q * Q2 + m * NQ + b]);
         A::fma(at, c1[m], W0[q * Q2 + a * NQ + m]);
       }
@@ -401,11 +404,11 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
       A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
       A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
       A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
-      vr[q] = A::finish(br);
+      W3[q * Q2 + ab] = A::finish(br);
       W1[q * Q2 + ab] = A::finish(bs);
       W2[q * Q2 + ab] = A::finish(bt);
     }
-    __syncthreads();  // barrier C: G tile consumed, W1 / W2 ready
+    __syncthreads();  // barrier C: G tile consumed, W1 / W2 / W3 ready
     if (tid == 0 && has_next) {
       fence_proxy_async_smem();
       T.issue_g(next);
@@ -428,31 +431,27 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
       c0[m] = sD[m * NQ + a];
       c1[m] = sD[m * NQ + b];
     }
+    Acc y[NM];
 #pragma unroll
+    for (int i = 0; i < NM; ++i) A::zero(y[i]);
+#pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       Acc s;
       A::zero(s);
 #pragma unroll
       for (int m = 0; m < NQ; ++m) {
-        A::fma(s, basis.D[m * NQ + q], vr[m]);
+        A::fma(s, sD[m * NQ + q], W3[m * Q2 + ab]);
         A::fma(s, c0[m], W1[q * Q2 + m * NQ + b]);
         A::fma(s, c1[m], W2[q * Q2 + a * NQ + m]);
       }
-      t[q] = A::finish(s);
+      const V tq = A::finish(s);
+#pragma unroll
+      for (int i = 0; i < NM; ++i) A::fma(y[i], sB[q * NM + i], tq);
     }
-    V y[NM];
+    // W0's last readers (the gradient) finished before barrier C
 #pragma unroll
-    for (int i = 0; i < NM; ++i) {
-      Acc s;
-      A::zero(s);
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) A::fma(s, basis.B[q * NM + i], t[q]);
-      y[i] = A::finish(s);
-    }
-    __syncthreads();  // W0 (gradient input), W1, W2 consumed
-#pragma unroll
-    for (int i = 0; i < NM; ++i) W0[i * Q2 + ab] = y[i];
-    __syncthreads();
+    for (int i = 0; i < NM; ++i) W0[i * Q2 + ab] = A::finish(y[i]);
+    __syncthreads();  // W0 ready; W1, W2, W3 consumed
     // ---- back along j: W1[i][a][b] (a < NM)
     if (a < NM) {
 #pragma unroll
