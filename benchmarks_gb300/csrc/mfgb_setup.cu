@@ -121,10 +121,13 @@ __device__ __forceinline__ void axis_span(int64_t c, int nf, int s, double &a, d
 // One CTA per cell: the deformed geometry nodes (GLL points of the geometry
 // degree) in shared memory, then J = dx/dxi at the operator's GLL points
 // (the derivative matrix when both degrees agree, the tensor-product
-// geometry basis otherwise) and G = |det J| w_i w_j w_k Jinv Jinv^T.
+// geometry basis otherwise, sum factorised through the dynamic shared arrays
+// T1 [ng][ng][n] and T2 [ng][n][n], 3 components each) and
+// G = |det J| w_i w_j w_k Jinv Jinv^T.
 __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__restrict__ G,
                                     double *__restrict__ JxW) {
   __shared__ double xyz[729 * 3];
+  extern __shared__ double sf[];
   __shared__ double s1[3][9];  // sin(2 pi X) of the cell's node coordinates, per axis
   const int n = gp.nt, n3 = n * n * n;
   const int ng = gp.ng, ng3 = ng * ng * ng;
@@ -157,6 +160,46 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
     xyz[3 * l + 2] = Z + s;
   }
   __syncthreads();
+  // general: the geometry basis applied one direction at a time
+  //   T1v = V_k x, T1d = Dv_k x; T2vv = V_j T1v, T2dv = Dv_j T1v, T2vd = V_j T1d
+  //   J(:,r) = Dv_i T2vv, J(:,s) = V_i T2dv, J(:,t) = V_i T2vd
+  const int t1 = ng * ng * n, t2 = ng * n * n;
+  double *T1v = sf, *T1d = T1v + 3 * t1, *T2vv = T1d + 3 * t1, *T2dv = T2vv + 3 * t2,
+         *T2vd = T2dv + 3 * t2;
+  if (gp.general) {
+    for (int l = threadIdx.x; l < t1; l += blockDim.x) {
+      const int ab = l / n, k = l % n;
+      double v0 = 0, v1 = 0, v2 = 0, d0 = 0, d1 = 0, d2 = 0;
+      for (int c = 0; c < ng; ++c) {
+        const double *x = xyz + 3 * (ab * ng + c);
+        const double vk = gp.V[k * ng + c], dk = gp.Dv[k * ng + c];
+        v0 += vk * x[0]; v1 += vk * x[1]; v2 += vk * x[2];
+        d0 += dk * x[0]; d1 += dk * x[1]; d2 += dk * x[2];
+      }
+      T1v[3 * l] = v0; T1v[3 * l + 1] = v1; T1v[3 * l + 2] = v2;
+      T1d[3 * l] = d0; T1d[3 * l + 1] = d1; T1d[3 * l + 2] = d2;
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < t2; l += blockDim.x) {
+      const int a = l / (n * n), j = (l / n) % n, k = l % n;
+      double vv[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, vd[3] = {0, 0, 0};
+      for (int bb = 0; bb < ng; ++bb) {
+        const int src = 3 * ((a * ng + bb) * n + k);
+        const double vj = gp.V[j * ng + bb], dj = gp.Dv[j * ng + bb];
+        for (int d = 0; d < 3; ++d) {
+          vv[d] += vj * T1v[src + d];
+          dv[d] += dj * T1v[src + d];
+          vd[d] += vj * T1d[src + d];
+        }
+      }
+      for (int d = 0; d < 3; ++d) {
+        T2vv[3 * l + d] = vv[d];
+        T2dv[3 * l + d] = dv[d];
+        T2vd[3 * l + d] = vd[d];
+      }
+    }
+    __syncthreads();
+  }
   for (int l = threadIdx.x; l < n3; l += blockDim.x) {
     const int i = l / (n * n), j = (l / n) % n, k = l % n;
     double J[3][3];
@@ -172,19 +215,15 @@ __global__ void box_geometry_kernel(mfgb_box_desc b, GeomParams gp, double *__re
       }
     } else {
       for (int d = 0; d < 3; ++d) J[d][0] = J[d][1] = J[d][2] = 0.0;
-      for (int a = 0; a < ng; ++a)
-        for (int bb = 0; bb < ng; ++bb)
-          for (int c = 0; c < ng; ++c) {
-            const double *x = xyz + 3 * (a * ng * ng + bb * ng + c);
-            const double wr = gp.Dv[i * ng + a] * gp.V[j * ng + bb] * gp.V[k * ng + c];
-            const double ws = gp.V[i * ng + a] * gp.Dv[j * ng + bb] * gp.V[k * ng + c];
-            const double wt = gp.V[i * ng + a] * gp.V[j * ng + bb] * gp.Dv[k * ng + c];
-            for (int d = 0; d < 3; ++d) {
-              J[d][0] += wr * x[d];
-              J[d][1] += ws * x[d];
-              J[d][2] += wt * x[d];
-            }
-          }
+      for (int a = 0; a < ng; ++a) {
+        const int src = 3 * ((a * n + j) * n + k);
+        const double va = gp.V[i * ng + a], da = gp.Dv[i * ng + a];
+        for (int d = 0; d < 3; ++d) {
+          J[d][0] += da * T2vv[src + d];
+          J[d][1] += va * T2dv[src + d];
+          J[d][2] += va * T2vd[src + d];
+        }
+      }
     }
     const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
     const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
@@ -281,8 +320,18 @@ cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const doub
   if (n_cells == 0) return cudaSuccess;
   const int pts = std::max(n * n * n, gp.ng * gp.ng * gp.ng);
   const int threads = ((pts + 31) / 32) * 32;
-  box_geometry_kernel<<<(unsigned)n_cells, threads > 256 ? 256 : threads, 0, s>>>(b, gp, d_G,
-                                                                                   d_JxW);
+  // sum-factorisation arrays of the general path (at most 103 KB: ng = 9, n = 10),
+  // beside the 17.5 KB static node array: above 48 KB in total the kernel needs
+  // the larger dynamic limit
+  const size_t smem =
+      gp.general ? sizeof(double) * 3 * (2 * gp.ng * gp.ng * n + 3 * gp.ng * n * n) : 0;
+  if (smem > 0) {
+    cudaError_t e = cudaFuncSetAttribute(box_geometry_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  box_geometry_kernel<<<(unsigned)n_cells, threads > 256 ? 256 : threads, smem, s>>>(b, gp, d_G,
+                                                                                      d_JxW);
   return cudaGetLastError();
 }
 
