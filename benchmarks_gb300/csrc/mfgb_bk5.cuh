@@ -83,11 +83,11 @@ __device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uin
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc ar, as, at;
-      A::zero(ar);
-      A::zero(as);
-      A::zero(at);
+      A::mul(ar, basis.D[i * N], u[0]);
+      A::mul(as, Dj[0], s_u[el * N3 + i * N2 + k]);
+      A::mul(at, Dk[0], s_u[el * N3 + i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(ar, basis.D[i * N + m], u[m]);
         A::fma(as, Dj[m], s_u[el * N3 + i * N2 + m * N + k]);
         A::fma(at, Dk[m], s_u[el * N3 + i * N2 + j * N + m]);
@@ -100,12 +100,9 @@ __device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uin
       const V gst = A::load_g(__ldg(Gc + 4 * N3 + i * N2));
       const V gtt = A::load_g(__ldg(Gc + 5 * N3 + i * N2));
       Acc br, bs, bt;
-      A::zero(br);
-      A::zero(bs);
-      A::zero(bt);
-      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
       vr[i] = A::finish(br);
       s_vs[el * N3 + i * N2 + jk] = A::finish(bs);
       s_vt[el * N3 + i * N2 + jk] = A::finish(bt);
@@ -240,11 +237,11 @@ __global__ void __launch_bounds__(E * N * N * N)
     __syncthreads();
 
     Acc ar, as, at;
-    A::zero(ar);
-    A::zero(as);
-    A::zero(at);
+    A::mul(ar, s_D[i * N], su[j * N + k]);
+    A::mul(as, s_D[j * N], su[i * N2 + k]);
+    A::mul(at, s_D[k * N], su[i * N2 + j * N]);
 #pragma unroll
-    for (int m = 0; m < N; ++m) {
+    for (int m = 1; m < N; ++m) {
       A::fma(ar, s_D[i * N + m], su[m * N2 + j * N + k]);
       A::fma(as, s_D[j * N + m], su[i * N2 + m * N + k]);
       A::fma(at, s_D[k * N + m], su[i * N2 + j * N + m]);
@@ -253,23 +250,20 @@ __global__ void __launch_bounds__(E * N * N * N)
     const V grr = A::load_g(g0), grs = A::load_g(g1), grt = A::load_g(g2);
     const V gss = A::load_g(g3), gst = A::load_g(g4), gtt = A::load_g(g5);
     Acc br, bs, bt;
-    A::zero(br);
-    A::zero(bs);
-    A::zero(bt);
-    A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-    A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-    A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+    A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+    A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+    A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
     s_vr[tid] = A::finish(br);
     s_vs[tid] = A::finish(bs);
     s_vt[tid] = A::finish(bt);
     __syncthreads();
 
     Acc cr, cs, ct;
-    A::zero(cr);
-    A::zero(cs);
-    A::zero(ct);
+    A::mul(cr, s_D[i], svr[j * N + k]);
+    A::mul(cs, s_D[j], svs[i * N2 + k]);
+    A::mul(ct, s_D[k], svt[i * N2 + j * N]);
 #pragma unroll
-    for (int m = 0; m < N; ++m) {
+    for (int m = 1; m < N; ++m) {
       A::fma(cr, s_D[m * N + i], svr[m * N2 + j * N + k]);
       A::fma(cs, s_D[m * N + j], svs[i * N2 + m * N + k]);
       A::fma(ct, s_D[m * N + k], svt[i * N2 + j * N + m]);
@@ -503,11 +497,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc ar, as, at;
-      A::zero(ar);
-      A::zero(as);
-      A::zero(at);
+      A::mul(ar, basis.D[i * N], u[0]);
+      A::mul(as, Dj[0], s_u[el * N3 + i * N2 + k]);
+      A::mul(at, Dk[0], s_u[el * N3 + i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(ar, basis.D[i * N + m], u[m]);
         A::fma(as, Dj[m], s_u[el * N3 + i * N2 + m * N + k]);
         A::fma(at, Dk[m], s_u[el * N3 + i * N2 + j * N + m]);
@@ -523,12 +517,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
         gtt = A::load_g(Gc[5 * N3 + i * N2]);
       }
       Acc br, bs, bt;
-      A::zero(br);
-      A::zero(bs);
-      A::zero(bt);
-      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
       vr[i] = A::finish(br);
       s_vs[el * N3 + i * N2 + jk] = A::finish(bs);
       s_vt[el * N3 + i * N2 + jk] = A::finish(bt);
@@ -656,9 +647,9 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[k * N], sa[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[k * N + m], sa[i * N2 + j * N + m]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[k * N + m], sa[i * N2 + j * N + m]);
       t[i] = A::finish(a);
     }
 #pragma unroll
@@ -667,17 +658,17 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[j * N], sb[i * N2 + k]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[j * N + m], sb[i * N2 + m * N + k]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[j * N + m], sb[i * N2 + m * N + k]);
       t[i] = A::finish(a);
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[i * N], t[0]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[i * N + m], t[m]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[i * N + m], t[m]);
       u[i] = A::finish(a);
       sa[i * N2 + jk] = u[i];
     }
@@ -688,11 +679,11 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc ar, as, at;
-      A::zero(ar);
-      A::zero(as);
-      A::zero(at);
+      A::mul(ar, basis.D[i * N], u[0]);
+      A::mul(as, Dj[0], sa[i * N2 + k]);
+      A::mul(at, Dk[0], sa[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(ar, basis.D[i * N + m], u[m]);
         A::fma(as, Dj[m], sa[i * N2 + m * N + k]);
         A::fma(at, Dk[m], sa[i * N2 + j * N + m]);
@@ -705,12 +696,9 @@ __global__ void __launch_bounds__(E * N * N)
       const V gst = A::load_g(__ldg(Gc + 4 * N3 + i * N2));
       const V gtt = A::load_g(__ldg(Gc + 5 * N3 + i * N2));
       Acc br, bs, bt;
-      A::zero(br);
-      A::zero(bs);
-      A::zero(bt);
-      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
       vr[i] = A::finish(br);
       sb[i * N2 + jk] = A::finish(bs);
       sc[i * N2 + jk] = A::finish(bt);
@@ -734,9 +722,9 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[i], t[0]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + i], t[m]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[m * N + i], t[m]);
       u[i] = A::finish(a);
     }
     __syncthreads();  // sb / sc consumed
@@ -746,18 +734,18 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[j], sa[i * N2 + k]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + j], sa[i * N2 + m * N + k]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[m * N + j], sa[i * N2 + m * N + k]);
       sb[i * N2 + jk] = A::finish(a);
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[k], sb[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + k], sb[i * N2 + j * N + m]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[m * N + k], sb[i * N2 + j * N + m]);
       const V y = A::finish(a);
       if (idx[i] != MFGB_INVALID_DOF) {
         const VT yv = A::store_vec(y);
@@ -893,9 +881,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, c0[0], a0[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a0[i * N2 + j * N + m]);
+      for (int m = 1; m < N; ++m) A::fma(a, c0[m], a0[i * N2 + j * N + m]);
       a1[i * N2 + jk] = A::finish(a);
     }
     __syncthreads();
@@ -903,17 +891,17 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, c0[0], a1[i * N2 + k]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a1[i * N2 + m * N + k]);
+      for (int m = 1; m < N; ++m) A::fma(a, c0[m], a1[i * N2 + m * N + k]);
       t[i] = A::finish(a);
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[i * N], t[0]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[i * N + m], t[m]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[i * N + m], t[m]);
       u[i] = A::finish(a);
       a0[i * N2 + jk] = u[i];
     }
@@ -926,11 +914,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc ar, as, at;
-      A::zero(ar);
-      A::zero(as);
-      A::zero(at);
+      A::mul(ar, basis.D[i * N], u[0]);
+      A::mul(as, c0[0], a0[i * N2 + k]);
+      A::mul(at, c1[0], a0[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(ar, basis.D[i * N + m], u[m]);
         A::fma(as, c0[m], a0[i * N2 + m * N + k]);
         A::fma(at, c1[m], a0[i * N2 + j * N + m]);
@@ -946,12 +934,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
         gtt = A::load_g(Gc[5 * N3 + i * N2]);
       }
       Acc br, bs, bt;
-      A::zero(br);
-      A::zero(bs);
-      A::zero(bt);
-      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
       vr[i] = A::finish(br);
       a1[i * N2 + jk] = A::finish(bs);
       a2[i * N2 + jk] = A::finish(bt);
@@ -992,9 +977,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.B[i], t[0]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, basis.B[m * N + i], t[m]);
+      for (int m = 1; m < N; ++m) A::fma(a, basis.B[m * N + i], t[m]);
       u[i] = A::finish(a);
     }
     // W0's last readers (the gradient) finished before barrier C
@@ -1005,9 +990,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, c0[0], a0[i * N2 + k]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a0[i * N2 + m * N + k]);
+      for (int m = 1; m < N; ++m) A::fma(a, c0[m], a0[i * N2 + m * N + k]);
       a1[i * N2 + jk] = A::finish(a);
     }
     __syncthreads();
@@ -1015,9 +1000,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, c0[0], a1[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) A::fma(a, c0[m], a1[i * N2 + j * N + m]);
+      for (int m = 1; m < N; ++m) A::fma(a, c0[m], a1[i * N2 + j * N + m]);
       if (cur[i] != MFGB_INVALID_DOF) atomicAdd(dst + cur[i], A::store_vec(A::finish(a)));
     }
     // W1 is read above until barrier A of the next batch; W0 is rewritten only after it
@@ -1084,11 +1069,11 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         Acc ar, as, at;
-        A::zero(ar);
-        A::zero(as);
-        A::zero(at);
+        A::mul(ar, basis.D[i * N], u[0]);
+        A::mul(as, Dj[0], s_u[el * N3 + i * N2 + k]);
+        A::mul(at, Dk[0], s_u[el * N3 + i * N2 + j * N]);
 #pragma unroll
-        for (int m = 0; m < N; ++m) {
+        for (int m = 1; m < N; ++m) {
           A::fma(ar, basis.D[i * N + m], u[m]);
           A::fma(as, Dj[m], s_u[el * N3 + i * N2 + m * N + k]);
           A::fma(at, Dk[m], s_u[el * N3 + i * N2 + j * N + m]);
@@ -1104,12 +1089,9 @@ __global__ void __launch_bounds__(E * N * N)
           gtt = A::load_g(Gc[5 * N3 + i * N2]);
         }
         Acc br, bs, bt;
-        A::zero(br);
-        A::zero(bs);
-        A::zero(bt);
-        A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-        A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-        A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+        A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+        A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+        A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
         vr[i] = A::finish(br);
         s_vs[el * N3 + i * N2 + jk] = A::finish(bs);
         s_vt[el * N3 + i * N2 + jk] = A::finish(bt);

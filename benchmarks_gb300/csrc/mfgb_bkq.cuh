@@ -75,9 +75,9 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int p = 0; p < NQ; ++p) {
         Acc a;
-        A::zero(a);
+        A::mul(a, sB[p * NM], r[0]);
 #pragma unroll
-        for (int i = 0; i < NM; ++i) A::fma(a, sB[p * NM + i], r[i]);
+        for (int i = 1; i < NM; ++i) A::fma(a, sB[p * NM + i], r[i]);
         a1[p * NM2 + t] = A::finish(a);
       }
     }
@@ -91,9 +91,9 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         Acc a;
-        A::zero(a);
+        A::mul(a, sB[q * NM], r[0]);
 #pragma unroll
-        for (int j = 0; j < NM; ++j) A::fma(a, sB[q * NM + j], r[j]);
+        for (int j = 1; j < NM; ++j) A::fma(a, sB[q * NM + j], r[j]);
         a0[(p * NQ + q) * NM + k] = A::finish(a);
       }
     }
@@ -106,9 +106,9 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int rr = 0; rr < NQ; ++rr) {
         Acc a;
-        A::zero(a);
+        A::mul(a, sB[rr * NM], r[0]);
 #pragma unroll
-        for (int k = 0; k < NM; ++k) A::fma(a, sB[rr * NM + k], r[k]);
+        for (int k = 1; k < NM; ++k) A::fma(a, sB[rr * NM + k], r[k]);
         V v = A::finish(a);
         if (!LAPLACE) {  // mass: JxW at the point
           Acc m;
@@ -131,11 +131,11 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int p = 0; p < NQ; ++p) {
         Acc ar, as, at;
-        A::zero(ar);
-        A::zero(as);
-        A::zero(at);
+        A::mul(ar, sD[p * NQ], u[0]);
+        A::mul(as, sD[q * NQ], a1[p * NQ2 + r]);
+        A::mul(at, sD[r * NQ], a1[p * NQ2 + q * NQ]);
 #pragma unroll
-        for (int m = 0; m < NQ; ++m) {
+        for (int m = 1; m < NQ; ++m) {
           A::fma(ar, sD[p * NQ + m], u[m]);
           A::fma(as, sD[q * NQ + m], a1[p * NQ2 + m * NQ + r]);
           A::fma(at, sD[r * NQ + m], a1[p * NQ2 + q * NQ + m]);
@@ -148,12 +148,9 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
         const V gst = A::load_vec(__ldg(Ge + 4 * NQ3 + p * NQ2));
         const V gtt = A::load_vec(__ldg(Ge + 5 * NQ3 + p * NQ2));
         Acc br, bs, bt;
-        A::zero(br);
-        A::zero(bs);
-        A::zero(bt);
-        A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-        A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-        A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+        A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+        A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+        A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
         vr[p] = A::finish(br);
         a2[p * NQ2 + lt] = A::finish(bs);
         a3[p * NQ2 + lt] = A::finish(bt);
@@ -181,9 +178,9 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int k = 0; k < NM; ++k) {
         Acc a;
-        A::zero(a);
+        A::mul(a, sB[k], r[0]);
 #pragma unroll
-        for (int rr = 0; rr < NQ; ++rr) A::fma(a, sB[rr * NM + k], r[rr]);
+        for (int rr = 1; rr < NQ; ++rr) A::fma(a, sB[rr * NM + k], r[rr]);
         a0[lt * NM + k] = A::finish(a);
       }
     }
@@ -197,9 +194,9 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int j = 0; j < NM; ++j) {
         Acc a;
-        A::zero(a);
+        A::mul(a, sB[j], r[0]);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) A::fma(a, sB[q * NM + j], r[q]);
+        for (int q = 1; q < NQ; ++q) A::fma(a, sB[q * NM + j], r[q]);
         a1[p * NM2 + j * NM + k] = A::finish(a);
       }
     }
@@ -212,9 +209,9 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int i = 0; i < NM; ++i) {
         Acc a;
-        A::zero(a);
+        A::mul(a, sB[i], r[0]);
 #pragma unroll
-        for (int p = 0; p < NQ; ++p) A::fma(a, sB[p * NM + i], r[p]);
+        for (int p = 1; p < NQ; ++p) A::fma(a, sB[p * NM + i], r[p]);
         if (!valid) continue;
         if (map) {  // scatter-add (atomic: DoFs shared between cells)
           const uint32_t d = __ldg(map + e * NM3 + i * NM2 + t);
@@ -338,9 +335,9 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
 #pragma unroll
       for (int i = 0; i < NM; ++i) {
         Acc s;
-        A::zero(s);
+        A::mul(s, c0[0], W0[i * M2 + a * NM]);
 #pragma unroll
-        for (int m = 0; m < NM; ++m) A::fma(s, c0[m], W0[i * M2 + a * NM + m]);
+        for (int m = 1; m < NM; ++m) A::fma(s, c0[m], W0[i * M2 + a * NM + m]);
         W1[i * MQ + a * NQ + b] = A::finish(s);
       }
     }
@@ -353,17 +350,17 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
 #pragma unroll
       for (int i = 0; i < NM; ++i) {
         Acc s;
-        A::zero(s);
+        A::mul(s, c0[0], W1[i * MQ + b]);
 #pragma unroll
-        for (int m = 0; m < NM; ++m) A::fma(s, c0[m], W1[i * MQ + m * NQ + b]);
+        for (int m = 1; m < NM; ++m) A::fma(s, c0[m], W1[i * MQ + m * NQ + b]);
         t[i] = A::finish(s);
       }
 #pragma unroll 1
       for (int q = 0; q < NQ; ++q) {
         Acc s;
-        A::zero(s);
+        A::mul(s, sB[q * NM], t[0]);
 #pragma unroll
-        for (int i = 0; i < NM; ++i) A::fma(s, sB[q * NM + i], t[i]);
+        for (int i = 1; i < NM; ++i) A::fma(s, sB[q * NM + i], t[i]);
         W0[q * Q2 + ab] = A::finish(s);
       }
     }
@@ -378,11 +375,11 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       Acc ar, as, at;
-      A::zero(ar);
-      A::zero(as);
-      A::zero(at);
+      A::mul(ar, sD[q * NQ], W0[ab]);
+      A::mul(as, c0[0], W0[q * Q2 + b]);
+      A::mul(at, c1[0], W0[q * Q2 + a * NQ]);
 #pragma unroll
-      for (int m = 0; m < NQ; ++m) {
+      for (int m = 1; m < NQ; ++m) {
         A::fma(ar, sD[q * NQ + m], W0[m * Q2 + ab]);
         A::fma(as, c0[m], W0[q * Q2 + m * NQ + b]);
         A::fma(at, c1[m], W0[q * Q2 + a * NQ + m]);
@@ -398,12 +395,9 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
         gtt = A::load_g(Gc[5 * Q3 + q * Q2]);
       }
       Acc br, bs, bt;
-      A::zero(br);
-      A::zero(bs);
-      A::zero(bt);
-      A::fma(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
-      A::fma(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
-      A::fma(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+      A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+      A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+      A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
       W3[q * Q2 + ab] = A::finish(br);
       W1[q * Q2 + ab] = A::finish(bs);
       W2[q * Q2 + ab] = A::finish(bt);
@@ -459,9 +453,9 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
 #pragma unroll
       for (int i = 0; i < NM; ++i) {
         Acc s;
-        A::zero(s);
+        A::mul(s, c0[0], W0[i * Q2 + b]);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) A::fma(s, c0[q], W0[i * Q2 + q * NQ + b]);
+        for (int q = 1; q < NQ; ++q) A::fma(s, c0[q], W0[i * Q2 + q * NQ + b]);
         W1[i * MQ + a * NQ + b] = A::finish(s);
       }
     }
@@ -473,9 +467,9 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
 #pragma unroll
       for (int i = 0; i < NM; ++i) {
         Acc s;
-        A::zero(s);
+        A::mul(s, c0[0], W1[i * MQ + a * NQ]);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) A::fma(s, c0[q], W1[i * MQ + a * NQ + q]);
+        for (int q = 1; q < NQ; ++q) A::fma(s, c0[q], W1[i * MQ + a * NQ + q]);
         if (cur[i] != MFGB_INVALID_DOF) atomicAdd(dst + cur[i], A::store_vec(A::finish(s)));
       }
     }

@@ -89,6 +89,15 @@ __device__ __forceinline__ void dfacc_fma(dfacc &a, df x, df y) {
   a.c = c;
 }
 
+// a = x * y  (the first term of a sum: the same value as dfacc_zero then
+// dfacc_fma, without the addition to zero)
+__device__ __forceinline__ void dfacc_set(dfacc &a, df x, df y) {
+  a.s = __fmul_rn(x.hi, y.hi);
+  float c = __fmaf_rn(x.hi, y.hi, -a.s);
+  c = __fmaf_rn(x.hi, y.lo, c);
+  a.c = __fmaf_rn(x.lo, y.hi, c);
+}
+
 // a += b  (two lazy accumulators)
 __device__ __forceinline__ void dfacc_merge(dfacc &a, const dfacc &b) {
   float s, t;
@@ -108,7 +117,7 @@ __device__ __forceinline__ df dfacc_finish(const dfacc &a) {
 // ----------------------------------------------------- arithmetic policies --
 // Every policy defines:
 //   V       value type carried through the contractions
-//   Acc     accumulator type
+//   Acc     accumulator type (zero / fma / mul = set to the first product)
 //   GType   storage type of one geometric-factor component
 //   VecT    L-vector element type
 struct ArithF64 {
@@ -118,6 +127,7 @@ struct ArithF64 {
   using VecT = double;
   static __device__ __forceinline__ void zero(Acc &a) { a = 0.0; }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fma_rn(x, y, a); }
+  static __device__ __forceinline__ void mul(Acc &a, V x, V y) { a = __dmul_rn(x, y); }
   static __device__ __forceinline__ void merge(Acc &a, const Acc &b) { a = __dadd_rn(a, b); }
   static __device__ __forceinline__ V finish(const Acc &a) { return a; }
   static __device__ __forceinline__ V load_vec(VecT x) { return x; }
@@ -134,6 +144,7 @@ struct ArithF32 {
   using VecT = float;
   static __device__ __forceinline__ void zero(Acc &a) { a = 0.f; }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fmaf_rn(x, y, a); }
+  static __device__ __forceinline__ void mul(Acc &a, V x, V y) { a = __fmul_rn(x, y); }
   static __device__ __forceinline__ void merge(Acc &a, const Acc &b) { a = __fadd_rn(a, b); }
   static __device__ __forceinline__ V finish(const Acc &a) { return a; }
   static __device__ __forceinline__ V load_vec(VecT x) { return x; }
@@ -150,6 +161,7 @@ struct ArithDF {
   using VecT = double;
   static __device__ __forceinline__ void zero(Acc &a) { dfacc_zero(a); }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { dfacc_fma(a, x, y); }
+  static __device__ __forceinline__ void mul(Acc &a, V x, V y) { dfacc_set(a, x, y); }
   static __device__ __forceinline__ void merge(Acc &a, const Acc &b) { dfacc_merge(a, b); }
   static __device__ __forceinline__ V finish(const Acc &a) { return dfacc_finish(a); }
   static __device__ __forceinline__ V load_vec(VecT x) { return df_from_double(x); }
