@@ -106,11 +106,15 @@ __device__ __forceinline__ void dfacc_merge(dfacc &a, const dfacc &b) {
   a.c = __fadd_rn(a.c, __fadd_rn(b.c, t));
 }
 
+// The accumulator as a value: the pair (s, c) itself, not renormalised (|c| may
+// exceed half an ulp of s).  Its consumers accept that: a product uses hi*hi
+// exactly and the two cross terms in float (dropping lo*lo), which keeps the
+// error at the 2^-48 level of the terms, and the conversion to double adds
+// hi and lo with one rounding.
 __device__ __forceinline__ df dfacc_finish(const dfacc &a) {
   df r;
-  float t;
-  two_sum(a.s, a.c, r.hi, t);
-  r.lo = t;
+  r.hi = a.s;
+  r.lo = a.c;
   return r;
 }
 
