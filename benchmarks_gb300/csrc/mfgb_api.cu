@@ -110,7 +110,7 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
 // shape per degree measured on a GB300 at ~3e7 DoFs (autotune.py re-measures).
 static int g_shape[3][10] = {
     {0, 0, 4, 3, 2, 4, 2, 1, 2, 1},  // FP64
-    {2, 2, 2, 4, 2, 4, 0, 2, 2, 2},  // double-float
+    {2, 2, 4, 4, 4, 4, 1, 1, 2, 1},  // double-float
     {0, 0, 3, 3, 0, 3, 2, 4, 4, 2},  // FP32
 };
 
