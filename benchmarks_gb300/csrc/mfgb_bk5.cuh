@@ -113,9 +113,11 @@ __device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uin
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.D[i], vr[0]);
+      A::fma(a, Dtj[0], s_vs[el * N3 + i * N2 + k]);
+      A::fma(a, Dtk[0], s_vt[el * N3 + i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(a, basis.D[m * N + i], vr[m]);
         A::fma(a, Dtj[m], s_vs[el * N3 + i * N2 + m * N + k]);
         A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
@@ -550,9 +552,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.D[i], vr[0]);
+      A::fma(a, Dtj[0], s_vs[el * N3 + i * N2 + k]);
+      A::fma(a, Dtk[0], s_vt[el * N3 + i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(a, basis.D[m * N + i], vr[m]);
         A::fma(a, Dtj[m], s_vs[el * N3 + i * N2 + m * N + k]);
         A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
@@ -709,9 +713,11 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.D[i], vr[0]);
+      A::fma(a, Dtj[0], sb[i * N2 + k]);
+      A::fma(a, Dtk[0], sc[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(a, basis.D[m * N + i], vr[m]);
         A::fma(a, Dtj[m], sb[i * N2 + m * N + k]);
         A::fma(a, Dtk[m], sc[i * N2 + j * N + m]);
@@ -964,9 +970,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::zero(a);
+      A::mul(a, basis.D[i], vr[0]);
+      A::fma(a, c0[0], a1[i * N2 + k]);
+      A::fma(a, c1[0], a2[i * N2 + j * N]);
 #pragma unroll
-      for (int m = 0; m < N; ++m) {
+      for (int m = 1; m < N; ++m) {
         A::fma(a, basis.D[m * N + i], vr[m]);
         A::fma(a, c0[m], a1[i * N2 + m * N + k]);
         A::fma(a, c1[m], a2[i * N2 + j * N + m]);
@@ -1100,9 +1108,11 @@ __global__ void __launch_bounds__(E * N * N)
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         Acc a;
-        A::zero(a);
+        A::mul(a, basis.D[i], vr[0]);
+        A::fma(a, Dtj[0], s_vs[el * N3 + i * N2 + k]);
+        A::fma(a, Dtk[0], s_vt[el * N3 + i * N2 + j * N]);
 #pragma unroll
-        for (int m = 0; m < N; ++m) {
+        for (int m = 1; m < N; ++m) {
           A::fma(a, basis.D[m * N + i], vr[m]);
           A::fma(a, Dtj[m], s_vs[el * N3 + i * N2 + m * N + k]);
           A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
@@ -1111,6 +1121,196 @@ __global__ void __launch_bounds__(E * N * N)
         if (idx[i] != MFGB_INVALID_DOF) atomicAdd(dst + (size_t)NC * idx[i] + c, A::store_vec(y));
       }
       __syncthreads();
+    }
+  }
+}
+
+
+// BK6 with the bulk-TMA pipeline of bk5_tma_kernel: a batch's G tile (shared by
+// the NC components) and the next batch's map tile arrive by bulk copies, and
+// each component's gather is prefetched into registers during the integrate
+// phase of the previous component (the next batch's first component during the
+// last one).  Per batch of E cells:
+//   A  wait G(b)
+//   for each component c:
+//        s_u = u_c (prefetched); B (c = 0: TMA map(b+next))
+//        gradient + metric -> vr, s_vs, s_vt; C (last c: TMA G(b+next))
+//        prefetch u_{c+1} (or, for the last c, wait map(b+next) and gather its u_0)
+//        integrate + atomic scatter of component c
+// Every wait is bounded (a timeout sets err_flag and the CTA returns).
+template <int N, int E, class A, int NC, int MB>
+__global__ void __launch_bounds__(E * N * N, MB)
+    bk6_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                   const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
+                   typename A::VecT *__restrict__ dst, const Basis<N, A> basis,
+                   int *__restrict__ err_flag) {
+  using V = typename A::V;
+  using Acc = typename A::Acc;
+  using GT = typename A::GType;
+  using VT = typename A::VecT;
+  using L = TmaLayout<N, E, A>;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  extern __shared__ __align__(128) unsigned char smem[];
+  GT *sG = reinterpret_cast<GT *>(smem);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *s_u = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
+  V *s_vs = s_u + E * N3;
+  V *s_vt = s_vs + E * N3;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+  uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
+
+  const int tid = threadIdx.x;
+  const int el = tid / N2;
+  const int jk = tid - el * N2;
+  const int j = jk / N;
+  const int k = jk - j * N;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  int64_t batch = blockIdx.x;
+  if (batch >= n_batches) return;  // uniform across the CTA
+
+  V Dj[N], Dk[N], Dtj[N], Dtk[N];
+#pragma unroll
+  for (int m = 0; m < N; ++m) {
+    Dj[m] = basis.D[j * N + m];
+    Dk[m] = basis.D[k * N + m];
+    Dtj[m] = basis.D[m * N + j];
+    Dtk[m] = basis.D[m * N + k];
+  }
+  const TmaTiles<N, E, A> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
+  // dof indices of column (el, jk) of batch b, from the map tile or global
+  auto indices = [&](int64_t b, uint32_t *idx) {
+    const int cells = T.cells_of(b);
+    const bool valid = el < cells;
+    const bool mt = T.map_by_tma(cells);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      idx[i] = valid ? (mt ? sMap[el * N3 + i * N2 + jk] : __ldg(map + (b * E + el) * N3 + i * N2 + jk))
+                     : MFGB_INVALID_DOF;
+  };
+  auto gather = [&](const uint32_t *idx, int c, VT *raw) {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + (size_t)NC * idx[i] + c) : VT(0);
+  };
+  auto fail = [&](uint32_t pg, uint32_t pm) {
+    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
+    mbar_wait(mbar_m, pm);
+  };
+
+  if (tid == 0) {
+    mbar_init(mbar_g, 1);
+    mbar_init(mbar_m, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    T.issue_g(batch);
+    T.issue_map(batch);
+  }
+  uint32_t ph_g = 0, ph_m = 0;
+  uint32_t idx[N], nidx[N];
+  VT raw[N];
+  {
+    const bool ok = mbar_wait(mbar_m, ph_m);
+    if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
+    ph_m ^= 1u;
+    indices(batch, idx);
+    gather(idx, 0, raw);
+  }
+
+  for (; batch < n_batches; batch += gridDim.x) {
+    const int64_t next = batch + gridDim.x;
+    const bool has_next = next < n_batches;
+    const bool okg = mbar_wait(mbar_g, ph_g);
+    if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
+    ph_g ^= 1u;
+    T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase by barrier B
+    const bool valid = el < T.cells_of(batch);
+    const GT *Gc = sG + el * 6 * N3 + jk;
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c) {
+      V u[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        u[i] = idx[i] != MFGB_INVALID_DOF ? A::load_vec(raw[i]) : A::zero_v();
+        s_u[el * N3 + i * N2 + jk] = u[i];
+      }
+      __syncthreads();  // barrier B: s_u ready (c = 0: the map tile is free)
+      if (c == 0 && tid == 0 && has_next) {
+        fence_proxy_async_smem();
+        T.issue_map(next);
+      }
+      V vr[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        Acc ar, as, at;
+        A::mul(ar, basis.D[i * N], u[0]);
+        A::mul(as, Dj[0], s_u[el * N3 + i * N2 + k]);
+        A::mul(at, Dk[0], s_u[el * N3 + i * N2 + j * N]);
+#pragma unroll
+        for (int m = 1; m < N; ++m) {
+          A::fma(ar, basis.D[i * N + m], u[m]);
+          A::fma(as, Dj[m], s_u[el * N3 + i * N2 + m * N + k]);
+          A::fma(at, Dk[m], s_u[el * N3 + i * N2 + j * N + m]);
+        }
+        const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+        V grr = A::zero_v(), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+        if (valid) {
+          grr = A::load_g(Gc[0 * N3 + i * N2]);
+          grs = A::load_g(Gc[1 * N3 + i * N2]);
+          grt = A::load_g(Gc[2 * N3 + i * N2]);
+          gss = A::load_g(Gc[3 * N3 + i * N2]);
+          gst = A::load_g(Gc[4 * N3 + i * N2]);
+          gtt = A::load_g(Gc[5 * N3 + i * N2]);
+        }
+        Acc br, bs, bt;
+        A::mul(br, grr, qr); A::fma(br, grs, qs); A::fma(br, grt, qt);
+        A::mul(bs, grs, qr); A::fma(bs, gss, qs); A::fma(bs, gst, qt);
+        A::mul(bt, grt, qr); A::fma(bt, gst, qs); A::fma(bt, gtt, qt);
+        vr[i] = A::finish(br);
+        s_vs[el * N3 + i * N2 + jk] = A::finish(bs);
+        s_vt[el * N3 + i * N2 + jk] = A::finish(bt);
+      }
+      __syncthreads();  // barrier C: s_vs / s_vt ready (last c: the G tile is consumed)
+      if (c == NC - 1 && tid == 0 && has_next) {
+        fence_proxy_async_smem();
+        T.issue_g(next);
+      }
+      // prefetch the next component (or the next batch's first one)
+      uint32_t cur[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) cur[i] = idx[i];
+      if (c + 1 < NC) {
+        gather(idx, c + 1, raw);
+      } else if (has_next) {
+        const bool okm = mbar_wait(mbar_m, ph_m);
+        if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+        ph_m ^= 1u;
+        if (okm) {
+          indices(next, nidx);
+#pragma unroll
+          for (int i = 0; i < N; ++i) idx[i] = nidx[i];
+          gather(idx, 0, raw);
+        } else {
+          for (int i = 0; i < N; ++i) { idx[i] = MFGB_INVALID_DOF; raw[i] = VT(0); }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        Acc a;
+        A::mul(a, basis.D[i], vr[0]);
+        A::fma(a, Dtj[0], s_vs[el * N3 + i * N2 + k]);
+        A::fma(a, Dtk[0], s_vt[el * N3 + i * N2 + j * N]);
+#pragma unroll
+        for (int m = 1; m < N; ++m) {
+          A::fma(a, basis.D[m * N + i], vr[m]);
+          A::fma(a, Dtj[m], s_vs[el * N3 + i * N2 + m * N + k]);
+          A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
+        }
+        if (cur[i] != MFGB_INVALID_DOF)
+          atomicAdd(dst + (size_t)NC * cur[i] + c, A::store_vec(A::finish(a)));
+      }
     }
   }
 }

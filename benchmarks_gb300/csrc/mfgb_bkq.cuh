@@ -159,9 +159,11 @@ __global__ void __launch_bounds__(NQ * NQ * BkqElems<NQ>::value)
 #pragma unroll
       for (int p = 0; p < NQ; ++p) {
         Acc a;
-        A::zero(a);
+        A::mul(a, sD[p], vr[0]);
+        A::fma(a, sD[q], a2[p * NQ2 + r]);
+        A::fma(a, sD[r], a3[p * NQ2 + q * NQ]);
 #pragma unroll
-        for (int m = 0; m < NQ; ++m) {
+        for (int m = 1; m < NQ; ++m) {
           A::fma(a, sD[m * NQ + p], vr[m]);
           A::fma(a, sD[m * NQ + q], a2[p * NQ2 + m * NQ + r]);
           A::fma(a, sD[m * NQ + r], a3[p * NQ2 + q * NQ + m]);
@@ -431,9 +433,11 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       Acc s;
-      A::zero(s);
+      A::mul(s, sD[q], W3[ab]);
+      A::fma(s, c0[0], W1[q * Q2 + b]);
+      A::fma(s, c1[0], W2[q * Q2 + a * NQ]);
 #pragma unroll
-      for (int m = 0; m < NQ; ++m) {
+      for (int m = 1; m < NQ; ++m) {
         A::fma(s, sD[m * NQ + q], W3[m * Q2 + ab]);
         A::fma(s, c0[m], W1[q * Q2 + m * NQ + b]);
         A::fma(s, c1[m], W2[q * Q2 + a * NQ + m]);

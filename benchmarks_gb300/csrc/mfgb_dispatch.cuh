@@ -118,6 +118,9 @@ cudaError_t bk5g_dispatch(int N, int64_t n_cells, const uint32_t *map, const typ
 
 namespace mfgb {
 
+// cells per CTA of the BK6 TMA kernel: as the Gauss-point one
+template <int N> struct Bk6TmaElems { static constexpr int value = GaussTmaElems<N>::value; };
+
 template <int N, class A>
 cudaError_t bk6_with_basis(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
                            const typename A::VecT *src, typename A::VecT *dst, const double *D64,
@@ -127,9 +130,24 @@ cudaError_t bk6_with_basis(int64_t n_cells, const uint32_t *map, const typename 
   for (int q = 0; q < N * N; ++q) b.D[q] = BasisValue<A>::from(D64[q]);
   const size_t smem = sizeof(typename A::GType) * E * 6 * N * N * N +
                       3 * sizeof(typename A::V) * E * N * N * N;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  // 16-byte aligned G and map: the bulk-TMA pipeline
+  if (((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(map)) & 15u) == 0) {
+    constexpr int ET = Bk6TmaElems<N>::value;
+    constexpr int MB = GaussTmaMinBlocks<N, ET, A>::value;
+    constexpr size_t smem_t = TmaLayout<N, ET, A>::total;
+    static int per_sm_tma = -1;
+    if (per_sm_tma < 0)
+      per_sm_tma = std::max(1, ctas_per_sm(bk6_tma_kernel<N, ET, A, 3, MB>, ET * N * N, smem_t));
+    const int64_t nb = (n_cells + ET - 1) / ET;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)per_sm_tma * num_sms()));
+    if (n_cells <= 0) return cudaSuccess;
+    bk6_tma_kernel<N, ET, A, 3, MB><<<g, ET * N * N, smem_t, s>>>(n_cells, map, G, src, dst, b,
+                                                                  device_error_flag());
+    return cudaGetLastError();
+  }
   static int per_sm = -1;
   if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk6_kernel<N, E, A, 3>, E * N * N, smem));
-  const int64_t n_batches = (n_cells + E - 1) / E;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>(n_batches, (int64_t)per_sm * num_sms()));
   if (n_cells <= 0) return cudaSuccess;
   bk6_kernel<N, E, A, 3><<<g, E * N * N, smem, s>>>(n_cells, map, G, src, dst, b);

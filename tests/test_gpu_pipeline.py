@@ -2,7 +2,7 @@
 pipelined path runs: the next batch's G and dof-map tiles copied while the
 current batch computes, and the next gather prefetched into registers.  The
 small meshes of the other tests give every CTA at most one batch.  Collocation
-(every TMA shape), Gauss-point, Helmholtz and BP3 forms against the oracle; 1e-12
+(every TMA shape), Gauss-point, Helmholtz, BP3 and BK6 forms against the oracle; 1e-12
 relative for FP64 and double-float, 1e-5 for FP32."""
 import ctypes
 
@@ -130,3 +130,23 @@ def test_bp3_tma_pipelined(mf, orc, p, arith):
     A.vmult(y, torch.from_numpy(src).cuda())
     _abi.check(mf.lib().mfgb_check_device_errors(None))
     assert rel(y.cpu().numpy(), ref.apply(src)) <= 1e-12
+
+
+@pytest.mark.parametrize("arith", ["df", "fp64"])
+@pytest.mark.parametrize("p", [2, 4, 7])
+def test_bk6_tma_pipelined(mf, orc, p, arith):
+    """BK6 (3 interleaved components): each component through the scalar
+    operator, with the component gathers prefetched across batches."""
+    import torch
+    from benchmarks_gb300 import _abi
+    cells = MESH[p]
+    A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.06))
+    ref = orc.BoxProblem(*cells, p, amplitude=0.06)
+    src = np.random.default_rng(p + 20).uniform(-1, 1, 3 * ref.n_dofs)
+    y = torch.zeros(3 * ref.n_dofs, dtype=torch.float64, device="cuda")
+    A.vmult_vector(y, torch.from_numpy(src).cuda(), arith=arith)
+    _abi.check(mf.lib().mfgb_check_device_errors(None))
+    want = np.empty_like(src)
+    for c in range(3):
+        want[c::3] = ref.apply(src[c::3])
+    assert rel(y.cpu().numpy(), want) <= 1e-12
