@@ -543,6 +543,7 @@ mfgb_status mfgb_set_host_pipeline(int slabs) {
 // completes (identity rows applied), while the next slab's planes arrive.
 // Slab k covers cell layers [z0, z1) and DoF planes p z0 .. p z1; plane p z1 is
 // shared with slab k + 1, so it is finished (and copied back) by slab k + 1.
+// The copies' ends are moved to page boundaries of the host buffers (below).
 mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const double *h_src, int arith,
                             void *stream) {
   if (!cop || (cop->n_dofs > 0 && (!h_dst || !h_src)) || h_dst == h_src ||

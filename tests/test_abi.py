@@ -60,3 +60,29 @@ def test_invalid_arguments_are_rejected_without_gpu(libmfgb):
     assert L.mfgb_cg_solve(None, None, None, None, None, None, None) == _abi.ERR_INVALID_ARG
     with pytest.raises(ValueError):
         mf._arith("fp16")
+
+
+def test_kernel_shape_table_round_trip_without_gpu(libmfgb):
+    """The autotuner's shape table (thread layout and cells per CTA per degree):
+    every shape the autotuner times is accepted, others are rejected, and the
+    defaults come back after a round trip.  Host-only calls."""
+    import benchmarks_gb300 as mf
+    from benchmarks_gb300 import _abi, autotune
+    L = mf.lib()
+    assert tuple(autotune.SHAPES) == (0, 1, 2, 3, 4)
+    for arith in autotune.ARITHS.values():
+        for degree in range(1, 9):
+            old = ctypes.c_int()
+            assert L.mfgb_get_kernel_shape(arith, degree, ctypes.byref(old)) == _abi.OK
+            assert old.value in autotune.SHAPES
+            for shape in autotune.SHAPES:
+                assert L.mfgb_set_kernel_shape(arith, degree, shape) == _abi.OK
+                got = ctypes.c_int()
+                assert L.mfgb_get_kernel_shape(arith, degree, ctypes.byref(got)) == _abi.OK
+                assert got.value == shape
+            assert L.mfgb_set_kernel_shape(arith, degree, old.value) == _abi.OK
+    assert L.mfgb_set_kernel_shape(1, 4, 5) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_set_kernel_shape(1, 9, 0) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_set_kernel_shape(3, 4, 0) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_set_host_pipeline(65) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_set_host_pipeline(0) == _abi.OK  # automatic slab count
