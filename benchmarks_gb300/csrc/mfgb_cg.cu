@@ -199,6 +199,17 @@ __global__ void finish_sum_kernel(const double *__restrict__ partials, int n, in
   if (threadIdx.x == 0) *out = s;
 }
 
+int dot_partials_count() { return VEC_BLOCKS; }
+
+// a.b into device memory (*out), stream ordered, no host synchronisation;
+// partials holds dot_partials_count() doubles
+cudaError_t dot_to_device(int64_t n, const double *a, const double *b, double *partials,
+                          double *out, cudaStream_t s) {
+  dot_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, a, b, partials);
+  finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(partials, VEC_BLOCKS, 1, out);
+  return cudaGetLastError();
+}
+
 }  // namespace mfgb
 
 using namespace mfgb;

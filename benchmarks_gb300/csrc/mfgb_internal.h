@@ -105,6 +105,12 @@ cudaError_t box_geometry(const mfgb_box_desc &b, const double *gll_x, const doub
 cudaError_t diagonal_gauss(int N, int NQ, int64_t n_cells, const uint32_t *map, const double *G,
                            const double *JxW, const double *B, const double *DG, double *diag,
                            cudaStream_t s);
+// device-side dot product (mfgb_cg.cu): *out = a.b, stream ordered, without a
+// host synchronisation; partials holds dot_partials_count() doubles
+int dot_partials_count();
+cudaError_t dot_to_device(int64_t n, const double *a, const double *b, double *partials,
+                          double *out, cudaStream_t s);
+
 // BP3 operator (mfgb_bkq.cu): dst += A src, q = p + 2 Gauss points, G[cell][6][nq^3]
 // in FP64 (G) and, for double-float arithmetic, as pairs (Gdf); the bases on the
 // device (d_B, d_DG) and on the host (h_B, h_DG)

@@ -345,7 +345,15 @@ mfgb_status mg_apply(mfgb_mg *mg, double *dst, const double *src, cudaStream_t s
   return cuda_status(cudaGetLastError(), "mg apply");
 }
 
-// lambda_max of Dinv A by power iteration (FP64 host-driven, set-up only)
+// v += (1/sqrt(*nv) - 1) v, i.e. v / |v| as the host formula 1/sqrt then axpy
+// (0 for a zero vector)
+__global__ void k_normalize(int64_t n, const double *__restrict__ nv, double *__restrict__ v) {
+  const double s = *nv;
+  const double a = (s > 0 ? 1.0 / sqrt(s) : 0.0) - 1.0;
+  GRID_STRIDE(t, n) v[t] += a * v[t];
+}
+
+// lambda_max of Dinv A by power iteration (FP64, device scalars; set-up only)
 mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
                           const double *dinv_given = nullptr) {
   const int64_t n = L.n;
@@ -355,14 +363,22 @@ mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
     st64 ^= st64 << 13; st64 ^= st64 >> 7; st64 ^= st64 << 17;
     h[i] = 0.5 + (double)(st64 >> 11) * (1.0 / 9007199254740992.0);
   }
-  double *v = nullptr, *w = nullptr, *dinv = nullptr;
+  // scratch: dot partials, then |v|^2 and the Rayleigh quotient (device scalars:
+  // the iteration runs without host synchronisation, one read at the end)
+  const int np = dot_partials_count();
+  double *v = nullptr, *w = nullptr, *dinv = nullptr, *scr = nullptr;
   mfgb_status st;
   if ((st = dalloc((void **)&v, sizeof(double) * n)) || (st = dalloc((void **)&w, sizeof(double) * n)) ||
-      (st = dalloc((void **)&dinv, sizeof(double) * n))) {
-    cudaFree(v); cudaFree(w); cudaFree(dinv);
+      (st = dalloc((void **)&dinv, sizeof(double) * n)) ||
+      (st = dalloc((void **)&scr, sizeof(double) * (np + 2)))) {
+    cudaFree(v); cudaFree(w); cudaFree(dinv); cudaFree(scr);
     return st;
   }
-  struct Free { double *a, *b, *c; ~Free() { cudaFree(a); cudaFree(b); cudaFree(c); } } fr{v, w, dinv};
+  struct Free {
+    double *a, *b, *c, *d;
+    ~Free() { cudaFree(a); cudaFree(b); cudaFree(c); cudaFree(d); }
+  } fr{v, w, dinv, scr};
+  double *d_nv = scr + np, *d_vw = scr + np + 1;
   if ((st = cuda_status(cudaMemcpy(v, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "lmax init")))
     return st;
   if (L.op->n_constrained)
@@ -378,10 +394,8 @@ mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
   }
   double lam = 0;
   for (int it = 0; it < iters; ++it) {
-    double nv = 0;
-    if ((st = mfgb_dot(n, v, v, &nv, nullptr))) return st;
-    const double inv = nv > 0 ? 1.0 / std::sqrt(nv) : 0.0;
-    k_axpy<double><<<grid1d(n), T256>>>(n, inv - 1.0, v, v);  // v *= inv
+    if ((st = cuda_status(dot_to_device(n, v, v, scr, d_nv, nullptr), "lmax |v|"))) return st;
+    k_normalize<<<grid1d(n), T256>>>(n, d_nv, v);  // v *= 1 / |v|
     if (prec == 32) {  // the smoother's own FP32 operator, on a float copy
       k_convert<float, double><<<grid1d(n), T256>>>(n, v, (float *)L.t);
       if ((st = level_vmult(L.op, 32, L.d, L.t, nullptr))) return st;
@@ -393,12 +407,14 @@ mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
       k_set_constrained<double><<<grid1d(L.op->n_constrained), T256>>>(L.op->n_constrained,
                                                                         L.op->d_constrained, w, 0.0);
     k_scale_by<double><<<grid1d(n), T256>>>(n, dinv, w);
-    double vw = 0;
-    if ((st = mfgb_dot(n, v, w, &vw, nullptr))) return st;  // Rayleigh quotient (|v| = 1)
-    lam = vw;
+    // Rayleigh quotient (|v| = 1)
+    if ((st = cuda_status(dot_to_device(n, v, w, scr, d_vw, nullptr), "lmax v.w"))) return st;
     std::swap(v, w);
   }
   fr.a = v; fr.b = w;
+  if (iters > 0 &&
+      (st = cuda_status(cudaMemcpy(&lam, d_vw, sizeof(double), cudaMemcpyDeviceToHost), "lmax")))
+    return st;
   *lmax = lam;
   return cuda_status(cudaGetLastError(), "lmax");
 }
@@ -535,17 +551,27 @@ static mfgb_status mg_setup_impl(const mfgb_box_desc *fine, const mfgb_mg_params
       st = MFGB_ERR_UNSUPPORTED;
     } else if (nc > 0) {
       std::vector<double> Ad((size_t)nc * nc), dinv(nc);
+      // columns A e_j in blocks of up to 32 MB of unit vectors: the applies are
+      // queued without host synchronisation, one copy back per block
+      const int64_t cb = std::max<int64_t>(1, std::min<int64_t>(nc, (4 << 20) / C.n));
       double *e = nullptr, *y = nullptr;
-      st = dalloc((void **)&e, sizeof(double) * C.n);
-      if (!st) st = dalloc((void **)&y, sizeof(double) * C.n);
-      std::vector<double> hy(C.n);
-      for (int j = 0; j < nc && !st; ++j) {
-        cudaMemset(e, 0, sizeof(double) * C.n);
-        const double one = 1.0;
-        cudaMemcpy(e + ids[j], &one, sizeof(double), cudaMemcpyHostToDevice);
-        st = vmult_impl(C.op, y, e, MFGB_ARITH_FP64, nullptr, nullptr, nullptr);
-        if (!st) st = cuda_status(cudaMemcpy(hy.data(), y, sizeof(double) * C.n, cudaMemcpyDeviceToHost), "coarse column");
-        for (int i = 0; i < nc && !st; ++i) Ad[(size_t)i * nc + j] = hy[ids[i]];
+      st = dalloc((void **)&e, sizeof(double) * C.n * cb);
+      if (!st) st = dalloc((void **)&y, sizeof(double) * C.n * cb);
+      std::vector<double> hy((size_t)C.n * cb), he((size_t)C.n * cb);
+      for (int j0 = 0; j0 < nc && !st; j0 += (int)cb) {
+        const int nb = (int)std::min<int64_t>(cb, nc - j0);
+        std::fill(he.begin(), he.begin() + (size_t)nb * C.n, 0.0);
+        for (int jj = 0; jj < nb; ++jj) he[(size_t)jj * C.n + ids[j0 + jj]] = 1.0;
+        st = cuda_status(cudaMemcpy(e, he.data(), sizeof(double) * C.n * nb, cudaMemcpyHostToDevice),
+                         "coarse unit vectors");
+        for (int jj = 0; jj < nb && !st; ++jj)
+          st = vmult_impl(C.op, y + (size_t)jj * C.n, e + (size_t)jj * C.n, MFGB_ARITH_FP64, nullptr,
+                          nullptr, nullptr);
+        if (!st)
+          st = cuda_status(cudaMemcpy(hy.data(), y, sizeof(double) * C.n * nb, cudaMemcpyDeviceToHost),
+                           "coarse columns");
+        for (int jj = 0; jj < nb && !st; ++jj)
+          for (int i = 0; i < nc; ++i) Ad[(size_t)i * nc + j0 + jj] = hy[(size_t)jj * C.n + ids[i]];
       }
       cudaFree(e);
       cudaFree(y);
