@@ -1,7 +1,7 @@
 """The N > 1 host path of bench.py on CPU: two gloo ranks, max-over-ranks
 timing and the replica throughput rule (value = all ranks' DoFs / slowest
-rank's time).  This build runs replicas only (one GPU per box), so there is no
-data-path collective to test."""
+rank's time).  Multi-GPU runs are independent replicas (one operator per GPU),
+so there is no data-path collective to test."""
 import os
 import socket
 
