@@ -417,38 +417,76 @@ struct GaussDiagParams {
   double B[100], DB[100];  // B[q*n + a], DB = DG B  (q < nq, a < n)
 };
 
+// The diagonal entry of DoF (a, b, c) is a sum over the Gauss points (i, j, k)
+// of seven terms (the six G components and the mass term), each a product of
+// 1D weights: with r = DB_i B_j B_k, s = B_i DB_j B_k, t = B_i B_j DB_k (basis
+// a, b, c; DB = DG B the derivative at the Gauss points)
+//   G_rr r^2 + G_ss s^2 + G_tt t^2 + 2 (G_rs r s + G_rt r t + G_st s t) + JxW (B_i B_j B_k)^2.
+// The kernel contracts the seven quadrature arrays one direction at a time
+// (k -> c, j -> b, i -> a) with the squared / mixed 1D weights (bb = B^2,
+// dd = DB^2, bd = B DB): O(nq^3 n) per cell instead of O(nq^3 n^3).  One CTA
+// per cell; shared memory holds the weights, stage 1 [T][nq][nq][n] and
+// stage 2 [T][nq][n][n].
+__constant__ int kDiagKind[3][7] = {
+    // rr  rs  rt  ss  st  tt  W     weight kind per direction: 0 bb, 1 dd, 2 bd
+    {1, 2, 2, 0, 0, 0, 0},  // i
+    {0, 2, 0, 1, 2, 0, 0},  // j
+    {0, 0, 2, 0, 2, 1, 0},  // k
+};
+__constant__ double kDiagFactor[7] = {1.0, 2.0, 2.0, 1.0, 2.0, 1.0, 1.0};
+
 __global__ void __launch_bounds__(256)
     diagonal_gauss_kernel(int N, int NQ, int64_t n_cells, const uint32_t *__restrict__ map,
                           const double *__restrict__ G, const double *__restrict__ JxW,
                           GaussDiagParams gp, double *__restrict__ diag) {
-  const int N2 = N * N, N3 = N2 * N, NQ3 = NQ * NQ * NQ;
+  extern __shared__ double sm[];
+  const int NT = JxW ? 7 : 6;
+  const int N2 = N * N, N3 = N2 * N, Q2 = NQ * NQ, Q3 = Q2 * NQ, QN = NQ * N;
+  double *w = sm;                        // [3][nq][n]: bb, dd, bd
+  double *S1 = w + 3 * QN;               // [T][nq][nq][n]  (i, j, c)
+  double *S2 = S1 + NT * Q2 * N;         // [T][nq][n][n]   (i, b, c)
+  for (int t = threadIdx.x; t < QN; t += blockDim.x) {
+    const double b = gp.B[t], d = gp.DB[t];
+    w[t] = b * b;
+    w[QN + t] = d * d;
+    w[2 * QN + t] = b * d;
+  }
+  __syncthreads();
   for (int64_t e = blockIdx.x; e < n_cells; e += gridDim.x) {
-    // every thread of the cell reads the same G and JxW entries (broadcast loads)
-    const double *Gc = G + e * 6 * NQ3;
-    const double *Wc = JxW ? JxW + e * NQ3 : nullptr;
-    for (int l = threadIdx.x; l < N3; l += blockDim.x) {
+    for (int l = threadIdx.x; l < NT * Q2 * N; l += blockDim.x) {  // k -> c
+      const int T = l / (Q2 * N), r = l - T * Q2 * N, ij = r / N, c = r - ij * N;
+      const double *src = (T < 6 ? G + (e * 6 + T) * Q3 : JxW + e * Q3) + ij * NQ;
+      const double *wk = w + kDiagKind[2][T] * QN + c;
+      double acc = 0.0;
+      for (int k = 0; k < NQ; ++k) acc += wk[k * N] * __ldg(src + k);
+      S1[l] = acc;
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < NT * NQ * N2; l += blockDim.x) {  // j -> b
+      const int T = l / (NQ * N2), r = l - T * NQ * N2, i = r / N2, bc = r - i * N2;
+      const int b = bc / N, c = bc - b * N;
+      const double *wj = w + kDiagKind[1][T] * QN + b;
+      const double *s1 = S1 + T * Q2 * N + i * NQ * N + c;
+      double acc = 0.0;
+      for (int j = 0; j < NQ; ++j) acc += wj[j * N] * s1[j * N];
+      S2[l] = acc;
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < N3; l += blockDim.x) {  // i -> a, scatter
       const uint32_t dof = map[e * N3 + l];
       if (dof == MFGB_INVALID_DOF) continue;
-      const int a = l / N2, b = (l / N) % N, c = l % N;
+      const int a = l / N2, bc = l - a * N2;
       double acc = 0.0;
-      for (int i = 0; i < NQ; ++i) {
-        const double bi = gp.B[i * N + a], di = gp.DB[i * N + a];
-        for (int j = 0; j < NQ; ++j) {
-          const double bj = gp.B[j * N + b], dj = gp.DB[j * N + b];
-          for (int k = 0; k < NQ; ++k) {
-            const double bk = gp.B[k * N + c], dk = gp.DB[k * N + c];
-            const int q = (i * NQ + j) * NQ + k;
-            const double r = di * bj * bk, s = bi * dj * bk, t = bi * bj * dk, ph = bi * bj * bk;
-            acc += __ldg(Gc + q) * r * r + __ldg(Gc + 3 * NQ3 + q) * s * s +
-                   __ldg(Gc + 5 * NQ3 + q) * t * t +
-                   2.0 * (__ldg(Gc + NQ3 + q) * r * s + __ldg(Gc + 2 * NQ3 + q) * r * t +
-                          __ldg(Gc + 4 * NQ3 + q) * s * t) +
-                   (Wc ? __ldg(Wc + q) * ph * ph : 0.0);
-          }
-        }
+      for (int T = 0; T < NT; ++T) {
+        const double *wi = w + kDiagKind[0][T] * QN + a;
+        const double *s2 = S2 + T * NQ * N2 + bc;
+        double t = 0.0;
+        for (int i = 0; i < NQ; ++i) t += wi[i * N] * s2[i * N2];
+        acc += kDiagFactor[T] * t;
       }
       atomicAdd(diag + dof, acc);
     }
+    __syncthreads();  // S1 / S2 are rewritten for the next cell
   }
 }
 
@@ -465,9 +503,15 @@ cudaError_t diagonal_gauss(int N, int NQ, int64_t n_cells, const uint32_t *map, 
       gp.DB[q * N + a] = d;
     }
   if (n_cells == 0) return cudaSuccess;
-  const int threads = std::min(256, ((N * N * N + 31) / 32) * 32);
-  const unsigned grid = (unsigned)std::min<int64_t>(n_cells, 152 * 16);
-  diagonal_gauss_kernel<<<grid, threads, 0, s>>>(N, NQ, n_cells, map, G, JxW, gp, diag);
+  const int NT = JxW ? 7 : 6;
+  const size_t smem = sizeof(double) * (3 * NQ * N + NT * NQ * NQ * N + NT * NQ * N * N);
+  if (smem > 48 * 1024) {  // at most 98 KB (nq = 10, n = 9, mass term)
+    const cudaError_t e = cudaFuncSetAttribute(diagonal_gauss_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const unsigned grid = (unsigned)std::min<int64_t>(n_cells, 152 * 8);
+  diagonal_gauss_kernel<<<grid, 256, smem, s>>>(N, NQ, n_cells, map, G, JxW, gp, diag);
   return cudaGetLastError();
 }
 
