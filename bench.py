@@ -190,8 +190,10 @@ def run_reference(args, rank, world):
     w = WORKLOAD
     prob = oracle.BoxProblem(w["nx"], w["ny"], w["nz"], w["degree"], amplitude=w["amplitude"])
     src = prob.rhs(w["seed"])
+    # bounded sample: at most 10 timed and 5 warm-up applies (about 0.2 s each on
+    # 16 Grace cores at this size); the line reports the counts it ran
     steps = max(1, min(args.steps, 10))
-    warm = max(1, min(args.warmup, 2))
+    warm = max(1, min(args.warmup, 5))
     rate, dt = cpu_reference_apply_rate(prob, steps, warm, src)
     cores = oracle.num_threads()
     line = {
