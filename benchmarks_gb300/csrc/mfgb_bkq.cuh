@@ -13,11 +13,13 @@
 // in/out[e][NM^3].  With a dof map (L-vector mode, the BP3 operator) the input
 // is gathered through map[e][NM^3] and the output scatter-added atomically.
 //
-// GB300 structure: a CTA holds E elements, NQ^2 threads per element.  The
-// interpolation passes run one 1D line per thread through shared memory; the
-// Laplacian's gradient/metric/integrate phase uses the BK5 column layout (thread
-// (q, r) keeps the direction-0 column of its points in registers).  Arithmetic
-// is FP64 or double-float (policy A).
+// GB300 structure (bkq_kernel): a CTA holds E elements, NQ^2 threads per
+// element.  The interpolation passes run one 1D line per thread through shared
+// memory; the Laplacian's gradient/metric/integrate phase uses the BK5 column
+// layout (thread (q, r) keeps the direction-0 column of its points in
+// registers).  Arithmetic is FP64 or double-float (policy A).  The BP3 L-vector
+// operator has its own kernel with the bulk-TMA pipeline (bp3_tma_kernel, below);
+// bkq_kernel serves the E-vector seams and unaligned BP3 slabs.
 #pragma once
 #include "mfgb_bk5.cuh"
 
