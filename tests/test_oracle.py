@@ -272,3 +272,41 @@ def test_helmholtz_mass_term_and_diagonal(orc):
     u[H.constrained] = w[H.constrained] = 0
     assert u @ H.apply(w) == pytest.approx(w @ H.apply(u), rel=1e-12)
     assert u @ H.apply(u) > 0
+
+
+@pytest.mark.parametrize("nq_extra, mass", [(0, False), (1, False), (0, True)])
+def test_gauss_diagonal_sum_factorisation(orc, nq_extra, mass):
+    """The factorised form of the Gauss-point diagonal that the GPU kernel
+    evaluates (seven quadrature sums, each contracted one direction at a time
+    with B^2, (DB)^2 or B DB; factor 2 on the three cross terms) equals the
+    oracle's direct sum over the quadrature points."""
+    p = 3
+    cls = orc.HelmholtzProblem if mass else orc.GaussProblem
+    if mass:  # Helmholtz: q = p + 1
+        P = cls(2, 3, 2, p, amplitude=0.08)
+    else:
+        P = cls(2, 3, 2, p, nq=p + 1 + nq_extra, amplitude=0.08)
+    n, q = P.n, P.nq
+    B, DG = P.B, P.DG
+    DB = DG @ B
+    w = {0: B * B, 1: DB * DB, 2: B * DB}  # [q][n]
+    kinds = [(1, 0, 0, 1.0), (2, 2, 0, 2.0), (2, 0, 2, 2.0), (0, 1, 0, 1.0), (0, 2, 2, 2.0),
+             (0, 0, 1, 1.0)]  # rr rs rt ss st tt: (i, j, k) weight kinds, factor
+    G = P.Gg.reshape(P.n_cells, 6, q, q, q)
+    diag = np.zeros(P.n_dofs)
+    for e in range(P.n_cells):
+        de = np.zeros((n, n, n))
+        for T, (ki, kj, kk, f) in enumerate(kinds):
+            de += f * np.einsum("ia,jb,kc,ijk->abc", w[ki], w[kj], w[kk], G[e, T])
+        if mass:
+            W = P.JxW.reshape(P.n_cells, q, q, q)[e]
+            de += np.einsum("ia,jb,kc,ijk->abc", w[0], w[0], w[0], W)
+        idx = P.map.reshape(P.n_cells, n ** 3)[e].astype(np.int64)
+        ok = idx != 0xFFFFFFFF  # Dirichlet DoFs are masked out of the map
+        np.add.at(diag, idx[ok], de.reshape(-1)[ok])
+    diag[P.constrained] = 1.0
+    direct = np.zeros(P.n_dofs)
+    orc._gauss_sigs().orc_gauss_diagonal(n, q, orc._p(B), orc._p(DG), P.n_cells, orc._p(P.map),
+                                         orc._p(P.Gg), orc._p(P.JxW) if mass else None, P.n_dofs,
+                                         P.constrained.size, orc._p(P.constrained), orc._p(direct))
+    assert np.max(np.abs(diag - direct)) <= 1e-13 * np.max(np.abs(direct))
