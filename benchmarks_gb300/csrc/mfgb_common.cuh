@@ -108,9 +108,10 @@ __device__ __forceinline__ void dfacc_merge(dfacc &a, const dfacc &b) {
 
 // The accumulator as a value: the pair (s, c) itself, not renormalised (|c| may
 // exceed half an ulp of s).  Its consumers accept that: a product uses hi*hi
-// exactly and the two cross terms in float (dropping lo*lo), which keeps the
-// error at the 2^-48 level of the terms, and the conversion to double adds
-// hi and lo with one rounding.
+// exactly and the two cross terms in float (dropping lo*lo), and the conversion
+// to double adds hi and lo with one rounding.  The error stays that of the
+// renormalising form: about 2^-45 of the sum of the absolute terms for the 3-
+// to 15-term sums of the operator kernels (float32 restatement, measured).
 __device__ __forceinline__ df dfacc_finish(const dfacc &a) {
   df r;
   r.hi = a.s;
