@@ -210,8 +210,14 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-# operator kernel thread layouts (mfgb_set_kernel_shape)
-SHAPE_CODES = {"column": 0, "point": 1, "tma": 2, "column_alt": 3, "tma_alt": 4}
+# operator kernel thread layouts (mfgb_set_kernel_shape; 5, 6 double-float only)
+SHAPE_CODES = {"column": 0, "point": 1, "tma": 2, "column_alt": 3, "tma_alt": 4, "fx": 5,
+               "fx_alt": 6}
+# what the arithmetic of the operator kernel is, and its accuracy against FP64
+ARITH_LABEL = {
+    "df": "FP64-accurate double-float on the FP32 pipes (offset accumulation, per-cell "
+          "exponent scaling; ~2^-43 normwise relative, 1e-12 bar)",
+    "fp64": "native FP64 (DFMA)"}
 
 
 def is_headline():
@@ -253,34 +259,27 @@ def run_ours(args, rank, world):
     sp = ctypes.c_void_p(stream.cuda_stream)
     op, d_dst, d_src = A.handle, ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr())
 
-    def step(ev0=None, ev1=None):
-        # vmult = dst = 0 ; cell loop (one kernel) ; constrained identity rows
-        dst.zero_()
-        if ev0 is not None:
-            ev0.record(stream)
-        _abi.check(L.mfgb_vmult_add(op, d_dst, d_src, arith, sp))
-        if ev1 is not None:
-            ev1.record(stream)
-        _abi.check(L.mfgb_copy_constrained(op, d_dst, d_src, sp))
+    def step():
+        # the library's vmult: dst = 0 ; cell loop (one kernel) ; constrained identity rows
+        _abi.check(L.mfgb_vmult(op, d_dst, d_src, arith, sp))
 
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
     barrier(world)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local).start() if rank == 0 else None
     torch.cuda.synchronize()
     start.record(stream)
     for k in range(args.steps):
-        step(*ev[k])
+        step()
     stop.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop() if clocks else None
     total_ms = start.elapsed_time(stop)
-    kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
     total_ms = max_over_ranks(total_ms, world)
+    _abi.check(L.mfgb_check_device_errors(sp))  # a timed-out copy wait voids the numbers
+    kernel_ms = operator_kernel_ms(L, op, d_dst, d_src, arith, sp, stream, args.steps)
     barrier(world)
 
     # end to end through the public vmult with pinned host buffers
@@ -308,6 +307,72 @@ def run_ours(args, rank, world):
     err = float(torch.linalg.norm(h_dst.cuda() - dst) / torch.linalg.norm(dst))
     assert err <= 1e-14, err
     return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk)
+
+
+def operator_kernel_ms(L, op, d_dst, d_src, arith, sp, stream, steps):
+    """Mean duration of the operator kernel alone (mfgb_vmult_add: the one cell-loop
+    launch of vmult, dst += A src), CUDA events on the launching stream around
+    every launch, over as many launches as the timed region had steps."""
+    import torch
+
+    from benchmarks_gb300 import _abi
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for _ in range(2):
+        _abi.check(L.mfgb_vmult_add(op, d_dst, d_src, arith, sp))
+    torch.cuda.synchronize()
+    for a, b in ev:
+        a.record(stream)
+        _abi.check(L.mfgb_vmult_add(op, d_dst, d_src, arith, sp))
+        b.record(stream)
+    torch.cuda.synchronize()
+    _abi.check(L.mfgb_check_device_errors(sp))
+    return statistics.mean(a.elapsed_time(b) for a, b in ev)
+
+
+def degree_sweep(args, degrees=(3, 4, 5, 6, 7, 8), target_dofs=4.0e7):
+    """The same measurement at p = 3..8 on n^3-cell deformed cubes of about 4e7 DoFs
+    (n = round((N^(1/3) - 1) / p), amplitude 0.05, seeded U[-1,1] src): GDoF/s of
+    the library's vmult (CUDA events over 20 steps after 3 warm-up steps), the
+    operator kernel's mean time and its algorithmic-byte HBM fraction."""
+    import ctypes
+
+    import torch
+
+    import benchmarks_gb300 as mf
+    from benchmarks_gb300 import _abi
+    L = mf.lib()
+    arith = mf._arith(args.arith)
+    peak = measured_peaks()[0]
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    out = {}
+    for p in degrees:
+        nc = max(2, round((target_dofs ** (1.0 / 3.0) - 1) / p))
+        A = mf.LaplaceOperator(mf.BoxMesh(nc, nc, nc, degree=p, amplitude=WORKLOAD["amplitude"]),
+                               arith=args.arith)
+        src = A.rhs_uniform(WORKLOAD["seed"])
+        dst = A.initialize_dof_vector()
+        op, d_dst, d_src = A.handle, ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr())
+        for _ in range(3):
+            _abi.check(L.mfgb_vmult(op, d_dst, d_src, arith, sp))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(20):
+            _abi.check(L.mfgb_vmult(op, d_dst, d_src, arith, sp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 20
+        kms = operator_kernel_ms(L, op, d_dst, d_src, arith, sp, stream, 20)
+        n = A.m()
+        byts = algorithmic_bytes(n, A.n_cells, p)
+        out[str(p)] = {"cells": [nc, nc, nc], "n_dofs": n, "GDoF/s": n / ms / 1e6,
+                       "ms_per_vmult": ms, "kernel_ms": kms,
+                       "hbm_frac": byts / (kms * 1e-3) / 1e9 / peak,
+                       "kernel": kernel_name(p, arith)}
+        del A, src, dst
+    return out
 
 
 def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk):
@@ -339,6 +404,7 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / 6.83 if is_headline() else None,
         "dtype": "f64",
+        "arith": ARITH_LABEL[args.arith],
         "data": "synthetic (seeded U[-1,1] src, deformed unit-cube mesh)",
         "config": config_dict(args, n, n_cells),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -355,6 +421,8 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if not args.no_degrees and world == 1 and is_headline():
+        line["degrees"] = degree_sweep(args)
     if not args.no_solve and world == 1 and is_headline():
         line["bp5"] = bp5_solves(A)
         line["bk6"] = bk6_rate(A, args)
@@ -691,7 +759,9 @@ def kernel_name(degree, arith):
     n = degree + 1
     pol = "ArithDF" if arith == 1 else "ArithF64"
     return {0: f"bk5_kernel<{n},{pol}>", 1: f"bk5_pt_kernel<{n},{pol}>",
-            2: f"bk5_tma_kernel<{n},{pol}>"}.get(shape.value, "bk5")
+            2: f"bk5_tma_kernel<{n},{pol}>", 3: f"bk5_kernel_mb<{n},{pol}>",
+            4: f"bk5_tma_kernel<{n},alt,{pol}>", 5: f"bk5fx_tma_kernel<{n}>",
+            6: f"bk5fx_tma_kernel<{n},alt>"}.get(shape.value, "bk5")
 
 
 def main():
@@ -703,6 +773,7 @@ def main():
     ap.add_argument("--arith", choices=["df", "fp64"], default="df")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
+    ap.add_argument("--no-degrees", action="store_true", help="skip the p = 3..8 sweep")
     ap.add_argument("--no-solve", action="store_true",
                     help="skip the BP5 solve comparison and the like-for-like Gauss figure")
     ap.add_argument("--cells", type=int, nargs=3, default=None,

@@ -441,3 +441,10 @@ def dot(a, b) -> float:
 
 
 from .batch import BatchSolver, batch_workload  # noqa: E402
+
+
+def check_device_errors():
+    """Reads and clears the device error word on the current stream
+    (mfgb_check_device_errors): raises MfgbError with status TIMEOUT if a kernel
+    gave up on a bulk-copy wait since the last check."""
+    _abi.check(lib().mfgb_check_device_errors(_stream_ptr()))

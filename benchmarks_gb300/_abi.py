@@ -9,6 +9,7 @@ _LIB = None
 
 OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_NOT_CONVERGED = 0, 1, 2, 3
 ERR_TIMEOUT, ERR_NONFINITE, ERR_CUDA, ERR_UNSUPPORTED = 4, 5, 6, 7
+ERR_RANGE = 8
 ARITH_FP64, ARITH_FP64_DF, ARITH_FP32 = 0, 1, 2
 INVALID_DOF = 0xFFFFFFFF
 
@@ -91,6 +92,7 @@ def lib():
         "mfgb_cg_solve_noalloc": ([P, P, P, P, ctypes.POINTER(CgControl),
                                    ctypes.POINTER(SolveInfo), P], I32),
         "mfgb_dot": ([I64, P, P, ctypes.POINTER(D), P], I32),
+        "mfgb_pipe_rate": ([I32, I32, I32, ctypes.POINTER(D)], I32),
         "mfgb_mg_set_smoother_weights": ([P, P], I32),
         "mfgb_mlp_n_params": ([], I32),
         "mfgb_cell_features": ([P, P, P], I32),

@@ -4,7 +4,8 @@ launch shape is a compile-time choice: CEED_BK/src/BK5/templated_cuda_benchmark.
 For each (arithmetic, degree) it times every thread layout the library has
 (0 column, 1 point-per-thread, 2 column with bulk-TMA prefetch, 3 and 4 the
 column and bulk-TMA kernels at an alternative number of cells per thread block,
-i.e. the elements-per-block choice) on a
+i.e. the elements-per-block choice; for double-float also 5 and 6, the
+offset-accumulation kernel at the shape-2 and shape-4 cells per block) on a
 representative deformed box mesh with CUDA events, and installs the fastest in
 the library's shape table (``mfgb_set_kernel_shape``).  Results can be saved
 to and loaded from a small JSON file.
@@ -19,6 +20,11 @@ from ._abi import lib
 
 ARITHS = {"fp64": 0, "df": 1, "fp32": 2}
 SHAPES = (0, 1, 2, 3, 4)
+DF_SHAPES = SHAPES + (5, 6)  # double-float: the offset-accumulation kernel as well
+
+
+def shapes_for(arith: int):
+    return DF_SHAPES if arith == ARITHS["df"] else SHAPES
 
 
 def _mesh_for(degree, target_dofs):
@@ -73,11 +79,13 @@ def tune(degrees=range(1, 9), ariths=("df", "fp32"), target_dofs=2.0e7, reps=10,
         A = mf.LaplaceOperator(_mesh_for(d, target_dofs))
         for name in ariths:
             a = ARITHS[name]
-            ms = [time_shape(A, a, s, reps) for s in SHAPES]
-            best = min(range(len(SHAPES)), key=lambda i: ms[i])
-            result.setdefault(name, {})[d] = {"best": SHAPES[best], "ms": ms, "n_dofs": A.m()}
+            shapes = shapes_for(a)
+            ms = [time_shape(A, a, s, reps) for s in shapes]
+            best = min(range(len(shapes)), key=lambda i: ms[i])
+            result.setdefault(name, {})[d] = {"best": shapes[best], "ms": ms, "n_dofs": A.m(),
+                                              "shapes": list(shapes)}
             if apply:
-                _abi.check(lib().mfgb_set_kernel_shape(a, d, SHAPES[best]))
+                _abi.check(lib().mfgb_set_kernel_shape(a, d, shapes[best]))
         del A
     return result
 
@@ -109,7 +117,7 @@ def main(argv=None):
     ap.add_argument("--ariths", nargs="+", choices=sorted(ARITHS), default=["df", "fp32"])
     ap.add_argument("--dofs", type=float, default=2.0e7, help="DoFs of the timing mesh")
     ap.add_argument("--reps", type=int, default=10)
-    ap.add_argument("--shape", type=int, choices=SHAPES, default=None,
+    ap.add_argument("--shape", type=int, choices=DF_SHAPES, default=None,
                     help="time only this shape (no tuning)")
     ap.add_argument("--out", default=None, help="write the measured table as JSON")
     a = ap.parse_args(argv)

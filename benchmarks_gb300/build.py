@@ -24,10 +24,12 @@ SOURCES = [
     "mfgb_bkq.cu",
     "mfgb_bk5_f64.cu",
     "mfgb_bk5_df.cu",
+    "mfgb_bk5_fx.cu",
     "mfgb_bk5_f32.cu",
     "mfgb_bk5g.cu",
     "mfgb_bk6.cu",
     "mfgb_mlp.cu",
+    "mfgb_rates.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

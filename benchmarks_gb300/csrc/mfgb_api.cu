@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <string>
 #include <vector>
@@ -43,7 +44,14 @@ mfgb_status ensure_df(mfgb_operator *op) {
   if (op->d_Gdf) return MFGB_OK;
   const int64_t nq = op->nq > 0 ? op->nq : op->n;  // G points per direction
   const int64_t ng = op->n_cells * 6 * nq * nq * nq;
-  mfgb_status st = dev_alloc((void **)&op->d_Gdf, sizeof(float2) * ng, "G (double-float)");
+  // the pairs carry FP64 accuracy only inside the range window (checked per cell)
+  mfgb_status st = range_check_sync(0, nullptr, op->n_cells, (int)(6 * nq * nq * nq), op->d_G,
+                                    nullptr, "double-float operator");
+  if (!st && op->d_JxW)
+    st = range_check_sync(0, nullptr, op->n_cells, op->n * op->n * op->n, op->d_JxW, nullptr,
+                          "double-float operator (mass term)");
+  if (st) return st;
+  st = dev_alloc((void **)&op->d_Gdf, sizeof(float2) * ng, "G (double-float)");
   if (st) return st;
   st = cuda_status(g_to_df(ng, op->d_G, op->d_Gdf, nullptr), "G -> double-float");
   if (st) return st;
@@ -54,6 +62,32 @@ mfgb_status ensure_df(mfgb_operator *op) {
       return st;
   }
   return cuda_status(cudaDeviceSynchronize(), "G -> double-float");
+}
+
+mfgb_status ensure_fx(mfgb_operator *op) {
+  if (op->d_Gfx) return MFGB_OK;
+  const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  mfgb_status st;
+  if ((st = dev_alloc((void **)&op->d_Gfx, sizeof(float2) * op->n_cells * 6 * n3,
+                      "G (scaled double-float)")) ||
+      (st = dev_alloc((void **)&op->d_Gexp, sizeof(int) * std::max<int64_t>(1, op->n_cells),
+                      "G exponent offsets")))
+    return st;
+  if ((st = cuda_status(g_to_fx(op->n_cells, (int)(6 * n3), op->d_G, op->d_Gfx, op->d_Gexp, nullptr),
+                        "G -> scaled double-float")))
+    return st;
+  return cuda_status(cudaDeviceSynchronize(), "G -> scaled double-float");
+}
+
+mfgb_status ensure_arith(mfgb_operator *op, int arith) {
+  if (arith != MFGB_ARITH_FP64_DF || op->n_cells == 0) return MFGB_OK;
+  // operators assembled from pairs only (the batched union operators) keep them
+  if (!op->d_G) {
+    if (op->d_Gdf || op->d_Gfx) return MFGB_OK;
+    set_error("operator has no geometric factors");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  return op->quadrature == 0 && kernel_shape(1, op->n) >= kShapeFx ? ensure_fx(op) : ensure_df(op);
 }
 
 // dst += A src over cells [cell0, cell0 + n) (the map keeps global DoF indices);
@@ -76,11 +110,15 @@ static cudaError_t apply_range(mfgb_operator *op, int64_t cell0, int64_t n, doub
                           partials, grid, s, done, op->d_JxW ? op->d_JxW + cell0 * n3 : nullptr)
                : bk5_f64(op->n, n, map, op->d_G + cell0 * 6 * n3, src, dst, op->D, partials, grid,
                          s, done);
-  return op->quadrature
-             ? bk5g_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->DG, op->Bq,
-                       partials, grid, s, done, op->d_JxWdf ? op->d_JxWdf + cell0 * n3 : nullptr)
-             : bk5_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->D, partials, grid, s,
-                      done);
+  if (op->quadrature)
+    return bk5g_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->DG, op->Bq, partials,
+                   grid, s, done, op->d_JxWdf ? op->d_JxWdf + cell0 * n3 : nullptr);
+  // GLL collocation: the offset-accumulation kernel (no energy partials)
+  if (op->d_Gfx && !partials && (kernel_shape(1, op->n) >= kShapeFx || !op->d_Gdf))
+    return bk5_fx(op->n, n, map, op->d_Gfx + cell0 * 6 * n3, op->d_Gexp + cell0, src, dst, op->D, s,
+                  done);
+  return bk5_df(op->n, n, map, op->d_Gdf + cell0 * 6 * n3, src, dst, op->D, partials, grid, s,
+                done);
 }
 
 mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int arith,
@@ -91,7 +129,9 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
     set_error("vmult: unknown arith mode");
     return MFGB_ERR_INVALID_ARG;
   }
-  if (arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if ((st = ensure_arith(op, arith))) return st;
+  if (arith == MFGB_ARITH_FP64_DF && !uses_fx(op) && (st = range_check_async(op, op->n_dofs, src, s)))
+    return st;
   if (full && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
                                 "vmult: dst = 0")))
     return st;
@@ -110,17 +150,23 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
 // shape per degree measured on a GB300 at ~3e7 DoFs (autotune.py re-measures).
 static int g_shape[3][10] = {
     {0, 0, 4, 3, 2, 4, 2, 1, 2, 1},  // FP64
-    {2, 2, 4, 4, 4, 4, 1, 1, 2, 1},  // double-float
+    {2, 2, 5, 5, 5, 5, 5, 5, 5, 5},  // double-float
     {0, 0, 3, 3, 0, 3, 2, 4, 4, 2},  // FP32
 };
 
-// device-side error word (a TMA wait that ran out of time), one per device
+// device-side error word, one per device: bit 0 a TMA wait that ran out of
+// time, bit 1 a double-float source vector outside its range
 static __device__ int g_device_error;
 static int *g_device_error_ptr[64] = {nullptr};
+static std::mutex g_device_error_mutex;
 
+// device address of the error word on the current device, looked up once per
+// device and cached for the life of the process (a cudaDeviceReset or a
+// teardown of the primary context invalidates it)
 int *device_error_flag() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_device_error_mutex);
   if (!g_device_error_ptr[dev]) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) {
@@ -130,6 +176,141 @@ int *device_error_flag() {
     g_device_error_ptr[dev] = (int *)p;
   }
   return g_device_error_ptr[dev];
+}
+
+// ---- input range of the double-float kernels without per-cell scaling --------
+// A pair keeps 48 significant bits while both of its floats stay normal; with
+// the largest magnitude of a vector (per cell for geometric factors) in
+// [2^-40, 2^55], results, products and their error terms keep clear of float
+// under- and overflow through the operator's sums.
+constexpr int kRangeLo = 1023 - 40, kRangeHi = 1023 + 55;  // biased exponents
+
+__device__ __forceinline__ int finite_exp(double x) {
+  const int e = (int)(((unsigned)(__double_as_longlong(x) >> 32) >> 20) & 0x7FFu);
+  return e == 0x7FF ? 0 : e;
+}
+
+__device__ __forceinline__ int block_max(int v, int *s_red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? s_red[threadIdx.x] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  }
+  return v;  // valid in thread 0
+}
+
+// largest biased exponent of the finite entries of v -> atomicMax(*slot)
+__global__ void __launch_bounds__(256) vec_exp_max_kernel(int64_t n, const double *__restrict__ v,
+                                                          int *slot) {
+  __shared__ int s_red[8];
+  int em = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    em = max(em, finite_exp(v[t]));
+  em = block_max(em, s_red);
+  if (threadIdx.x == 0 && em) atomicMax(slot, em);
+}
+
+// *flag |= bit when the (nonzero) largest exponent lies outside the window
+__global__ void exp_window_kernel(const int *slot, int *flag, int bit) {
+  const int em = *slot;
+  if (em && (em < kRangeLo || em > kRangeHi)) atomicOr(flag, bit);
+}
+
+// one warp per cell: *flag |= bit when a cell's largest exponent (nonzero cells)
+// lies outside the window
+__global__ void cell_exp_window_kernel(int64_t n_cells, int per_cell, const double *__restrict__ G,
+                                       int *flag, int bit) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < n_cells; c += n_warps) {
+    int em = 0;
+    for (int t = lane; t < per_cell; t += 32) em = max(em, finite_exp(G[c * per_cell + t]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, o));
+    if (lane == 0 && em && (em < kRangeLo || em > kRangeHi)) atomicOr(flag, bit);
+  }
+}
+
+static unsigned range_grid(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8));
+}
+
+// stream-ordered check of a vector (slot: one device int of scratch): the
+// device error word gets kDevErrRange when its largest magnitude is outside
+// the window
+mfgb_status vec_range_check(int *slot, int64_t n, const double *v, cudaStream_t s) {
+  int *flag = device_error_flag();
+  if (!flag) {
+    set_error("range check: no device error word");
+    return MFGB_ERR_CUDA;
+  }
+  if (n <= 0) return MFGB_OK;
+  mfgb_status st;
+  if ((st = cuda_status(cudaMemsetAsync(slot, 0, sizeof(int), s), "range slot = 0"))) return st;
+  vec_exp_max_kernel<<<range_grid(n), 256, 0, s>>>(n, v, slot);
+  exp_window_kernel<<<1, 1, 0, s>>>(slot, flag, kDevErrRange);
+  return cuda_status(cudaGetLastError(), "range check");
+}
+
+// the same for per-cell geometric factors
+mfgb_status cells_range_check(int64_t n_cells, int per_cell, const double *G, cudaStream_t s) {
+  int *flag = device_error_flag();
+  if (!flag) {
+    set_error("range check: no device error word");
+    return MFGB_ERR_CUDA;
+  }
+  if (n_cells <= 0) return MFGB_OK;
+  cell_exp_window_kernel<<<range_grid(n_cells * 32), 256, 0, s>>>(n_cells, per_cell, G, flag,
+                                                                    kDevErrRange);
+  return cuda_status(cudaGetLastError(), "range check");
+}
+
+mfgb_status range_check_async(mfgb_operator *op, int64_t n, const double *v, cudaStream_t s) {
+  mfgb_status st;
+  if (!op->d_range && (st = dev_alloc((void **)&op->d_range, sizeof(int), "range slot")))
+    return st;
+  return vec_range_check(op->d_range, n, v, s);
+}
+
+// synchronous check of caller arrays (a vector and per-cell geometric
+// factors, either may be empty): MFGB_ERR_RANGE when one is outside the window
+mfgb_status range_check_sync(int64_t n, const double *v, int64_t n_cells, int per_cell,
+                             const double *G, cudaStream_t s, const char *what) {
+  int *d = nullptr;
+  mfgb_status st;
+  if ((st = cuda_status(cudaMallocAsync((void **)&d, 2 * sizeof(int), s), "range scratch")))
+    return st;
+  int h = 0;
+  cudaError_t e = cudaMemsetAsync(d, 0, 2 * sizeof(int), s);
+  if (e == cudaSuccess && n > 0) {
+    vec_exp_max_kernel<<<range_grid(n), 256, 0, s>>>(n, v, d);
+    exp_window_kernel<<<1, 1, 0, s>>>(d, d + 1, 1);
+  }
+  if (e == cudaSuccess && n_cells > 0)
+    cell_exp_window_kernel<<<range_grid(n_cells * 32), 256, 0, s>>>(n_cells, per_cell, G, d + 1,
+                                                                      2);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if ((st = cuda_status(e, "range check"))) return st;
+  if (h) {
+    set_error(std::string(what) + ": " + ((h & 2) ? "geometric factors of a cell" : "an input vector") +
+              " with largest magnitude outside [2^-40, 2^55], the range of the double-float "
+              "arithmetic without per-cell scaling (use MFGB_ARITH_FP64)");
+    return MFGB_ERR_RANGE;
+  }
+  return MFGB_OK;
+}
+
+bool uses_fx(const mfgb_operator *op) {
+  return op->quadrature == 0 && op->d_Gfx && (kernel_shape(1, op->n) >= kShapeFx || !op->d_Gdf);
 }
 
 int kernel_shape(int arith_class, int N) {
@@ -144,7 +325,9 @@ mfgb_status apply_add_impl(mfgb_operator *op, double *dst, const double *src, in
     set_error("apply: unknown arith mode");
     return MFGB_ERR_INVALID_ARG;
   }
-  if (arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if ((st = ensure_arith(op, arith))) return st;
+  if (arith == MFGB_ARITH_FP64_DF && !uses_fx(op) && (st = range_check_async(op, op->n_dofs, src, s)))
+    return st;
   if (done && op->quadrature == 2) done = nullptr;  // the BP3 kernel runs every time
   return cuda_status(apply_range(op, 0, op->n_cells, dst, src, arith, nullptr, nullptr, s, done),
                      "apply: operator kernel");
@@ -156,6 +339,9 @@ static void free_operator(mfgb_operator *op) {
   cudaFree(op->d_G);
   cudaFree(op->d_Gdf);
   cudaFree(op->d_G32);
+  cudaFree(op->d_Gfx);
+  cudaFree(op->d_Gexp);
+  cudaFree(op->d_range);
   cudaFree(op->d_constrained);
   cudaFree(op->d_partials);
   cudaFree(op->d_JxW);
@@ -194,6 +380,7 @@ const char *mfgb_status_string(mfgb_status s) {
     case MFGB_ERR_NONFINITE: return "non-finite value";
     case MFGB_ERR_CUDA: return "CUDA error";
     case MFGB_ERR_UNSUPPORTED: return "unsupported";
+    case MFGB_ERR_RANGE: return "input outside the double-float range";
     default: return "unknown status";
   }
 }
@@ -203,7 +390,8 @@ const char *mfgb_last_error(void) { return g_last_error.c_str(); }
 int mfgb_version(void) { return 1; }
 
 mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape) {
-  if (arith < 0 || arith > 2 || degree < 1 || degree > 8 || shape < 0 || shape > 4) {
+  if (arith < 0 || arith > 2 || degree < 1 || degree > 8 || shape < 0 ||
+      shape > (arith == MFGB_ARITH_FP64_DF ? 6 : 4)) {
     set_error("mfgb_set_kernel_shape: invalid argument");
     return MFGB_ERR_INVALID_ARG;
   }
@@ -225,9 +413,14 @@ mfgb_status mfgb_check_device_errors(void *stream) {
       (st = cuda_status(cudaMemsetAsync(flag, 0, sizeof(int), s), "clear device error word")) ||
       (st = cuda_status(cudaStreamSynchronize(s), "device error word")))
     return st;
-  if (h) {
+  if (h & kDevErrTimeout) {
     set_error("a kernel's bulk-copy wait exceeded its time limit; results are invalid");
     return MFGB_ERR_TIMEOUT;
+  }
+  if (h & kDevErrRange) {
+    set_error("a double-float operator application got a source vector whose largest magnitude "
+              "lies outside [2^-40, 2^55]; its result is invalid (use MFGB_ARITH_FP64)");
+    return MFGB_ERR_RANGE;
   }
   return MFGB_OK;
 }
@@ -495,8 +688,13 @@ mfgb_status mfgb_bk5_lvector(int degree, int64_t n_cells, const double *d_dbasis
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64)
     e = bk5_f64(degree + 1, n_cells, d_dof_indices, d_G, d_src, d_dst, D, nullptr, nullptr, s);
-  else if (arith == MFGB_ARITH_FP64_DF)
+  else if (arith == MFGB_ARITH_FP64_DF) {
+    // (the source vector's length is not an argument of this seam: G is checked)
+    const int n3 = (degree + 1) * (degree + 1) * (degree + 1);
+    mfgb_status st = range_check_sync(0, nullptr, n_cells, 6 * n3, d_G, s, "mfgb_bk5_lvector");
+    if (st) return st;
     e = bk5_df_g64(degree + 1, n_cells, d_dof_indices, d_G, d_src, d_dst, D, s);
+  }
   else {
     set_error("mfgb_bk5_lvector: unknown arith");
     return MFGB_ERR_INVALID_ARG;
@@ -518,8 +716,12 @@ mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, 
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64)
     e = bk5_f64(degree + 1, nelmt, nullptr, d_G, d_in, d_out, D, nullptr, nullptr, s);
-  else if (arith == MFGB_ARITH_FP64_DF)
+  else if (arith == MFGB_ARITH_FP64_DF) {
+    const int n3 = (degree + 1) * (degree + 1) * (degree + 1);
+    mfgb_status st = range_check_sync(nelmt * n3, d_in, nelmt, 6 * n3, d_G, s, "mfgb_bk5_evector");
+    if (st) return st;
     e = bk5_df_g64(degree + 1, nelmt, nullptr, d_G, d_in, d_out, D, s);
+  }
   else {
     set_error("mfgb_bk5_evector: unknown arith");
     return MFGB_ERR_INVALID_ARG;
@@ -554,7 +756,7 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
   mfgb_operator *op = const_cast<mfgb_operator *>(cop);
   if (op->n_dofs == 0) return MFGB_OK;
   mfgb_status st;
-  if (arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if ((st = ensure_arith(op, arith))) return st;
   if (!op->d_hsrc) {
     if ((st = dev_alloc((void **)&op->d_hsrc, sizeof(double) * op->n_dofs, "host apply src")) ||
         (st = dev_alloc((void **)&op->d_hdst, sizeof(double) * op->n_dofs, "host apply dst")))
@@ -652,6 +854,10 @@ mfgb_status mfgb_vmult_host(const mfgb_operator *cop, double *h_dst, const doubl
     last_out = 3 + 3 * k;
   }
   cudaStreamWaitEvent(s, ev[last_out], 0);
+  // double-float kernels without per-cell scaling: the uploaded source's range
+  if (arith == MFGB_ARITH_FP64_DF && !uses_fx(op) &&
+      (st = range_check_async(op, op->n_dofs, op->d_hsrc, s)))
+    return st;
   return cuda_status(cudaGetLastError(), "mfgb_vmult_host");
 }
 

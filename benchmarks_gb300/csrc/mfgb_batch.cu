@@ -659,7 +659,8 @@ mfgb_status gather_plan(const mfgb_batch *B, const std::vector<char> &active, Pl
       const int64_t n3 = (int64_t)op->n * op->n * op->n;
       if ((st = dalloc((void **)&op->d_map, sizeof(uint32_t) * op->n_cells * n3)) ||
           (st = dalloc((void **)&op->d_G32, sizeof(float) * op->n_cells * 6 * n3)) ||
-          (l == 0 && (st = dalloc((void **)&op->d_Gdf, sizeof(float2) * op->n_cells * 6 * n3))))
+          (l == 0 && (st = dalloc((void **)&op->d_Gfx, sizeof(float2) * op->n_cells * 6 * n3))) ||
+          (l == 0 && (st = dalloc((void **)&op->d_Gexp, sizeof(int) * op->n_cells))))
         return fail(st);
       int64_t c0 = 0;
       for (int k : gparts[g]) {
@@ -669,9 +670,12 @@ mfgb_status gather_plan(const mfgb_batch *B, const std::vector<char> &active, Pl
                         sizeof(uint32_t) * Q.n_cells * n3, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(op->d_G32 + c0 * 6 * n3, src->d_G32 + Q.cell_off * 6 * n3,
                         sizeof(float) * Q.n_cells * 6 * n3, cudaMemcpyDeviceToDevice, s);
-        if (l == 0)
-          cudaMemcpyAsync(op->d_Gdf + c0 * 6 * n3, src->d_Gdf + Q.cell_off * 6 * n3,
+        if (l == 0) {
+          cudaMemcpyAsync(op->d_Gfx + c0 * 6 * n3, src->d_Gfx + Q.cell_off * 6 * n3,
                           sizeof(float2) * Q.n_cells * 6 * n3, cudaMemcpyDeviceToDevice, s);
+          cudaMemcpyAsync(op->d_Gexp + c0, src->d_Gexp + Q.cell_off, sizeof(int) * Q.n_cells,
+                          cudaMemcpyDeviceToDevice, s);
+        }
         cudaMemcpyAsync(cons + cpos, F.d_cons + Q.cons_off, sizeof(int64_t) * Q.n_constrained,
                         cudaMemcpyDeviceToDevice, s);
         cpos += Q.n_constrained;
@@ -838,7 +842,8 @@ mfgb_status build_batch(mfgb_batch *B, const mfgb_box_desc *boxes, int n,
       if ((st = dalloc((void **)&op->d_map, sizeof(uint32_t) * op->n_cells * n3)) ||
           (st = dalloc((void **)&op->d_G32, sizeof(float) * op->n_cells * 6 * n3)))
         return st;
-      if (l == 0 && (st = dalloc((void **)&op->d_Gdf, sizeof(float2) * op->n_cells * 6 * n3)))
+      if (l == 0 && ((st = dalloc((void **)&op->d_Gfx, sizeof(float2) * op->n_cells * 6 * n3)) ||
+                     (st = dalloc((void **)&op->d_Gexp, sizeof(int) * op->n_cells))))
         return st;
     }
     if ((st = dalloc((void **)&D.d_cons, sizeof(int64_t) * D.n_cons))) return st;
@@ -949,11 +954,15 @@ mfgb_status build_batch(mfgb_batch *B, const mfgb_box_desc *boxes, int n,
                               "batch G32")))
           return st;
         if (l == 0) {
-          if ((st = ensure_df(L.op))) return st;
-          if ((st = cuda_status(cudaMemcpy(U->d_Gdf + P.cell_off * 6 * n3, L.op->d_Gdf,
+          // the outer FP64 operator: offset-accumulation kernel on per-cell scaled G
+          if ((st = ensure_fx(L.op))) return st;
+          if ((st = cuda_status(cudaMemcpy(U->d_Gfx + P.cell_off * 6 * n3, L.op->d_Gfx,
                                            sizeof(float2) * P.n_cells * 6 * n3,
                                            cudaMemcpyDeviceToDevice),
-                                "batch Gdf")))
+                                "batch Gfx")) ||
+              (st = cuda_status(cudaMemcpy(U->d_Gexp + P.cell_off, L.op->d_Gexp,
+                                           sizeof(int) * P.n_cells, cudaMemcpyDeviceToDevice),
+                                "batch G exponents")))
             return st;
         }
         kb_offset_i64<<<grid1d(P.n_constrained), T256>>>(P.n_constrained, L.op->d_constrained,

@@ -335,12 +335,13 @@ struct TmaTilesQ {
   GT *sG;
   uint32_t *sMap;
   uint64_t *mbar_g, *mbar_m;
+  bool map_ok = true;  // false: the map array is not 16-byte aligned (plain loads)
 
   __device__ __forceinline__ int cells_of(int64_t b) const {
     return (int)min((int64_t)E, n_cells - b * E);
   }
   __device__ __forceinline__ bool map_by_tma(int cells) const {
-    return L::map_tma && ((cells * M3 * 4) % 16 == 0);
+    return map_ok && L::map_tma && ((cells * M3 * 4) % 16 == 0);
   }
   // a bulk copy needs a 16-byte aligned start and a 16-byte multiple: 4-byte G
   // tiles of an odd number of cells with odd NQ^3 (an odd E, or the last batch)

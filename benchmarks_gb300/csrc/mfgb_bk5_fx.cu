@@ -1,0 +1,121 @@
+// The FP64-accurate collocation operator with offset double-float accumulation
+// (mfgb_bk5fx.cuh): its launcher, and the set-up of the per-cell scaled
+// geometric factors it reads.
+#include <algorithm>
+#include <cmath>
+
+#include "mfgb_bk5fx.cuh"
+#include "mfgb_internal.h"
+#include "mfgb_launch.cuh"
+
+namespace mfgb {
+
+// cells per CTA and resident CTAs per SM of the two thread-block shapes
+// (shape 4 = the alternative cells per CTA of mfgb_launch.cuh)
+template <int N> struct FxElems { static constexpr int value = ElemsPerCtaTma<N, ArithDF>::value; };
+template <int N> struct FxMinBlocks { static constexpr int value = TmaMinBlocks<N, ArithDF>::value; };
+template <int N> struct FxAltElems { static constexpr int value = AltElemsN<N>::value; };
+template <int N> struct FxAltMinBlocks {
+  static constexpr int value = AltMinBlocks<N, FxAltElems<N>::value, ArithDF>::value;
+};
+
+template <int N, int E, int MB, bool MT>
+static cudaError_t fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
+                             const double *src, double *dst, const BasisFX<N> &b, cudaStream_t s,
+                             const int *done) {
+  constexpr size_t smem = TmaLayout<N, E, ArithDF>::total;
+  static int per_sm = -1;
+  if (per_sm < 0)
+    per_sm = std::max(1, ctas_per_sm(bk5fx_tma_kernel<N, E, MB, MT>, E * N * N, smem));
+  const int64_t nb = (n_cells + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)per_sm * num_sms()));
+  if (n_cells <= 0) return cudaSuccess;
+  bk5fx_tma_kernel<N, E, MB, MT><<<grid, E * N * N, smem, s>>>(n_cells, map, G, gexp, src, dst, b,
+                                                                done, device_error_flag());
+  return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t fx_with_basis(int64_t n_cells, const uint32_t *map, const float2 *G,
+                                 const int *gexp, const double *src, double *dst, const double *D,
+                                 cudaStream_t s, const int *done) {
+  BasisFX<N> b;
+  const double K = 2.0 * (1.0 + std::ldexp(1.0, -20));
+  for (int q = 0; q < N * N; ++q) {
+    b.Dh[q] = (float)D[q];
+    b.Dl[q] = (float)(D[q] - (double)b.Dh[q]);
+  }
+  for (int i = 0; i < N; ++i) {
+    double rs = 0.0, cs = 0.0;
+    for (int m = 0; m < N; ++m) {
+      rs += std::fabs((double)b.Dh[i * N + m]);
+      cs += std::fabs((double)b.Dh[m * N + i]);
+    }
+    b.cg[i] = (float)(K * rs);
+    b.ci[i] = (float)(K * cs);
+  }
+  b.K = (float)K;
+  // bulk copies of the dof-map tiles need a 16-byte aligned map
+  const bool mt = (reinterpret_cast<uintptr_t>(map) & 15u) == 0;
+  const bool alt = kernel_shape(ArithClass<ArithDF>::value, N) == SHAPE_FX_ALT;
+  constexpr int E = FxElems<N>::value, MB = FxMinBlocks<N>::value;
+  constexpr int EA = FxAltElems<N>::value, MBA = FxAltMinBlocks<N>::value;
+  if (alt)
+    return mt ? fx_launch<N, EA, MBA, true>(n_cells, map, G, gexp, src, dst, b, s, done)
+              : fx_launch<N, EA, MBA, false>(n_cells, map, G, gexp, src, dst, b, s, done);
+  return mt ? fx_launch<N, E, MB, true>(n_cells, map, G, gexp, src, dst, b, s, done)
+            : fx_launch<N, E, MB, false>(n_cells, map, G, gexp, src, dst, b, s, done);
+}
+
+cudaError_t bk5_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
+                   const double *src, double *dst, const double *D, cudaStream_t s,
+                   const int *done) {
+  if (n_cells <= 0) return cudaSuccess;
+  if (map == nullptr || (reinterpret_cast<uintptr_t>(G) & 15u)) return cudaErrorInvalidValue;
+  switch (N) {
+#define MFGB_FXCASE(NN) \
+  case NN: return fx_with_basis<NN>(n_cells, map, G, gexp, src, dst, D, s, done);
+    MFGB_FXCASE(2) MFGB_FXCASE(3) MFGB_FXCASE(4) MFGB_FXCASE(5) MFGB_FXCASE(6) MFGB_FXCASE(7)
+    MFGB_FXCASE(8) MFGB_FXCASE(9)
+#undef MFGB_FXCASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Per-cell scaled split of the FP64 geometric factors: one warp per cell finds
+// the largest biased exponent e among the cell's 6 n^3 values and writes
+// G * 2^-(e - 1022) as float pairs (hi = nearest float, lo = nearest float of
+// the remainder); gexp[cell] = e - 1022 (0 for an all-zero cell).
+__global__ void g_to_fx_kernel(int64_t n_cells, int per_cell, const double *__restrict__ G,
+                               float2 *__restrict__ out, int *__restrict__ gexp) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < n_cells; c += n_warps) {
+    const double *g = G + c * per_cell;
+    int em = 0;
+    for (int t = lane; t < per_cell; t += 32) {
+      const int e = dexp(g[t]);
+      em = max(em, e == 0x7FF ? 0 : e);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, o));
+    const int off = fx_offset(em);
+    for (int t = lane; t < per_cell; t += 32) {
+      const double x = scalbn(g[t], -off);
+      const float hi = __double2float_rn(x);
+      out[c * per_cell + t] = make_float2(hi, __double2float_rn(x - (double)hi));
+    }
+    if (lane == 0) gexp[c] = off;
+  }
+}
+
+cudaError_t g_to_fx(int64_t n_cells, int per_cell, const double *G, float2 *Gfx, int *gexp,
+                    cudaStream_t s) {
+  if (n_cells <= 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n_cells + 7) / 8, 152 * 32);
+  g_to_fx_kernel<<<(int)blocks, 256, 0, s>>>(n_cells, per_cell, G, Gfx, gexp);
+  return cudaGetLastError();
+}
+
+}  // namespace mfgb

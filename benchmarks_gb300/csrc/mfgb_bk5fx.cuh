@@ -1,0 +1,397 @@
+// mfgb_bk5fx.cuh -- FP64-accurate BK5 collocation operator on the FP32 pipes with
+// offset ("fixed-exponent") double-float accumulation and per-cell exponent scaling.
+//
+// The operator is the one of bk5_tma_kernel (GLL collocation: gather through the
+// dof map with the 0xFFFFFFFF mask, collocation gradient, symmetric metric G,
+// transpose, atomic scatter; reference CEED_BK/include/kernels/BK5/
+// templated_cuda_kernels.cuh:50-122 and bakeoff_problems_dealii/include/
+// bk3_kokkos_kernel.h:129-151, 406-426) with the same bulk-TMA pipeline.  What
+// differs is the arithmetic:
+//
+// * Scaling.  Every cell's gathered values are multiplied by 2^-su, su chosen
+//   from the largest binary exponent among them so that |u| < 1, and the
+//   geometric factors are stored pre-multiplied by a per-cell 2^-sg (|G| < 1;
+//   sg in a per-cell int array).  The scalings are exact.  The cell's result is
+//   multiplied by 2^(su + sg) when it is converted back to double, so any FP64
+//   input range is carried (no float over- or underflow of the pairs).
+//
+// * Offset accumulation.  A dot product sum_k x_k y_k of double-float pairs is
+//   accumulated as T + S with T started at an offset C >= 2 B, where B bounds
+//   sum_k |x_k.hi y_k.hi|.  Every partial sum then keeps C/2 <= T <= 3C/2, so
+//     T' = fma(x.hi, y.hi, T)     rounds the product into T,
+//     d  = T' - T                 is exact (|T| >= |product|: Dekker's Fast2Sum),
+//     r  = fma(x.hi, y.hi, -d)    is the rounding error of T' (to float precision),
+//     S += (r + x.hi y.lo) + x.lo y.hi
+//   and at the end hi = T - C is exact (Sterbenz), lo = S.  That is 6 FP32-pipe
+//   instructions per multiply-add (5 for the first), against 12 for the
+//   TwoSum-based form of ArithDF, with an error of about 2^-46 of C.  The bounds
+//   B come from the data at hand: |u| < 1 for the gradient (B = sum_m |D[i][m]|),
+//   max |q| times the row sum of |G| per point for the metric, and the line
+//   maxima of |v| times the column sums of |D| for the transpose.
+//
+// A float32 restatement of this arithmetic with its error bound is in
+// tests/test_fx_arith.py.
+#pragma once
+#include "mfgb_bk5.cuh"
+
+namespace mfgb {
+
+// D split into float pairs plus the bound factors of the two contractions:
+//   cg[i] = K * sum_m |Dh[i][m]|  (gradient output i, |data| < 1)
+//   ci[i] = K * sum_m |Dh[m][i]|  (transpose output i, per unit of line maximum)
+//   K = 2 (1 + 2^-20): the factor 2 of the offset, plus a margin for the float
+//   rounding of the bound itself
+template <int N>
+struct BasisFX {
+  float Dh[N * N], Dl[N * N];
+  float cg[N], ci[N];
+  float K;
+};
+
+// offset accumulator: value = (T - C) + S
+struct fxacc {
+  float T, S;
+};
+
+__device__ __forceinline__ void fx_first(fxacc &a, float xh, float xl, float yh, float yl,
+                                         float C) {
+  a.T = __fmaf_rn(xh, yh, C);
+  const float d = __fsub_rn(a.T, C);
+  const float r = __fmaf_rn(xh, yh, -d);
+  a.S = __fmaf_rn(xl, yh, __fmaf_rn(xh, yl, r));
+}
+
+// the low-order terms of one product (its rounding error and the two cross
+// products) are summed first and join S with one addition: the two chains a
+// sum carries (T and S) advance by one dependent instruction per term
+__device__ __forceinline__ void fx_fma(fxacc &a, float xh, float xl, float yh, float yl) {
+  const float t = __fmaf_rn(xh, yh, a.T);
+  const float d = __fsub_rn(t, a.T);
+  const float r = __fmaf_rn(xh, yh, -d);
+  const float e = __fmaf_rn(xl, yh, __fmaf_rn(xh, yl, r));
+  a.S = __fadd_rn(a.S, e);
+  a.T = t;
+}
+
+__device__ __forceinline__ df fx_finish(const fxacc &a, float C) {
+  df r;
+  r.hi = __fsub_rn(a.T, C);
+  r.lo = a.S;
+  return r;
+}
+
+// biased binary exponent of a double (0 for zero and subnormals, 2047 for inf/NaN)
+__device__ __forceinline__ int dexp(double x) {
+  return (int)(((unsigned)(__double_as_longlong(x) >> 32) >> 20) & 0x7FFu);
+}
+
+// x * 2^-off as a float pair by integer operations (off chosen so that the
+// cell's largest value lands in [0.5, 1)): hi = the top 24 significant bits,
+// lo = the next 29 bits rounded to float.  Values below 2^-126 after scaling
+// (126 binades under the cell's largest) flush to zero; inf and NaN give NaN.
+__device__ __forceinline__ df fx_from_double(double x, int off) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const unsigned sign = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7FFu);
+  df r;
+  if (e == 0x7FF) { r.hi = __uint_as_float(0x7FC00000u); r.lo = 0.f; return r; }
+  const int es = e - off;
+  if (es <= 896) { r.hi = 0.f; r.lo = 0.f; return r; }
+  const unsigned hm = ((hw & 0xFFFFFu) << 3) | (lw >> 29);
+  r.hi = __uint_as_float(sign | ((unsigned)(es - 896) << 23) | hm);
+  const unsigned rem = lw & 0x1FFFFFFFu;
+  if (rem == 0u || es < 949) {
+    r.lo = 0.f;
+  } else {
+    const unsigned fb = __float_as_uint(__uint2float_rn(rem));
+    r.lo = __uint_as_float(sign | (fb + ((unsigned)(es - 1075) << 23)));
+  }
+  return r;
+}
+
+// f * 2^sc as a double by integer operations; float subnormals -> 0, results
+// outside the double range -> 0 or +-inf, inf/NaN kept
+__device__ __forceinline__ double fx_f2d(float f, int sc) {
+  const unsigned u = __float_as_uint(f);
+  const int ex = (int)((u >> 23) & 0xFFu);
+  const unsigned long long sgn = (unsigned long long)(u & 0x80000000u) << 32;
+  if (ex == 0) return 0.0;
+  if (ex == 255)
+    return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull |
+                                            ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+  const int e2 = ex + 896 + sc;
+  if (e2 <= 0) return __longlong_as_double((long long)sgn);
+  if (e2 >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)e2 << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
+// the scale offset of a cell from its largest biased exponent
+__device__ __forceinline__ int fx_offset(int emax) { return emax > 0 ? emax - 1022 : 0; }
+
+// Column kernel (thread (e, j, k) owns the i-column of cell e) with the bulk-TMA
+// pipeline of bk5_tma_kernel: per batch, barrier A waits for G(b) (the u(b)
+// gather was prefetched into registers during batch b-1, its largest exponent
+// per cell reduced into s_emax by shared atomics), then the scaled u goes to
+// shared memory (barrier B), map(b+next) is requested, gradient + metric run
+// (barrier C), G(b+next) is requested, u(b+next) is prefetched and the
+// transpose + atomic scatter of batch b runs.  MAPTMA = false loads the dof map
+// with plain loads (a map array that is not 16-byte aligned).  gexp[cell] is
+// the per-cell exponent offset of the scaled G.
+template <int N, int E, int MB, bool MAPTMA>
+__global__ void __launch_bounds__(E * N * N, MB)
+    bk5fx_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                     const float2 *__restrict__ G, const int *__restrict__ gexp,
+                     const double *__restrict__ src, double *__restrict__ dst,
+                     const BasisFX<N> basis, const int *__restrict__ done_flag,
+                     int *__restrict__ err_flag) {
+  if (done_flag != nullptr && *done_flag) return;
+  using L = TmaLayout<N, E, ArithDF>;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float2 *sG = reinterpret_cast<float2 *>(smem);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  df *s_u = reinterpret_cast<df *>(smem + L::g_bytes + L::map_bytes);
+  df *s_vs = s_u + E * N3;
+  df *s_vt = s_vs + E * N3;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+  uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
+  __shared__ int s_emax[2][E];
+  // per cell: max |v_s(i, ., k)| at [i][k] and max |v_t(i, j, .)| at [i][j] (float bits)
+  __shared__ int s_ms[E][N2], s_mt[E][N2];
+
+  const int tid = threadIdx.x;
+  const int el = tid / N2;
+  const int jk = tid - el * N2;
+  const int j = jk / N;
+  const int k = jk - j * N;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  int64_t batch = blockIdx.x;
+  if (batch >= n_batches) return;  // uniform across the CTA
+
+  // rows / columns of D this thread needs with a runtime index, and their bounds
+  float Djh[N], Djl[N], Dkh[N], Dkl[N], Dtjh[N], Dtjl[N], Dtkh[N], Dtkl[N];
+#pragma unroll
+  for (int m = 0; m < N; ++m) {
+    Djh[m] = basis.Dh[j * N + m];
+    Djl[m] = basis.Dl[j * N + m];
+    Dkh[m] = basis.Dh[k * N + m];
+    Dkl[m] = basis.Dl[k * N + m];
+    Dtjh[m] = basis.Dh[m * N + j];
+    Dtjl[m] = basis.Dl[m * N + j];
+    Dtkh[m] = basis.Dh[m * N + k];
+    Dtkl[m] = basis.Dl[m * N + k];
+  }
+  const float cgj = basis.cg[j], cgk = basis.cg[k], cij = basis.ci[j], cik = basis.ci[k];
+
+  TmaTiles<N, E, ArithDF> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
+  T.map_ok = MAPTMA;
+  auto fail = [&](uint32_t pg, uint32_t pm) {
+    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
+    mbar_wait(mbar_m, pm);
+  };
+
+  if (tid < 2 * E) (&s_emax[0][0])[tid] = 0;
+  if (tid == 0) {
+    mbar_init(mbar_g, 1);
+    mbar_init(mbar_m, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    T.issue_g(batch);
+    T.issue_map(batch);
+  }
+  uint32_t ph_g = 0, ph_m = 0;
+  uint32_t idx[N];
+  double raw[N];
+  int ge = 0;  // G exponent offset of this thread's cell in the prefetched batch
+  // gathered column -> its largest exponent into the cell's slot
+  auto reduce_exp = [&](int slot) {
+    int em = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) em = max(em, idx[i] != MFGB_INVALID_DOF ? dexp(raw[i]) : 0);
+    if (em) atomicMax(&s_emax[slot][el], em);
+  };
+  {
+    const bool ok = mbar_wait(mbar_m, ph_m);
+    if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
+    ph_m ^= 1u;
+    T.gather(batch, el, jk, idx, raw);
+    reduce_exp(0);
+    if (el < T.cells_of(batch)) ge = __ldg(gexp + batch * E + el);
+  }
+
+  for (int it = 0; batch < n_batches; batch += gridDim.x, ++it) {
+    const int slot = it & 1;
+    const int64_t next = batch + gridDim.x;
+    const bool has_next = next < n_batches;
+    const bool okg = mbar_wait(mbar_g, ph_g);
+    if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
+    ph_g ^= 1u;
+    T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase by barrier B
+    s_ms[el][jk] = 0;  // read by the previous batch's transpose before barrier A
+    s_mt[el][jk] = 0;
+    const int su = fx_offset(s_emax[slot][el]);
+    const int sc = su + ge;  // the cell's result scale
+    df u[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      u[i] = idx[i] != MFGB_INVALID_DOF ? fx_from_double(raw[i], su) : df{0.f, 0.f};
+      s_u[el * N3 + i * N2 + jk] = u[i];
+    }
+    __syncthreads();  // barrier B: s_u ready, s_emax[slot] read; the map tile is free
+    if (jk == 0) s_emax[slot][el] = 0;  // next written after barrier C of the next batch
+    if (tid == 0 && has_next) {
+      fence_proxy_async_smem();
+      T.issue_map(next);
+    }
+
+    const bool valid = el < T.cells_of(batch);
+    df vr[N];
+    const float2 *Gc = sG + el * 6 * N3 + jk;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      // ---- gradient: q_r = D[i][.] u(., j, k), q_s = D[j][.] u(i, ., k), q_t = D[k][.] u(i, j, .)
+      fxacc ar, as, at;
+      const float cr = basis.cg[i];
+      fx_first(ar, basis.Dh[i * N], basis.Dl[i * N], u[0].hi, u[0].lo, cr);
+      {
+        const df a = s_u[el * N3 + i * N2 + k], b = s_u[el * N3 + i * N2 + j * N];
+        fx_first(as, Djh[0], Djl[0], a.hi, a.lo, cgj);
+        fx_first(at, Dkh[0], Dkl[0], b.hi, b.lo, cgk);
+      }
+#pragma unroll
+      for (int m = 1; m < N; ++m) {
+        fx_fma(ar, basis.Dh[i * N + m], basis.Dl[i * N + m], u[m].hi, u[m].lo);
+        const df a = s_u[el * N3 + i * N2 + m * N + k], b = s_u[el * N3 + i * N2 + j * N + m];
+        fx_fma(as, Djh[m], Djl[m], a.hi, a.lo);
+        fx_fma(at, Dkh[m], Dkl[m], b.hi, b.lo);
+      }
+      const df qr = fx_finish(ar, cr), qs = fx_finish(as, cgj), qt = fx_finish(at, cgk);
+      // ---- metric, bound per point: max |q| times the row sums of |G|
+      float2 grr = make_float2(0.f, 0.f), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+      if (valid) {
+        grr = Gc[0 * N3 + i * N2];
+        grs = Gc[1 * N3 + i * N2];
+        grt = Gc[2 * N3 + i * N2];
+        gss = Gc[3 * N3 + i * N2];
+        gst = Gc[4 * N3 + i * N2];
+        gtt = Gc[5 * N3 + i * N2];
+      }
+      const float kq = basis.K * fmaxf(fmaxf(fabsf(qr.hi), fabsf(qs.hi)), fabsf(qt.hi));
+      const float Cr = (fabsf(grr.x) + fabsf(grs.x) + fabsf(grt.x)) * kq;
+      const float Cs = (fabsf(grs.x) + fabsf(gss.x) + fabsf(gst.x)) * kq;
+      const float Ct = (fabsf(grt.x) + fabsf(gst.x) + fabsf(gtt.x)) * kq;
+      fxacc br, bs, bt;
+      fx_first(br, grr.x, grr.y, qr.hi, qr.lo, Cr);
+      fx_fma(br, grs.x, grs.y, qs.hi, qs.lo);
+      fx_fma(br, grt.x, grt.y, qt.hi, qt.lo);
+      fx_first(bs, grs.x, grs.y, qr.hi, qr.lo, Cs);
+      fx_fma(bs, gss.x, gss.y, qs.hi, qs.lo);
+      fx_fma(bs, gst.x, gst.y, qt.hi, qt.lo);
+      fx_first(bt, grt.x, grt.y, qr.hi, qr.lo, Ct);
+      fx_fma(bt, gst.x, gst.y, qs.hi, qs.lo);
+      fx_fma(bt, gtt.x, gtt.y, qt.hi, qt.lo);
+      vr[i] = fx_finish(br, Cr);
+      const df vs = fx_finish(bs, Cs), vt = fx_finish(bt, Ct);
+      s_vs[el * N3 + i * N2 + jk] = vs;
+      s_vt[el * N3 + i * N2 + jk] = vt;
+      atomicMax(&s_ms[el][i * N + k], __float_as_int(fabsf(vs.hi)));
+      atomicMax(&s_mt[el][i * N + j], __float_as_int(fabsf(vt.hi)));
+    }
+    __syncthreads();  // barrier C: G tile consumed, s_vs / s_vt ready
+    if (tid == 0 && has_next) {
+      fence_proxy_async_smem();
+      T.issue_g(next);
+    }
+
+    // this batch's scatter targets; then prefetch the next batch's gather
+    uint32_t cur[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cur[i] = idx[i];
+    if (has_next) {
+      const bool okm = mbar_wait(mbar_m, ph_m);
+      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+      ph_m ^= 1u;
+      if (okm) {
+        T.gather(next, el, jk, idx, raw);
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) { idx[i] = MFGB_INVALID_DOF; raw[i] = 0.0; }
+      }
+      ge = el < T.cells_of(next) ? __ldg(gexp + next * E + el) : 0;
+    }
+
+    // ---- transpose: y = sum_m D[m][i] v_r(m,j,k) + D[m][j] v_s(i,m,k) + D[m][k] v_t(i,j,m),
+    // the thread's N outputs accumulated together (N independent chains); the
+    // bound of output i: max |v_r| of the own column and the s- and t-line maxima
+    // the metric phase reduced into s_ms / s_mt
+    float mr = 0.f;
+#pragma unroll
+    for (int m = 0; m < N; ++m) mr = fmaxf(mr, fabsf(vr[m].hi));
+    if constexpr (N <= 5) {
+      fxacc a[N];
+      float C[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const float ms = __int_as_float(s_ms[el][i * N + k]);
+        const float mt = __int_as_float(s_mt[el][i * N + j]);
+        C[i] = __fmaf_rn(mt, cik, __fmaf_rn(ms, cij, mr * basis.ci[i]));
+        fx_first(a[i], basis.Dh[i], basis.Dl[i], vr[0].hi, vr[0].lo, C[i]);
+      }
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        if (m > 0) {
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+            fx_fma(a[i], basis.Dh[m * N + i], basis.Dl[m * N + i], vr[m].hi, vr[m].lo);
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const df ls = s_vs[el * N3 + i * N2 + m * N + k];
+          fx_fma(a[i], Dtjh[m], Dtjl[m], ls.hi, ls.lo);
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const df lt = s_vt[el * N3 + i * N2 + j * N + m];
+          fx_fma(a[i], Dtkh[m], Dtkl[m], lt.hi, lt.lo);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const df y = fx_finish(a[i], C[i]);
+        if (cur[i] != MFGB_INVALID_DOF)
+          atomicAdd(dst + cur[i], fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
+      }
+    } else {
+      // larger N: one output at a time (the N accumulators would not fit)
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const float ms = __int_as_float(s_ms[el][i * N + k]);
+        const float mt = __int_as_float(s_mt[el][i * N + j]);
+        const float C = __fmaf_rn(mt, cik, __fmaf_rn(ms, cij, mr * basis.ci[i]));
+        fxacc a;
+        fx_first(a, basis.Dh[i], basis.Dl[i], vr[0].hi, vr[0].lo, C);
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          if (m > 0) fx_fma(a, basis.Dh[m * N + i], basis.Dl[m * N + i], vr[m].hi, vr[m].lo);
+          const df ls = s_vs[el * N3 + i * N2 + m * N + k];
+          const df lt = s_vt[el * N3 + i * N2 + j * N + m];
+          fx_fma(a, Dtjh[m], Dtjl[m], ls.hi, ls.lo);
+          fx_fma(a, Dtkh[m], Dtkl[m], lt.hi, lt.lo);
+        }
+        const df y = fx_finish(a, C);
+        if (cur[i] != MFGB_INVALID_DOF)
+          atomicAdd(dst + cur[i], fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
+      }
+    }
+    // the prefetched gather's largest exponent per cell, once its loads have
+    // landed (read after the next barrier A)
+    if (has_next) reduce_exp(slot ^ 1);
+  }
+}
+
+}  // namespace mfgb

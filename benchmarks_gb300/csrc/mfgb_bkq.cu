@@ -61,6 +61,17 @@ mfgb_status bkq_entry(const char *name, bool laplace, int degree, int64_t nelmt,
   if (nelmt == 0) return MFGB_OK;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
+  if (arith == MFGB_ARITH_FP64_DF) {
+    // the double-float range of the inputs and of the caller's coefficients,
+    // reported through the device error word (mfgb_check_device_errors)
+    const int nm = degree + 1, nq = degree + 2;
+    int *slot = nullptr;
+    mfgb_status st = cuda_status(cudaMallocAsync((void **)&slot, sizeof(int), s), "range slot");
+    if (!st) st = vec_range_check(slot, nelmt * nm * nm * nm, in, s);
+    if (slot) cudaFreeAsync(slot, s);
+    if (!st) st = cells_range_check(nelmt, (laplace ? 6 : 1) * nq * nq * nq, coef, s);
+    if (st) return st;
+  }
   if (arith == MFGB_ARITH_FP64)
     e = laplace ? bkq_dispatch<ArithF64, true>(degree, nelmt, basis, dbasis, coef, in, out, s)
                 : bkq_dispatch<ArithF64, false>(degree, nelmt, basis, dbasis, coef, in, out, s);

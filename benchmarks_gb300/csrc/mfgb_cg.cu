@@ -270,7 +270,7 @@ extern "C" mfgb_status mfgb_cg_solve(const mfgb_operator *cop, const double *d_b
   const int64_t n = op->n_dofs;
   cudaStream_t user = (cudaStream_t)stream;
   mfgb_status st;
-  if (ctl->arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if ((st = ensure_arith(op, ctl->arith))) return st;
 
   // work vectors: r, p, v, partials, scalars
   DevBuf br, bp, bv, bpart, bsc;
@@ -425,7 +425,8 @@ namespace mfgb {
 constexpr int64_t NOALLOC_PAP_CAP = 152 * 64 + 1;
 constexpr int64_t NOALLOC_VEC_PART = 2 * VEC_BLOCKS + 8;
 constexpr int64_t NOALLOC_SCALARS = 32;  // doubles reserved for CgScalars
-static_assert(sizeof(CgScalars) <= NOALLOC_SCALARS * sizeof(double), "scalar slot too small");
+// the last 8 bytes of the scalar slot hold the double-float range check's int
+static_assert(sizeof(CgScalars) <= NOALLOC_SCALARS * sizeof(double) - 8, "scalar slot too small");
 constexpr int64_t NOALLOC_DOUBLES =
     3 * (int64_t)MFGB_CG_NOALLOC_MAX_DOFS + NOALLOC_PAP_CAP + NOALLOC_VEC_PART + NOALLOC_SCALARS;
 
@@ -434,7 +435,10 @@ static __device__ __align__(256) double g_cg_noalloc_scratch[NOALLOC_DOUBLES];
 static std::mutex g_noalloc_mutex;
 static double *g_noalloc_ptr[64] = {nullptr};
 
-// device address of the scratch array on the current device (looked up once)
+// device address of the scratch array on the current device (looked up once
+// per device and cached for the life of the process; a cudaDeviceReset or a
+// teardown of the primary context invalidates the cached address, so the
+// library must not be used across either)
 static mfgb_status noalloc_scratch(double **out) {
   int dev = 0;
   mfgb_status st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
@@ -457,17 +461,24 @@ static mfgb_status noalloc_scratch(double **out) {
 // vmult (partials == nullptr) or accumulate-with-energy, never allocating:
 // double-float arithmetic uses the operator's split copy of G when an earlier
 // call created it, and otherwise splits the FP64 geometric factors on load.
+// The double-float kernels without per-cell scaling also check src's range
+// into the device error word (range_slot: an int of the scratch array).
 static mfgb_status noalloc_apply(const mfgb_operator *op, double *dst, const double *src, int arith,
                                  double *partials, int *grid, cudaStream_t s, const int *done,
-                                 bool accumulate = false) {
+                                 int *range_slot, bool accumulate = false) {
   mfgb_status st;
   const bool full = !partials && !accumulate;
   if (full && (st = cuda_status(cudaMemsetAsync(dst, 0, sizeof(double) * op->n_dofs, s),
                                 "dst = 0")))
     return st;
+  if (arith == MFGB_ARITH_FP64_DF && !(op->d_Gfx && !partials) &&
+      (st = vec_range_check(range_slot, op->n_dofs, src, s)))
+    return st;
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64)
     e = bk5_f64(op->n, op->n_cells, op->d_map, op->d_G, src, dst, op->D, partials, grid, s, done);
+  else if (op->d_Gfx && !partials)
+    e = bk5_fx(op->n, op->n_cells, op->d_map, op->d_Gfx, op->d_Gexp, src, dst, op->D, s, done);
   else if (op->d_Gdf)
     e = bk5_df(op->n, op->n_cells, op->d_map, op->d_Gdf, src, dst, op->D, partials, grid, s, done);
   else
@@ -513,11 +524,18 @@ extern "C" mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const doub
   double *pap_part = v + MFGB_CG_NOALLOC_MAX_DOFS;
   double *vec_part = pap_part + NOALLOC_PAP_CAP;
   CgScalars *sc = (CgScalars *)(vec_part + NOALLOC_VEC_PART);
+  int *range_slot = reinterpret_cast<int *>(vec_part + NOALLOC_VEC_PART + NOALLOC_SCALARS - 1);
   cudaStream_t s = (cudaStream_t)stream;
   const double *dinv = d_inv_diag;
+  // double-float without a prebuilt copy of G splits the FP64 factors on load:
+  // their per-cell range goes to the device error word
+  if (ctl->arith == MFGB_ARITH_FP64_DF && !op->d_Gfx && !op->d_Gdf &&
+      (st = cells_range_check(op->n_cells, 6 * op->n * op->n * op->n, op->d_G, s)))
+    return st;
 
   // r0 = b - A x0, p0 = z0
-  if ((st = noalloc_apply(op, v, d_x, ctl->arith, nullptr, nullptr, s, nullptr))) return st;
+  if ((st = noalloc_apply(op, v, d_x, ctl->arith, nullptr, nullptr, s, nullptr, range_slot)))
+    return st;
   cg_init_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_b, v, r, p, dinv, vec_part);
   finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(vec_part, VEC_BLOCKS, 2, vec_part + 2 * VEC_BLOCKS);
   finish_sum_kernel<<<1, VEC_THREADS, 0, s>>>(vec_part + 1, VEC_BLOCKS, 2,
@@ -534,6 +552,8 @@ extern "C" mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const doub
   info->steps = 0;
   info->converged = 0;
   const double tol_eff = std::fmax(ctl->tol, ctl->reduce * res0);
+  // a bounded copy wait that ran out inside the first apply voids r0
+  if ((st = mfgb_check_device_errors(s))) return st;
   if (res0 <= tol_eff) {
     info->converged = 1;
     return MFGB_OK;
@@ -561,7 +581,7 @@ extern "C" mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const doub
   for (;;) {
     for (int k = 0; k < K; ++k) {
       const int parity = k & 1;
-      if ((st = noalloc_apply(op, v, p, ctl->arith, nullptr, nullptr, s, &sc->done,
+      if ((st = noalloc_apply(op, v, p, ctl->arith, nullptr, nullptr, s, &sc->done, range_slot,
                               /*accumulate=*/true)))
         return st;
       if (op->n_constrained)
@@ -583,6 +603,9 @@ extern "C" mfgb_status mfgb_cg_solve_noalloc(const mfgb_operator *op, const doub
   info->steps = out.final_its;
   info->last = out.final_res;
   info->converged = out.done == 1;
+  // reads and clears the device error word (a 4-byte copy, no allocation): a
+  // bounded copy wait that ran out in any operator launch of the solve voids x
+  if ((st = mfgb_check_device_errors(s))) return st;
   if (out.done == 1) return MFGB_OK;
   if (std::isnan(out.final_res)) {
     set_error("mfgb_cg_solve_noalloc: residual became NaN");

@@ -25,8 +25,10 @@ struct df {
 
 // double -> (hi, lo) with integer ops: hi = x truncated to 24 significant
 // bits, lo = the remaining 29 mantissa bits rounded to float.  |x| < 2^-126
-// flushes to zero (below any value this engine carries); |x| >= 2^128 is
-// outside the float exponent range and is returned as (+-inf, 0).
+// flushes to zero; |x| >= 2^128 is outside the float exponent range and is
+// returned as (+-inf, 0); NaN stays NaN.  (The GLL collocation operator scales
+// every cell by a power of two first, mfgb_bk5fx.cuh; the other double-float
+// kernels rely on the range check of their inputs, mfgb_api.cu.)
 __device__ __forceinline__ df df_from_double(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
@@ -34,7 +36,12 @@ __device__ __forceinline__ df df_from_double(double x) {
   const int e = (int)((hw >> 20) & 0x7FFu);
   df r;
   if (e <= 896) { r.hi = 0.f; r.lo = 0.f; return r; }
-  if (e >= 1151) { r.hi = __uint_as_float(sign | 0x7F800000u); r.lo = 0.f; return r; }
+  if (e >= 1151) {
+    const bool nan = e == 0x7FF && ((hw & 0xFFFFFu) | lw) != 0u;
+    r.hi = __uint_as_float(sign | (nan ? 0x7FC00000u : 0x7F800000u));
+    r.lo = 0.f;
+    return r;
+  }
   const unsigned hm = ((hw & 0xFFFFFu) << 3) | (lw >> 29);
   r.hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | hm);
   const unsigned rem = lw & 0x1FFFFFFFu;
@@ -47,11 +54,16 @@ __device__ __forceinline__ df df_from_double(double x) {
   return r;
 }
 
-// exact float -> double widening by integer ops (subnormal floats -> 0)
+// exact float -> double widening by integer ops (subnormal floats -> 0; inf
+// and NaN kept)
 __device__ __forceinline__ double double_from_float_exact(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned ex = (u >> 23) & 0xFFu;
   if (ex == 0u) return 0.0;
+  if (ex == 0xFFu)
+    return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                            0x7FF0000000000000ull |
+                                            ((unsigned long long)(u & 0x7FFFFFu) << 29)));
   const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
                                ((unsigned long long)(ex + 896u) << 52) |
                                ((unsigned long long)(u & 0x7FFFFFu) << 29);

@@ -16,6 +16,9 @@ struct mfgb_operator {
   double *d_G = nullptr;          // [n_cells][6][n^3]
   float2 *d_Gdf = nullptr;        // same, double-float pairs (built on demand)
   float *d_G32 = nullptr;         // same, FP32 (built on demand)
+  float2 *d_Gfx = nullptr;        // GLL operators: G * 2^-gexp[cell] as float pairs (built on demand)
+  int *d_Gexp = nullptr;          // the per-cell exponent offsets of d_Gfx
+  int *d_range = nullptr;         // slot of the double-float input range check
   int64_t *d_constrained = nullptr;
   double D[81] = {0};             // derivative matrix D[q*n + b]
   double gll_x[9] = {0}, gll_w[9] = {0};
@@ -57,6 +60,13 @@ cudaError_t bk5_f64(int N, int64_t n_cells, const uint32_t *map, const double *G
 cudaError_t bk5_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const double *src,
                    double *dst, const double *D, double *partials, int *grid, cudaStream_t s,
                     const int *done = nullptr);
+// FP64-accurate collocation operator with offset double-float accumulation and
+// per-cell scaling (mfgb_bk5_fx.cu); G = the scaled pairs, gexp their offsets
+cudaError_t bk5_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
+                   const double *src, double *dst, const double *D, cudaStream_t s,
+                   const int *done = nullptr);
+cudaError_t g_to_fx(int64_t n_cells, int per_cell, const double *G, float2 *Gfx, int *gexp,
+                    cudaStream_t s);
 cudaError_t bk5_df_g64(int N, int64_t n_cells, const uint32_t *map, const double *G,
                        const double *src, double *dst, const double *D, cudaStream_t s,
                        const int *done = nullptr);
@@ -131,7 +141,26 @@ cudaError_t invert_diagonal(int64_t n, double *d, cudaStream_t s);
 // operator helpers (mfgb_api.cu)
 mfgb_status create_box_strided(const mfgb_box_desc *box, const BoxStride *bs,
                                mfgb_operator **out);
+// kernel shape table (arithmetic class 0 FP64, 1 double-float, 2 FP32; N = p + 1);
+// double-float shapes >= kShapeFx select the offset-accumulation kernel
+int kernel_shape(int arith_class, int N);
+constexpr int kShapeFx = 5;
+// bits of the device error word (mfgb_check_device_errors)
+constexpr int kDevErrTimeout = 1, kDevErrRange = 2;
+// the double-float input range (mfgb_api.cu): stream-ordered check of a source
+// vector into the device error word, and a synchronous check of caller arrays
+mfgb_status range_check_async(mfgb_operator *op, int64_t n, const double *v, cudaStream_t s);
+mfgb_status vec_range_check(int *slot, int64_t n, const double *v, cudaStream_t s);
+mfgb_status cells_range_check(int64_t n_cells, int per_cell, const double *G, cudaStream_t s);
+mfgb_status range_check_sync(int64_t n, const double *v, int64_t n_cells, int per_cell,
+                             const double *G, cudaStream_t s, const char *what);
+// true when double-float applies of op run the per-cell scaled kernel
+bool uses_fx(const mfgb_operator *op);
 mfgb_status ensure_df(mfgb_operator *op);
+// the copy of G the FP64_DF arithmetic of apply_range reads: the scaled pairs of
+// the offset-accumulation kernel for GLL operators, the plain pairs otherwise
+mfgb_status ensure_fx(mfgb_operator *op);
+mfgb_status ensure_arith(mfgb_operator *op, int arith);
 mfgb_status ensure_partials(mfgb_operator *op, int n);
 // dst += A src (cell loop only: no zeroing, no identity rows); `done` lets
 // a captured solver iteration skip the work once converged

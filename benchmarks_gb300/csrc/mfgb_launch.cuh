@@ -67,7 +67,10 @@ template <> struct ElemsPerCtaPt<9> { static constexpr int value = 1; };
 // Kernel shape: 0 = column (thread owns an i-column), 1 = point-per-thread,
 // 2 = column with TMA-prefetched geometric factors.  Default per
 // (arithmetic, N); overridable at run time (autotuner).
-enum { SHAPE_COLUMN = 0, SHAPE_POINT = 1, SHAPE_TMA = 2, SHAPE_COLUMN_ALT = 3, SHAPE_TMA_ALT = 4 };
+// 5 and 6 (double-float only, GLL operators): the offset-accumulation kernel of
+// mfgb_bk5fx.cuh at the shape-2 and shape-4 cells per CTA; elsewhere they run as 2 / 4.
+enum { SHAPE_COLUMN = 0, SHAPE_POINT = 1, SHAPE_TMA = 2, SHAPE_COLUMN_ALT = 3, SHAPE_TMA_ALT = 4,
+       SHAPE_FX = 5, SHAPE_FX_ALT = 6 };
 int kernel_shape(int arith_class, int N);  // mfgb_api.cu
 int *device_error_flag();                  // mfgb_api.cu
 
@@ -149,6 +152,8 @@ cudaError_t bk5_launch(int64_t n_cells, const uint32_t *map, const typename A::G
                        const Basis<N, A> &basis, double *partials, int *grid_used,
                        cudaStream_t stream, const int *done_flag = nullptr) {
   int shape = kernel_shape(ArithClass<A>::value, N);
+  if (shape == SHAPE_FX) shape = SHAPE_TMA;
+  if (shape == SHAPE_FX_ALT) shape = SHAPE_TMA_ALT;
   // without an alternative cells-per-CTA instantiation (E-vector mode, other
   // arithmetic, large N) shapes 3 / 4 run as 0 / 2; bulk copies need 16-byte
   // aligned tiles: caller arrays that are not 16-byte aligned use the column

@@ -501,7 +501,7 @@ static mfgb_status mg_setup_impl(const mfgb_box_desc *fine, const mfgb_mg_params
         (st = dalloc(&M.t, ts * M.n)) || (st = dalloc(&M.inv_diag, ts * M.n)))
       break;
     if (prm->precision == 32 && (st = ensure_g32(M.op))) break;
-    if (prm->precision == 64 && (st = ensure_df(M.op))) break;
+    if (prm->precision == 64 && (st = ensure_arith(M.op, MFGB_ARITH_FP64_DF))) break;
     // Jacobi in the V-cycle precision
     double *d64 = nullptr;
     if ((st = dalloc((void **)&d64, sizeof(double) * M.n))) break;
@@ -703,7 +703,7 @@ extern "C" mfgb_status mfgb_mg_cg_solve(const mfgb_operator *cop, mfgb_mg *mg, c
   cudaStreamWaitEvent(s, ev, 0);
   cudaEventDestroy(ev);
   const int arith = ctl->arith;
-  if (arith == MFGB_ARITH_FP64_DF && (st = ensure_df(op))) return st;
+  if ((st = ensure_arith(op, arith))) return st;
   const unsigned g = grid1d(n);
   double *r = mg->r, *z = mg->z, *p = mg->p, *v = mg->v, *part = mg->part, *scal = mg->scal;
   // scal: [0] r.z (current), [1] p.v, [2] r.z (new), [3] |r|^2

@@ -1,0 +1,151 @@
+// mfgb_rates.cu -- arithmetic-pipe throughput on the running GPU, the numbers the
+// operator kernels' choice of arithmetic rests on: FP64 FMA (DFMA), FP32 FMA,
+// FP64 tensor-core MMA (mma.sync m8n8k4 f64, the instruction of the reference's
+// sum_factorization/include/kernels/BK1/cuda_mma_kernels.cuh:94-100) and the
+// legacy BF16 tensor-core MMA (mma.sync m16n8k16, FP32 accumulation).
+//
+// Every kernel runs independent dependency chains in registers (no memory
+// traffic but one store per thread, which keeps the work alive) on a grid of
+// 8 CTAs x 256 threads per SM.  mfgb_pipe_rate returns operations per second
+// (FLOP/s counting an FMA as 2) from CUDA-event timing of `reps` launches.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mfgb.h"
+#include "mfgb_internal.h"
+
+namespace mfgb {
+namespace {
+
+constexpr int kChains = 8;
+
+__global__ void __launch_bounds__(256) dfma_kernel(int iters, double *out) {
+  double a[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) a[c] = 1.0 + 1e-3 * (threadIdx.x + c);
+  const double x = 0.999999, y = 1e-7;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) a[c] = __fma_rn(a[c], x, y);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) s += a[c];
+  out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) ffma_kernel(int iters, double *out) {
+  float a[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) a[c] = 1.f + 1e-3f * (threadIdx.x + c);
+  const float x = 0.9999f, y = 1e-7f;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) a[c] = __fmaf_rn(a[c], x, y);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) s += a[c];
+  out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+// D(8x8) += A(8x4) B(4x8) in FP64: per thread one A and one B element, two
+// accumulator elements; 4 independent accumulators per warp
+__global__ void __launch_bounds__(256) dmma_kernel(int iters, double *out) {
+  double acc[4][2];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) acc[c][0] = acc[c][1] = 0.0;
+  const double a = 1.0 + 1e-3 * threadIdx.x, b = 0.5 - 1e-4 * threadIdx.x;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      asm volatile(
+          "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+          : "+d"(acc[c][0]), "+d"(acc[c][1])
+          : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) s += acc[c][0] + acc[c][1];
+  out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+// D(16x8) += A(16x16) B(16x8), BF16 inputs, FP32 accumulation
+__global__ void __launch_bounds__(256) hmma_kernel(int iters, double *out) {
+  float acc[4][4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[c][r] = 0.f;
+  const uint32_t a0 = 0x3F803F80u + threadIdx.x, b0 = 0x3F003F00u + threadIdx.x;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+          "{%8, %9}, {%0, %1, %2, %3};"
+          : "+f"(acc[c][0]), "+f"(acc[c][1]), "+f"(acc[c][2]), "+f"(acc[c][3])
+          : "r"(a0), "r"(a0), "r"(a0), "r"(a0), "r"(b0), "r"(b0));
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) s += acc[c][0] + acc[c][1] + acc[c][2] + acc[c][3];
+  out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+}  // namespace mfgb
+
+using namespace mfgb;
+
+// pipe: 0 DFMA, 1 FFMA, 2 DMMA m8n8k4 f64, 3 BF16 mma.sync m16n8k16.
+// *ops_per_s = floating-point operations per second (FMA = 2, MMA = 2 m n k).
+extern "C" mfgb_status mfgb_pipe_rate(int pipe, int iters, int reps, double *ops_per_s) {
+  if (pipe < 0 || pipe > 3 || iters < 1 || reps < 1 || !ops_per_s) {
+    set_error("mfgb_pipe_rate: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  int dev = 0, sms = 0;
+  mfgb_status st;
+  if ((st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice")) ||
+      (st = cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                        "SM count")))
+    return st;
+  const int blocks = 8 * sms, threads = 256;
+  double *out = nullptr;
+  if ((st = cuda_status(cudaMalloc(&out, sizeof(double) * blocks * threads), "rates buffer")))
+    return st;
+  auto launch = [&]() {
+    switch (pipe) {
+      case 0: dfma_kernel<<<blocks, threads>>>(iters, out); break;
+      case 1: ffma_kernel<<<blocks, threads>>>(iters, out); break;
+      case 2: dmma_kernel<<<blocks, threads>>>(iters, out); break;
+      default: hmma_kernel<<<blocks, threads>>>(iters, out); break;
+    }
+  };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  launch();  // warm-up
+  cudaEventRecord(e0);
+  for (int r = 0; r < reps; ++r) launch();
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if ((st = cuda_status(e, "mfgb_pipe_rate"))) return st;
+  const double threads_total = (double)blocks * threads;
+  double flops_per_iter;  // per thread
+  switch (pipe) {
+    case 0:
+    case 1: flops_per_iter = 2.0 * kChains; break;
+    case 2: flops_per_iter = 4.0 * 2.0 * 8 * 8 * 4 / 32.0; break;   // 4 MMAs per warp
+    default: flops_per_iter = 4.0 * 2.0 * 16 * 8 * 16 / 32.0; break;
+  }
+  *ops_per_s = threads_total * flops_per_iter * iters * reps / (ms * 1e-3);
+  return MFGB_OK;
+}

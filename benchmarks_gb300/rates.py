@@ -1,0 +1,40 @@
+"""Arithmetic-pipe throughput of the running GPU (mfgb_pipe_rate): FP64 FMA,
+FP32 FMA, FP64 tensor-core MMA (m8n8k4) and BF16 tensor-core mma.sync, in
+FLOP/s.  These rates decide the operator kernels' arithmetic: FP64-accurate
+applies run as float pairs on the FP32 pipes because the FP64 pipes, scalar
+and tensor, are far slower on this part.
+
+    python -m benchmarks_gb300.rates [--iters 4096] [--reps 5]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+
+from . import _abi
+from ._abi import lib
+
+PIPES = {"fp64_fma": 0, "fp32_fma": 1, "fp64_mma_m8n8k4": 2, "bf16_mma_m16n8k16": 3}
+
+
+def pipe_rates(iters=4096, reps=5):
+    out = {}
+    for name, code in PIPES.items():
+        r = ctypes.c_double()
+        _abi.check(lib().mfgb_pipe_rate(code, iters, reps, ctypes.byref(r)))
+        out[name] = r.value
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m benchmarks_gb300.rates")
+    ap.add_argument("--iters", type=int, default=4096)
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args(argv)
+    r = pipe_rates(a.iters, a.reps)
+    print(json.dumps({k: v / 1e12 for k, v in r.items()} | {"unit": "TFLOP/s"}))
+
+
+if __name__ == "__main__":
+    main()

@@ -29,10 +29,24 @@ enum {
   MFGB_ERR_TIMEOUT = 4,
   MFGB_ERR_NONFINITE = 5,
   MFGB_ERR_CUDA = 6,
-  MFGB_ERR_UNSUPPORTED = 7
+  MFGB_ERR_UNSUPPORTED = 7,
+  /* an input outside the range the double-float kernels without per-cell
+     scaling carry at FP64 accuracy: the largest magnitude of a vector, or of a
+     cell's geometric factors, outside [2^-40, 2^55] (use MFGB_ARITH_FP64) */
+  MFGB_ERR_RANGE = 8
 };
 
-/* Arithmetic used inside the operator kernels (vectors stay FP64). */
+/* Arithmetic used inside the operator kernels (vectors stay FP64).
+   MFGB_ARITH_FP64_DF computes with float pairs on the FP32 pipes (48
+   significant bits; 1e-12 relative against FP64 on the operator).  On GLL
+   collocation operators (shapes 5 / 6 of the kernel shape table, the default
+   from p = 3) every cell is scaled by a power of two, so any FP64 input range
+   is carried.  Elsewhere (Gauss and BP3 forms, BK6, the kernel seams, shapes
+   0-4) inputs must lie in the window of MFGB_ERR_RANGE: the operator's own
+   geometric factors are checked when their pairs are built (the call returns
+   MFGB_ERR_RANGE), caller-supplied G and vectors of the seams on every call,
+   and the source vectors of operator applications on the device (reported by
+   mfgb_check_device_errors, which the solvers call). */
 enum {
   MFGB_ARITH_FP64 = 0,    /* native FP64 (DFMA) */
   MFGB_ARITH_FP64_DF = 1, /* FP64-accurate double-float on the FP32 pipes */
@@ -83,7 +97,9 @@ mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape);
 mfgb_status mfgb_get_kernel_shape(int arith, int degree, int *shape);
 
 /* Reads and clears the device error word: MFGB_ERR_TIMEOUT if a kernel gave
-   up on a bulk-copy wait since the last check (its results are invalid). */
+   up on a bulk-copy wait since the last check (its results are invalid),
+   MFGB_ERR_RANGE if a double-float application without per-cell scaling was
+   given a source vector outside its range. */
 mfgb_status mfgb_check_device_errors(void *stream);
 
 const char *mfgb_status_string(mfgb_status s);
@@ -345,6 +361,16 @@ mfgb_status mfgb_mlp_train(float *d_params, const float *d_X, const float *d_t, 
 mfgb_status mfgb_mlp_forward_f32(const float *d_params, const float *d_X, int n, float *d_y);
 mfgb_status mfgb_mlp_infer(const float *d_params, const float *d_X, int64_t n, double *d_y,
                            void *stream);
+
+/* ---- arithmetic-pipe throughput (no counterpart in the reference) --------
+ * Floating-point operations per second of one arithmetic pipe on the current
+ * GPU, from independent register-only chains on 8 CTAs of 256 threads per SM:
+ * pipe 0 FP64 FMA, 1 FP32 FMA, 2 FP64 tensor-core MMA (mma.sync m8n8k4 f64, the
+ * instruction of sum_factorization/include/kernels/BK1/cuda_mma_kernels.cuh:94-100),
+ * 3 BF16 tensor-core mma.sync m16n8k16 with FP32 accumulation.  An FMA counts 2,
+ * an m x n x k MMA 2 m n k.  The operator kernels' choice of arithmetic rests on
+ * these rates. */
+mfgb_status mfgb_pipe_rate(int pipe, int iters, int reps, double *ops_per_s);
 
 /* ---- vector kernels used by the solver (exposed for tests) -------------- */
 /* result[0] = sum a_i b_i (deterministic two-stage reduction) */

@@ -70,18 +70,21 @@ def test_kernel_shape_table_round_trip_without_gpu(libmfgb):
     from benchmarks_gb300 import _abi, autotune
     L = mf.lib()
     assert tuple(autotune.SHAPES) == (0, 1, 2, 3, 4)
+    assert tuple(autotune.shapes_for(1)) == (0, 1, 2, 3, 4, 5, 6)  # + offset accumulation
     for arith in autotune.ARITHS.values():
         for degree in range(1, 9):
             old = ctypes.c_int()
             assert L.mfgb_get_kernel_shape(arith, degree, ctypes.byref(old)) == _abi.OK
-            assert old.value in autotune.SHAPES
-            for shape in autotune.SHAPES:
+            assert old.value in autotune.shapes_for(arith)
+            for shape in autotune.shapes_for(arith):
                 assert L.mfgb_set_kernel_shape(arith, degree, shape) == _abi.OK
                 got = ctypes.c_int()
                 assert L.mfgb_get_kernel_shape(arith, degree, ctypes.byref(got)) == _abi.OK
                 assert got.value == shape
             assert L.mfgb_set_kernel_shape(arith, degree, old.value) == _abi.OK
-    assert L.mfgb_set_kernel_shape(1, 4, 5) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_set_kernel_shape(1, 4, 7) == _abi.ERR_INVALID_ARG
+    assert L.mfgb_set_kernel_shape(0, 4, 5) == _abi.ERR_INVALID_ARG  # double-float only
+    assert L.mfgb_set_kernel_shape(2, 4, 5) == _abi.ERR_INVALID_ARG
     assert L.mfgb_set_kernel_shape(1, 9, 0) == _abi.ERR_INVALID_ARG
     assert L.mfgb_set_kernel_shape(3, 4, 0) == _abi.ERR_INVALID_ARG
     assert L.mfgb_set_host_pipeline(65) == _abi.ERR_INVALID_ARG

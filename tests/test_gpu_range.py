@@ -1,0 +1,120 @@
+"""Range of the FP64-accurate double-float arithmetic (MFGB_ARITH_FP64_DF).
+
+* GLL collocation operators scale every cell by a power of two: source vectors
+  and geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
+  oracle result to the operator's 1e-12 bar.
+* The double-float kernels without per-cell scaling (the Gauss form here, the
+  E-vector seam) take inputs whose largest magnitude lies in [2^-40, 2^55]:
+  inside it they meet 1e-12, outside it they report MFGB_ERR_RANGE (the seam on
+  the call, an operator application through the device error word).
+* A NaN in the right-hand side ends conjugate gradients with MFGB_ERR_NONFINITE.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def mf():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import benchmarks_gb300 as mf
+    mf.lib()
+    return mf
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def cuda(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.fixture(scope="module")
+def box(orc):
+    ref = orc.BoxProblem(4, 3, 3, 4, amplitude=0.1)
+    src = np.random.default_rng(11).uniform(-1, 1, ref.n_dofs)
+    return ref, src, ref.apply(src)
+
+
+@pytest.mark.parametrize("scale", [2.0 ** -100, 1e-30, 1e30, 2.0 ** 300])
+def test_gll_df_carries_any_source_scale(mf, box, scale):
+    ref, src, want = box
+    A = mf.LaplaceOperator(mf.BoxMesh(4, 3, 3, degree=4, amplitude=0.1))
+    y = A.initialize_dof_vector()
+    A.vmult(y, cuda(src * scale), arith="df")
+    mf.check_device_errors()
+    assert rel(y.cpu().numpy(), want * scale) <= TOL
+
+
+@pytest.mark.parametrize("gscale", [2.0 ** -100, 1e-30, 1e30])
+def test_gll_df_carries_any_geometry_scale(mf, box, gscale):
+    ref, src, want = box
+    A = mf.LaplaceOperator(degree=4, n_dofs=ref.n_dofs, dof_map=ref.map, G=ref.G * gscale,
+                           constrained=ref.constrained)
+    y = A.initialize_dof_vector()
+    for sscale in (1.0, 1e-30):
+        A.vmult(y, cuda(src * sscale), arith="df")
+        mf.check_device_errors()
+        want_s = want * gscale * sscale
+        want_s[ref.constrained] = src[ref.constrained] * sscale  # identity rows are not scaled by G
+        assert rel(y.cpu().numpy(), want_s) <= TOL
+
+
+def test_gauss_df_range_window(mf, orc):
+    from benchmarks_gb300 import MfgbError, _abi
+    ref = orc.GaussProblem(3, 3, 2, 3, amplitude=0.05)
+    A = mf.LaplaceOperator(mf.BoxMesh(3, 3, 2, degree=3, amplitude=0.05), quadrature="gauss")
+    src = np.random.default_rng(5).uniform(-1, 1, ref.n_dofs)
+    y = A.initialize_dof_vector()
+    for scale in (2.0 ** -30, 2.0 ** 40):  # inside the window
+        A.vmult(y, cuda(src * scale), arith="df")
+        mf.check_device_errors()
+        assert rel(y.cpu().numpy(), ref.apply(src) * scale) <= TOL
+    for scale in (2.0 ** -100, 1e-30, 2.0 ** 300):  # outside: reported, not silent
+        A.vmult(y, cuda(src * scale), arith="df")
+        with pytest.raises(MfgbError) as e:
+            mf.check_device_errors()
+        assert e.value.status == _abi.ERR_RANGE
+    mf.check_device_errors()  # the word was cleared
+    A.vmult(y, cuda(src * 1e-30), arith="fp64")  # native FP64 has no window
+    mf.check_device_errors()
+    assert rel(y.cpu().numpy(), ref.apply(src) * 1e-30) <= TOL
+
+
+def test_evector_seam_df_range_is_reported_on_the_call(mf, orc):
+    from benchmarks_gb300 import MfgbError, _abi
+    import torch
+    p, nelmt = 3, 20
+    nq = p + 1
+    rng = np.random.default_rng(2)
+    x, _ = orc.gll(nq)
+    D = orc.derivative_matrix(x).reshape(-1)
+    G = rng.uniform(0.1, 1, nelmt * 6 * nq ** 3)
+    u = rng.uniform(-1, 1, nelmt * nq ** 3)
+    out = torch.zeros(nelmt * nq ** 3, dtype=torch.float64, device="cuda")
+    mf.bk5_evector(p, cuda(D), cuda(G * 2.0 ** -30), cuda(u), out, arith="df")
+    assert rel(out.cpu().numpy(), orc.evector(nq, D, G, u) * 2.0 ** -30) <= TOL
+    for g, v in ((G * 1e-30, u), (G, u * 2.0 ** 100), (G * 1e30, u)):
+        with pytest.raises(MfgbError) as e:
+            mf.bk5_evector(p, cuda(D), cuda(g), cuda(v), out, arith="df")
+        assert e.value.status == _abi.ERR_RANGE
+
+
+@pytest.mark.parametrize("arith", ["df", "fp64"])
+def test_nan_in_rhs_is_nonfinite(mf, arith):
+    from benchmarks_gb300 import MfgbError, _abi
+    A = mf.LaplaceOperator(mf.BoxMesh(4, 4, 4, degree=3, amplitude=0.05))
+    b = A.rhs_uniform(3)
+    b[A.m() // 2] = float("nan")
+    x = A.initialize_dof_vector()
+    ctl = mf.ReductionControl(100, 1e-300, 1e-8)
+    with pytest.raises(MfgbError) as e:
+        mf.SolverCG(ctl).solve(A, x, b, A.get_matrix_diagonal_inverse(), arith=arith)
+    assert e.value.status == _abi.ERR_NONFINITE

@@ -59,6 +59,40 @@ def test_noalloc_cg_matches_allocating_cg(mf, arith):
     assert np.linalg.norm(x - x_ref) <= 1e-7 * np.linalg.norm(x_ref)
 
 
+@pytest.mark.parametrize("arith", ["df", "fp64"])
+def test_noalloc_cg_first_on_a_fresh_operator(mf, orc, arith):
+    """No allocating call has built the operator's double-float copy of G, so a
+    double-float solve splits the FP64 factors on load.  Checked against the
+    oracle's CG (same iteration count, solution to 1e-7), on two calls in a
+    row; the second call leaves the device's free memory unchanged (the first
+    may still load kernels)."""
+    import torch
+    mesh = mf.BoxMesh(9, 8, 7, degree=3, amplitude=0.05)
+    ref = orc.BoxProblem(9, 8, 7, 3, amplitude=0.05)
+    A = mf.LaplaceOperator(mesh)  # geometry only: no split copy of G yet
+    inv_h = orc.invert_diagonal(ref.diagonal())
+    inv = torch.from_numpy(inv_h).cuda()
+    from benchmarks_gb300 import _abi
+    for k, seed in enumerate((4, 5)):
+        b = A.rhs_uniform(seed)
+        x_ref, info = ref.cg(b.cpu().numpy(), diag_inv=inv_h, reduce=1e-10, max_steps=100000)
+        x = A.initialize_dof_vector()
+        ctl = _abi.CgControl(100000, 1e-300, 1e-10, mf._arith(arith))
+        sinfo = _abi.SolveInfo()
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        _abi.check(mf.lib().mfgb_cg_solve_noalloc(
+            A.handle, ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(x.data_ptr()),
+            ctypes.c_void_p(inv.data_ptr()), ctypes.byref(ctl), ctypes.byref(sinfo),
+            mf._stream_ptr()))
+        torch.cuda.synchronize()
+        if k == 1:
+            assert torch.cuda.mem_get_info()[0] == free0
+        assert sinfo.steps == info["steps"]
+        xs = x.cpu().numpy()
+        assert np.linalg.norm(xs - x_ref) <= 1e-7 * np.linalg.norm(x_ref)
+
+
 def test_noalloc_cg_rejects_too_large(mf):
     from benchmarks_gb300 import MfgbError
     A = mf.LaplaceOperator(mf.BoxMesh(26, 26, 26, degree=4))
