@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <random>
 #include <string>
@@ -23,9 +24,20 @@ mfgb_status cuda_status(cudaError_t e, const char *what) {
   return e == cudaErrorMemoryAllocation ? MFGB_ERR_OUT_OF_MEMORY : MFGB_ERR_CUDA;
 }
 
+// Test hook (mfgb_test_fail_allocation): the n-th device allocation from the
+// call on fails as if the device were out of memory; 0 = off.
+static std::atomic<int> g_alloc_countdown{0};
+
+bool alloc_hook_fails(const char *what) {
+  if (g_alloc_countdown.load() <= 0 || g_alloc_countdown.fetch_sub(1) != 1) return false;
+  set_error(std::string(what) + ": allocation failed (injected by mfgb_test_fail_allocation)");
+  return true;
+}
+
 static mfgb_status dev_alloc(void **p, size_t bytes, const char *what) {
   *p = nullptr;
   if (bytes == 0) return MFGB_OK;
+  if (alloc_hook_fails(what)) return MFGB_ERR_OUT_OF_MEMORY;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes > free_b) {
     set_error(std::string(what) + ": needs " + std::to_string(bytes) + " bytes, " +
@@ -51,17 +63,26 @@ mfgb_status ensure_df(mfgb_operator *op) {
     st = range_check_sync(0, nullptr, op->n_cells, op->n * op->n * op->n, op->d_JxW, nullptr,
                           "double-float operator (mass term)");
   if (st) return st;
+  // all or nothing: a failed step frees what this call allocated
+  auto undo = [&](mfgb_status e) {
+    cudaFree(op->d_Gdf);
+    cudaFree(op->d_JxWdf);
+    op->d_Gdf = nullptr;
+    op->d_JxWdf = nullptr;
+    return e;
+  };
   st = dev_alloc((void **)&op->d_Gdf, sizeof(float2) * ng, "G (double-float)");
-  if (st) return st;
+  if (st) return undo(st);
   st = cuda_status(g_to_df(ng, op->d_G, op->d_Gdf, nullptr), "G -> double-float");
-  if (st) return st;
-  if (op->d_JxW && !op->d_JxWdf) {
+  if (st) return undo(st);
+  if (op->d_JxW) {
     const int64_t nw = op->n_cells * (int64_t)op->n * op->n * op->n;
     if ((st = dev_alloc((void **)&op->d_JxWdf, sizeof(float2) * nw, "JxW (double-float)")) ||
         (st = cuda_status(g_to_df(nw, op->d_JxW, op->d_JxWdf, nullptr), "JxW -> double-float")))
-      return st;
+      return undo(st);
   }
-  return cuda_status(cudaDeviceSynchronize(), "G -> double-float");
+  if ((st = cuda_status(cudaDeviceSynchronize(), "G -> double-float"))) return undo(st);
+  return MFGB_OK;
 }
 
 mfgb_status ensure_fx(mfgb_operator *op) {
@@ -71,12 +92,18 @@ mfgb_status ensure_fx(mfgb_operator *op) {
   if ((st = dev_alloc((void **)&op->d_Gfx, sizeof(float2) * op->n_cells * 6 * n3,
                       "G (scaled double-float)")) ||
       (st = dev_alloc((void **)&op->d_Gexp, sizeof(int) * std::max<int64_t>(1, op->n_cells),
-                      "G exponent offsets")))
+                      "G exponent offsets")) ||
+      (st = cuda_status(g_to_fx(op->n_cells, (int)(6 * n3), op->d_G, op->d_Gfx, op->d_Gexp, nullptr),
+                        "G -> scaled double-float")) ||
+      (st = cuda_status(cudaDeviceSynchronize(), "G -> scaled double-float"))) {
+    // all or nothing: the pair of arrays exists only complete
+    cudaFree(op->d_Gfx);
+    cudaFree(op->d_Gexp);
+    op->d_Gfx = nullptr;
+    op->d_Gexp = nullptr;
     return st;
-  if ((st = cuda_status(g_to_fx(op->n_cells, (int)(6 * n3), op->d_G, op->d_Gfx, op->d_Gexp, nullptr),
-                        "G -> scaled double-float")))
-    return st;
-  return cuda_status(cudaDeviceSynchronize(), "G -> scaled double-float");
+  }
+  return MFGB_OK;
 }
 
 mfgb_status ensure_arith(mfgb_operator *op, int arith) {
@@ -150,7 +177,7 @@ mfgb_status vmult_impl(mfgb_operator *op, double *dst, const double *src, int ar
 // shape per degree measured on a GB300 at ~3e7 DoFs (autotune.py re-measures).
 static int g_shape[3][10] = {
     {0, 0, 4, 3, 2, 4, 2, 1, 2, 1},  // FP64
-    {2, 2, 5, 5, 5, 5, 5, 5, 5, 5},  // double-float
+    {2, 2, 6, 6, 6, 5, 6, 6, 5, 5},  // double-float (5, 6: offset accumulation)
     {0, 0, 3, 3, 0, 3, 2, 4, 4, 2},  // FP32
 };
 
@@ -396,6 +423,15 @@ mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape) {
     return MFGB_ERR_INVALID_ARG;
   }
   g_shape[arith][degree + 1] = shape;
+  return MFGB_OK;
+}
+
+mfgb_status mfgb_test_fail_allocation(int n) {
+  if (n < 0) {
+    set_error("mfgb_test_fail_allocation: n must be >= 0");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  g_alloc_countdown.store(n);
   return MFGB_OK;
 }
 

@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
 
   const TmaTiles<N, E, A> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
   auto fail = [&](uint32_t pg, uint32_t pm) {
-    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    if (tid == 0 && err_flag) atomicOr(err_flag, 1);
     mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
     mbar_wait(mbar_m, pm);
   };
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
     }
     if (has_next) {
       const bool okm = mbar_wait(mbar_m, ph_m);
-      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+      if (!okm && err_flag) atomicOr(err_flag, 1);  // the launch's result is void
       ph_m ^= 1u;
       if (okm) T.gather(next, el, jk, idx, raw);
       else
@@ -841,7 +841,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
 
   const TmaTiles<N, E, A> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
   auto fail = [&](uint32_t pg, uint32_t pm) {
-    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    if (tid == 0 && err_flag) atomicOr(err_flag, 1);
     mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
     mbar_wait(mbar_m, pm);
   };
@@ -959,7 +959,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
     for (int i = 0; i < N; ++i) cur[i] = idx[i];
     if (has_next) {
       const bool okm = mbar_wait(mbar_m, ph_m);
-      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+      if (!okm && err_flag) atomicOr(err_flag, 1);  // the launch's result is void
       ph_m ^= 1u;
       if (okm) T.gather(next, el, jk, idx, raw);
       else
@@ -1194,7 +1194,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
       raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + (size_t)NC * idx[i] + c) : VT(0);
   };
   auto fail = [&](uint32_t pg, uint32_t pm) {
-    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    if (tid == 0 && err_flag) atomicOr(err_flag, 1);
     mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
     mbar_wait(mbar_m, pm);
   };
@@ -1286,7 +1286,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
         gather(idx, c + 1, raw);
       } else if (has_next) {
         const bool okm = mbar_wait(mbar_m, ph_m);
-        if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+        if (!okm && err_flag) atomicOr(err_flag, 1);  // the launch's result is void
         ph_m ^= 1u;
         if (okm) {
           indices(next, nidx);

@@ -2,6 +2,7 @@
 // (mfgb_bk5fx.cuh): its launcher, and the set-up of the per-cell scaled
 // geometric factors it reads.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "mfgb_bk5fx.cuh"
@@ -19,6 +20,15 @@ template <int N> struct FxAltMinBlocks {
   static constexpr int value = AltMinBlocks<N, FxAltElems<N>::value, ArithDF>::value;
 };
 
+// test hook: applications left whose first copy wait is made to run out
+static std::atomic<int> g_expire{0};
+
+static bool take_expire() {
+  for (int c = g_expire.load(); c > 0; c = g_expire.load())
+    if (g_expire.compare_exchange_weak(c, c - 1)) return true;
+  return false;
+}
+
 template <int N, int E, int MB, bool MT>
 static cudaError_t fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
                              const double *src, double *dst, const BasisFX<N> &b, cudaStream_t s,
@@ -32,6 +42,21 @@ static cudaError_t fx_launch(int64_t n_cells, const uint32_t *map, const float2 
   if (n_cells <= 0) return cudaSuccess;
   bk5fx_tma_kernel<N, E, MB, MT><<<grid, E * N * N, smem, s>>>(n_cells, map, G, gexp, src, dst, b,
                                                                 done, device_error_flag());
+  return cudaGetLastError();
+}
+
+// one application with the copy-wait test hook (the default cells per CTA)
+template <int N>
+static cudaError_t fx_launch_expire(int64_t n_cells, const uint32_t *map, const float2 *G,
+                                    const int *gexp, const double *src, double *dst,
+                                    const BasisFX<N> &b, cudaStream_t s, const int *done) {
+  constexpr int E = FxElems<N>::value, MB = FxMinBlocks<N>::value;
+  constexpr size_t smem = TmaLayout<N, E, ArithDF>::total;
+  ctas_per_sm(bk5fx_tma_kernel<N, E, MB, false, true>, E * N * N, smem);  // sets the smem limit
+  const int64_t nb = (n_cells + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)num_sms()));
+  bk5fx_tma_kernel<N, E, MB, false, true><<<grid, E * N * N, smem, s>>>(
+      n_cells, map, G, gexp, src, dst, b, done, device_error_flag());
   return cudaGetLastError();
 }
 
@@ -60,6 +85,7 @@ static cudaError_t fx_with_basis(int64_t n_cells, const uint32_t *map, const flo
   const bool alt = kernel_shape(ArithClass<ArithDF>::value, N) == SHAPE_FX_ALT;
   constexpr int E = FxElems<N>::value, MB = FxMinBlocks<N>::value;
   constexpr int EA = FxAltElems<N>::value, MBA = FxAltMinBlocks<N>::value;
+  if (take_expire()) return fx_launch_expire<N>(n_cells, map, G, gexp, src, dst, b, s, done);
   if (alt)
     return mt ? fx_launch<N, EA, MBA, true>(n_cells, map, G, gexp, src, dst, b, s, done)
               : fx_launch<N, EA, MBA, false>(n_cells, map, G, gexp, src, dst, b, s, done);
@@ -119,3 +145,12 @@ cudaError_t g_to_fx(int64_t n_cells, int per_cell, const double *G, float2 *Gfx,
 }
 
 }  // namespace mfgb
+
+extern "C" mfgb_status mfgb_test_expire_copy_wait(int n) {
+  if (n < 0) {
+    mfgb::set_error("mfgb_test_expire_copy_wait: n must be >= 0");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  mfgb::g_expire.store(n);
+  return MFGB_OK;
+}

@@ -139,7 +139,9 @@ __device__ __forceinline__ int fx_offset(int emax) { return emax > 0 ? emax - 10
 // transpose + atomic scatter of batch b runs.  MAPTMA = false loads the dof map
 // with plain loads (a map array that is not 16-byte aligned).  gexp[cell] is
 // the per-cell exponent offset of the scaled G.
-template <int N, int E, int MB, bool MAPTMA>
+// EXPIRE (test hook): the first G copy is armed but not issued, and every wait
+// gives up after 1 ms, so the timeout path runs with no copy in flight.
+template <int N, int E, int MB, bool MAPTMA, bool EXPIRE = false>
 __global__ void __launch_bounds__(E * N * N, MB)
     bk5fx_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
                      const float2 *__restrict__ G, const int *__restrict__ gexp,
@@ -158,8 +160,6 @@ __global__ void __launch_bounds__(E * N * N, MB)
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
   uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
   __shared__ int s_emax[2][E];
-  // per cell: max |v_s(i, ., k)| at [i][k] and max |v_t(i, j, .)| at [i][j] (float bits)
-  __shared__ int s_ms[E][N2], s_mt[E][N2];
 
   const int tid = threadIdx.x;
   const int el = tid / N2;
@@ -187,10 +187,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
 
   TmaTiles<N, E, ArithDF> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
   T.map_ok = MAPTMA;
+  constexpr uint64_t wlim = EXPIRE ? 1000000ull : MFGB_WAIT_LIMIT_NS;
   auto fail = [&](uint32_t pg, uint32_t pm) {
-    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
-    mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
-    mbar_wait(mbar_m, pm);
+    if (tid == 0 && err_flag) atomicOr(err_flag, 1);
+    mbar_wait(mbar_g, pg, wlim);  // bounded waits for copies still in flight
+    mbar_wait(mbar_m, pm, wlim);
   };
 
   if (tid < 2 * E) (&s_emax[0][0])[tid] = 0;
@@ -201,7 +202,10 @@ __global__ void __launch_bounds__(E * N * N, MB)
   }
   __syncthreads();
   if (tid == 0) {
-    T.issue_g(batch);
+    if (EXPIRE)
+      mbar_arrive_expect_tx(mbar_g, 16u);
+    else
+      T.issue_g(batch);
     T.issue_map(batch);
   }
   uint32_t ph_g = 0, ph_m = 0;
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
     if (em) atomicMax(&s_emax[slot][el], em);
   };
   {
-    const bool ok = mbar_wait(mbar_m, ph_m);
+    const bool ok = mbar_wait(mbar_m, ph_m, wlim);
     if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
     ph_m ^= 1u;
     T.gather(batch, el, jk, idx, raw);
@@ -228,12 +232,10 @@ __global__ void __launch_bounds__(E * N * N, MB)
     const int slot = it & 1;
     const int64_t next = batch + gridDim.x;
     const bool has_next = next < n_batches;
-    const bool okg = mbar_wait(mbar_g, ph_g);
+    const bool okg = mbar_wait(mbar_g, ph_g, wlim);
     if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
     ph_g ^= 1u;
     T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase by barrier B
-    s_ms[el][jk] = 0;  // read by the previous batch's transpose before barrier A
-    s_mt[el][jk] = 0;
     const int su = fx_offset(s_emax[slot][el]);
     const int sc = su + ge;  // the cell's result scale
     df u[N];
@@ -296,11 +298,8 @@ __global__ void __launch_bounds__(E * N * N, MB)
       fx_fma(bt, gst.x, gst.y, qs.hi, qs.lo);
       fx_fma(bt, gtt.x, gtt.y, qt.hi, qt.lo);
       vr[i] = fx_finish(br, Cr);
-      const df vs = fx_finish(bs, Cs), vt = fx_finish(bt, Ct);
-      s_vs[el * N3 + i * N2 + jk] = vs;
-      s_vt[el * N3 + i * N2 + jk] = vt;
-      atomicMax(&s_ms[el][i * N + k], __float_as_int(fabsf(vs.hi)));
-      atomicMax(&s_mt[el][i * N + j], __float_as_int(fabsf(vt.hi)));
+      s_vs[el * N3 + i * N2 + jk] = fx_finish(bs, Cs);
+      s_vt[el * N3 + i * N2 + jk] = fx_finish(bt, Ct);
     }
     __syncthreads();  // barrier C: G tile consumed, s_vs / s_vt ready
     if (tid == 0 && has_next) {
@@ -313,8 +312,8 @@ __global__ void __launch_bounds__(E * N * N, MB)
 #pragma unroll
     for (int i = 0; i < N; ++i) cur[i] = idx[i];
     if (has_next) {
-      const bool okm = mbar_wait(mbar_m, ph_m);
-      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+      const bool okm = mbar_wait(mbar_m, ph_m, wlim);
+      if (!okm && err_flag) atomicOr(err_flag, 1);  // the launch's result is void
       ph_m ^= 1u;
       if (okm) {
         T.gather(next, el, jk, idx, raw);
@@ -325,68 +324,36 @@ __global__ void __launch_bounds__(E * N * N, MB)
       ge = el < T.cells_of(next) ? __ldg(gexp + next * E + el) : 0;
     }
 
-    // ---- transpose: y = sum_m D[m][i] v_r(m,j,k) + D[m][j] v_s(i,m,k) + D[m][k] v_t(i,j,m),
-    // the thread's N outputs accumulated together (N independent chains); the
-    // bound of output i: max |v_r| of the own column and the s- and t-line maxima
-    // the metric phase reduced into s_ms / s_mt
+    // ---- transpose: y = sum_m D[m][i] v_r(m,j,k) + D[m][j] v_s(i,m,k) + D[m][k] v_t(i,j,m);
+    // the bound of output i: max |v_r| of the own column and the maxima of the
+    // s- and t-lines it reads
     float mr = 0.f;
 #pragma unroll
     for (int m = 0; m < N; ++m) mr = fmaxf(mr, fabsf(vr[m].hi));
-    if constexpr (N <= 5) {
-      fxacc a[N];
-      float C[N];
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        const float ms = __int_as_float(s_ms[el][i * N + k]);
-        const float mt = __int_as_float(s_mt[el][i * N + j]);
-        C[i] = __fmaf_rn(mt, cik, __fmaf_rn(ms, cij, mr * basis.ci[i]));
-        fx_first(a[i], basis.Dh[i], basis.Dl[i], vr[0].hi, vr[0].lo, C[i]);
-      }
+    for (int i = 0; i < N; ++i) {
+      df ls[N], lt[N];
+      float ms = 0.f, mt = 0.f;
 #pragma unroll
       for (int m = 0; m < N; ++m) {
-        if (m > 0) {
-#pragma unroll
-          for (int i = 0; i < N; ++i)
-            fx_fma(a[i], basis.Dh[m * N + i], basis.Dl[m * N + i], vr[m].hi, vr[m].lo);
-        }
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-          const df ls = s_vs[el * N3 + i * N2 + m * N + k];
-          fx_fma(a[i], Dtjh[m], Dtjl[m], ls.hi, ls.lo);
-        }
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-          const df lt = s_vt[el * N3 + i * N2 + j * N + m];
-          fx_fma(a[i], Dtkh[m], Dtkl[m], lt.hi, lt.lo);
-        }
+        ls[m] = s_vs[el * N3 + i * N2 + m * N + k];
+        lt[m] = s_vt[el * N3 + i * N2 + j * N + m];
+        ms = fmaxf(ms, fabsf(ls[m].hi));
+        mt = fmaxf(mt, fabsf(lt[m].hi));
       }
+      const float C = __fmaf_rn(mt, cik, __fmaf_rn(ms, cij, mr * basis.ci[i]));
+      fxacc a;
+      fx_first(a, basis.Dh[i], basis.Dl[i], vr[0].hi, vr[0].lo, C);
+      fx_fma(a, Dtjh[0], Dtjl[0], ls[0].hi, ls[0].lo);
+      fx_fma(a, Dtkh[0], Dtkl[0], lt[0].hi, lt[0].lo);
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        const df y = fx_finish(a[i], C[i]);
-        if (cur[i] != MFGB_INVALID_DOF)
-          atomicAdd(dst + cur[i], fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
+      for (int m = 1; m < N; ++m) {
+        fx_fma(a, basis.Dh[m * N + i], basis.Dl[m * N + i], vr[m].hi, vr[m].lo);
+        fx_fma(a, Dtjh[m], Dtjl[m], ls[m].hi, ls[m].lo);
+        fx_fma(a, Dtkh[m], Dtkl[m], lt[m].hi, lt[m].lo);
       }
-    } else {
-      // larger N: one output at a time (the N accumulators would not fit)
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        const float ms = __int_as_float(s_ms[el][i * N + k]);
-        const float mt = __int_as_float(s_mt[el][i * N + j]);
-        const float C = __fmaf_rn(mt, cik, __fmaf_rn(ms, cij, mr * basis.ci[i]));
-        fxacc a;
-        fx_first(a, basis.Dh[i], basis.Dl[i], vr[0].hi, vr[0].lo, C);
-#pragma unroll
-        for (int m = 0; m < N; ++m) {
-          if (m > 0) fx_fma(a, basis.Dh[m * N + i], basis.Dl[m * N + i], vr[m].hi, vr[m].lo);
-          const df ls = s_vs[el * N3 + i * N2 + m * N + k];
-          const df lt = s_vt[el * N3 + i * N2 + j * N + m];
-          fx_fma(a, Dtjh[m], Dtjl[m], ls.hi, ls.lo);
-          fx_fma(a, Dtkh[m], Dtkl[m], lt.hi, lt.lo);
-        }
-        const df y = fx_finish(a, C);
-        if (cur[i] != MFGB_INVALID_DOF)
-          atomicAdd(dst + cur[i], fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
-      }
+      const df y = fx_finish(a, C);
+      if (cur[i] != MFGB_INVALID_DOF) atomicAdd(dst + cur[i], fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
     }
     // the prefetched gather's largest exponent per cell, once its loads have
     // landed (read after the next barrier A)

@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
 
   const TmaTilesQ<NM, NQ, E, A> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
   auto fail = [&](uint32_t pg, uint32_t pm) {
-    if (tid == 0 && err_flag) atomicExch(err_flag, 1);
+    if (tid == 0 && err_flag) atomicOr(err_flag, 1);
     mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
     mbar_wait(mbar_m, pm);
   };
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
     for (int i = 0; i < NM; ++i) cur[i] = idx[i];
     if (has_next) {
       const bool okm = mbar_wait(mbar_m, ph_m);
-      if (!okm && err_flag) atomicExch(err_flag, 1);  // the launch's result is void
+      if (!okm && err_flag) atomicOr(err_flag, 1);  // the launch's result is void
       ph_m ^= 1u;
       if (okm) T.gather(next, el, jk, idx, raw, node_col);
       else

@@ -224,6 +224,7 @@ struct DevBuf {
 };
 
 mfgb_status alloc(DevBuf &b, size_t bytes) {
+  if (alloc_hook_fails("cg work vector")) return MFGB_ERR_OUT_OF_MEMORY;
   const cudaError_t e = cudaMalloc(&b.p, bytes);
   if (e == cudaErrorMemoryAllocation) {
     cudaGetLastError();

@@ -45,6 +45,9 @@ struct mfgb_operator {
 namespace mfgb {
 
 void set_error(const std::string &msg);
+// true when the allocation test hook makes this device allocation fail (every
+// device allocation of the library asks first; mfgb_api.cu)
+bool alloc_hook_fails(const char *what);
 mfgb_status cuda_status(cudaError_t e, const char *what);
 
 // 1D bases (host, FP64)

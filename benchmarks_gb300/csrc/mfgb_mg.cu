@@ -186,6 +186,7 @@ namespace mfgb {
 mfgb_status dalloc(void **p, size_t bytes) {
   *p = nullptr;
   if (!bytes) return MFGB_OK;
+  if (alloc_hook_fails("multigrid allocation")) return MFGB_ERR_OUT_OF_MEMORY;
   const cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
     *p = nullptr;

@@ -40,8 +40,8 @@ enum {
    MFGB_ARITH_FP64_DF computes with float pairs on the FP32 pipes (48
    significant bits; 1e-12 relative against FP64 on the operator).  On GLL
    collocation operators (shapes 5 / 6 of the kernel shape table, the default
-   from p = 3) every cell is scaled by a power of two, so any FP64 input range
-   is carried.  Elsewhere (Gauss and BP3 forms, BK6, the kernel seams, shapes
+   at every degree) every cell is scaled by a power of two, so any FP64 input
+   range is carried.  Elsewhere (Gauss and BP3 forms, BK6, the kernel seams, shapes
    0-4) inputs must lie in the window of MFGB_ERR_RANGE: the operator's own
    geometric factors are checked when their pairs are built (the call returns
    MFGB_ERR_RANGE), caller-supplied G and vectors of the seams on every call,
@@ -89,8 +89,10 @@ typedef struct {
    (j,k) column of an element, 1 = one thread per quadrature point, 2 = columns
    with the geometric factors prefetched by bulk TMA copies, 3 / 4 = shapes 0 /
    2 at an alternative number of cells per thread block (the autotuner's
-   elements-per-block choice).  The library starts from a built-in table; the
-   autotuner overrides it.  No
+   elements-per-block choice); for MFGB_ARITH_FP64_DF also 5 / 6 = the
+   offset-accumulation kernel with per-cell scaling at the cells per block of
+   shapes 2 / 4 (GLL operators; elsewhere they run as 2 / 4).  The library
+   starts from a built-in table; the autotuner overrides it.  No
    counterpart in the reference (its launch shape is a compile-time choice,
    CEED_BK/src/BK5/templated_cuda_benchmark.cc:114-124). */
 mfgb_status mfgb_set_kernel_shape(int arith, int degree, int shape);
@@ -101,6 +103,18 @@ mfgb_status mfgb_get_kernel_shape(int arith, int degree, int *shape);
    MFGB_ERR_RANGE if a double-float application without per-cell scaling was
    given a source vector outside its range. */
 mfgb_status mfgb_check_device_errors(void *stream);
+
+/* Test hooks for the failure paths (no counterpart in the reference, whose
+   drivers exit on any error, CEED_BK/src/BK5/templated_cuda_benchmark.cc:9-27).
+   mfgb_test_fail_allocation(n): the n-th device allocation of the library from
+   this call on fails as if the device were out of memory (0 = off).
+   mfgb_test_expire_copy_wait(n): the next n applications of the double-float
+   GLL operator (the offset-accumulation kernel) arm their first geometric-
+   factor copy wait without issuing the copy and give up after 1 ms, so the
+   bounded wait runs out with nothing in flight: the result is void and
+   mfgb_check_device_errors returns MFGB_ERR_TIMEOUT. */
+mfgb_status mfgb_test_fail_allocation(int n);
+mfgb_status mfgb_test_expire_copy_wait(int n);
 
 const char *mfgb_status_string(mfgb_status s);
 const char *mfgb_last_error(void);
