@@ -27,6 +27,11 @@ namespace mfgb {
 template <int N, class A> struct ColumnMinBlocks { static constexpr int value = 0; };
 template <> struct ColumnMinBlocks<5, ArithF32> { static constexpr int value = 5; };
 
+// even-odd form of the in-register contractions (plain arithmetics)
+template <class A> struct EvenOddArith { static constexpr bool value = false; };
+template <> struct EvenOddArith<ArithF64> { static constexpr bool value = true; };
+template <> struct EvenOddArith<ArithF32> { static constexpr bool value = true; };
+
 template <int N, int E, class A, bool EVEC, bool WITH_ENERGY>
 __device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uint32_t *__restrict__ map,
                const typename A::GType *__restrict__ G, const typename A::VecT *__restrict__ src,
@@ -36,6 +41,7 @@ __device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uin
   using V = typename A::V;
   using Acc = typename A::Acc;
   constexpr int N2 = N * N, N3 = N * N * N;
+  constexpr bool kEvenOdd = EvenOddArith<A>::value;
   __shared__ V s_u[E * N3];
   __shared__ V s_vs[E * N3];
   __shared__ V s_vt[E * N3];
@@ -77,22 +83,33 @@ __device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uin
     }
     __syncthreads();
 
-    // ---- reference gradient + metric apply
-    V vr[N];
+    // ---- reference gradient + metric apply; the r-derivative of the own
+    // column first (even-odd form where the basis has it)
+    V vr[N], qrv[N];
+    if (kEvenOdd && basis.eo) {
+      if constexpr (kEvenOdd) even_odd_apply<N, A>(basis.Pg, basis.Qg, u, qrv);
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        Acc ar;
+        A::mul(ar, basis.D[i * N], u[0]);
+#pragma unroll
+        for (int m = 1; m < N; ++m) A::fma(ar, basis.D[i * N + m], u[m]);
+        qrv[i] = A::finish(ar);
+      }
+    }
     const typename A::GType *Gc = G + (valid ? cell : 0) * 6 * N3 + jk;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      Acc ar, as, at;
-      A::mul(ar, basis.D[i * N], u[0]);
+      Acc as, at;
       A::mul(as, Dj[0], s_u[el * N3 + i * N2 + k]);
       A::mul(at, Dk[0], s_u[el * N3 + i * N2 + j * N]);
 #pragma unroll
       for (int m = 1; m < N; ++m) {
-        A::fma(ar, basis.D[i * N + m], u[m]);
         A::fma(as, Dj[m], s_u[el * N3 + i * N2 + m * N + k]);
         A::fma(at, Dk[m], s_u[el * N3 + i * N2 + j * N + m]);
       }
-      const V qr = A::finish(ar), qs = A::finish(as), qt = A::finish(at);
+      const V qr = qrv[i], qs = A::finish(as), qt = A::finish(at);
       const V grr = A::load_g(__ldg(Gc + 0 * N3 + i * N2));
       const V grs = A::load_g(__ldg(Gc + 1 * N3 + i * N2));
       const V grt = A::load_g(__ldg(Gc + 2 * N3 + i * N2));
@@ -109,16 +126,27 @@ __device__ __forceinline__ void bk5_column_body(const int64_t n_cells, const uin
     }
     __syncthreads();
 
-    // ---- integrate (D^T, sum of the three directions) + scatter
+    // ---- integrate (D^T, sum of the three directions) + scatter; the
+    // r-part from the own column first (even-odd form where available)
+    V rv[N];
+    if (kEvenOdd && basis.eo) {
+      if constexpr (kEvenOdd) even_odd_apply<N, A>(basis.Pt, basis.Qt, vr, rv);
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        Acc a;
+        A::mul(a, basis.D[i], vr[0]);
+#pragma unroll
+        for (int m = 1; m < N; ++m) A::fma(a, basis.D[m * N + i], vr[m]);
+        rv[i] = A::finish(a);
+      }
+    }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       Acc a;
-      A::mul(a, basis.D[i], vr[0]);
-      A::fma(a, Dtj[0], s_vs[el * N3 + i * N2 + k]);
-      A::fma(a, Dtk[0], s_vt[el * N3 + i * N2 + j * N]);
+      A::set(a, rv[i]);
 #pragma unroll
-      for (int m = 1; m < N; ++m) {
-        A::fma(a, basis.D[m * N + i], vr[m]);
+      for (int m = 0; m < N; ++m) {
         A::fma(a, Dtj[m], s_vs[el * N3 + i * N2 + m * N + k]);
         A::fma(a, Dtk[m], s_vt[el * N3 + i * N2 + j * N + m]);
       }

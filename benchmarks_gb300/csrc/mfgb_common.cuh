@@ -134,7 +134,8 @@ __device__ __forceinline__ df dfacc_finish(const dfacc &a) {
 // ----------------------------------------------------- arithmetic policies --
 // Every policy defines:
 //   V       value type carried through the contractions
-//   Acc     accumulator type (zero / fma / mul = set to the first product)
+//   Acc     accumulator type (zero / fma / mul = set to the first product /
+//           set = start from a value)
 //   GType   storage type of one geometric-factor component
 //   VecT    L-vector element type
 struct ArithF64 {
@@ -142,6 +143,7 @@ struct ArithF64 {
   using Acc = double;
   using GType = double;
   using VecT = double;
+  static __device__ __forceinline__ void set(Acc &a, V x) { a = x; }
   static __device__ __forceinline__ void zero(Acc &a) { a = 0.0; }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fma_rn(x, y, a); }
   static __device__ __forceinline__ void mul(Acc &a, V x, V y) { a = __dmul_rn(x, y); }
@@ -159,6 +161,7 @@ struct ArithF32 {
   using Acc = float;
   using GType = float;
   using VecT = float;
+  static __device__ __forceinline__ void set(Acc &a, V x) { a = x; }
   static __device__ __forceinline__ void zero(Acc &a) { a = 0.f; }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { a = __fmaf_rn(x, y, a); }
   static __device__ __forceinline__ void mul(Acc &a, V x, V y) { a = __fmul_rn(x, y); }
@@ -176,6 +179,7 @@ struct ArithDF {
   using Acc = dfacc;
   using GType = float2;  // (hi, lo)
   using VecT = double;
+  static __device__ __forceinline__ void set(Acc &a, V x) { a.s = x.hi; a.c = x.lo; }
   static __device__ __forceinline__ void zero(Acc &a) { dfacc_zero(a); }
   static __device__ __forceinline__ void fma(Acc &a, V x, V y) { dfacc_fma(a, x, y); }
   static __device__ __forceinline__ void mul(Acc &a, V x, V y) { dfacc_set(a, x, y); }
@@ -197,9 +201,54 @@ struct ArithDFG64 : ArithDF {
 
 // 1D derivative matrix D[point*N + basis] passed by value (kernel parameter
 // space, i.e. the constant bank), in the value type of the policy.
+// The even-odd tables (used when `eo` is set): the collocation derivative on
+// nodes symmetric about the cell centre satisfies D[N-1-i][N-1-m] = -D[i][m],
+// so y = D x splits into half-size products of the even and odd parts of x,
+//   P[i][m] = (M[i][m] + M[i][N-1-m]) / 2  (m < N/2; column N/2 = M[i][mid] for odd N),
+//   Q[i][m] = (M[i][m] - M[i][N-1-m]) / 2,
+// for the rows i < (N+1)/2 of M = D (Pg, Qg) and of M = D^T (Pt, Qt).
 template <int N, class A>
 struct Basis {
   typename A::V D[N * N];
+  typename A::V Pg[(N + 1) / 2][N / 2 + 1], Qg[(N + 1) / 2][N / 2 + 1];
+  typename A::V Pt[(N + 1) / 2][N / 2 + 1], Qt[(N + 1) / 2][N / 2 + 1];
+  int eo;
 };
+
+// y = M x in even-odd form for M[N-1-i][N-1-m] = -M[i][m] (tables of Basis):
+// with e_m = x_m + x_{N-1-m}, o_m = x_m - x_{N-1-m},
+//   a_i = sum_m P[i][m] e_m (+ P[i][N/2] x_mid),  b_i = sum_m Q[i][m] o_m,
+//   y_i = a_i + b_i,  y_{N-1-i} = b_i - a_i  (y_mid = b_mid: a_mid vanishes),
+// about N^2/2 multiply-adds and 2N additions instead of N^2 multiply-adds.
+// Plain arithmetics only.
+template <int N, class A>
+__device__ __forceinline__ void even_odd_apply(const typename A::V (&P)[(N + 1) / 2][N / 2 + 1],
+                                               const typename A::V (&Q)[(N + 1) / 2][N / 2 + 1],
+                                               const typename A::V (&x)[N], typename A::V (&y)[N]) {
+  using V = typename A::V;
+  constexpr int H = N / 2;
+  V e[H > 0 ? H : 1], o[H > 0 ? H : 1];
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    e[m] = x[m] + x[N - 1 - m];
+    o[m] = x[m] - x[N - 1 - m];
+  }
+#pragma unroll
+  for (int i = 0; i < (N + 1) / 2; ++i) {
+    typename A::Acc a, b;
+    if constexpr (N % 2) A::mul(a, P[i][H], x[H]); else A::zero(a);
+#pragma unroll
+    for (int m = 0; m < H; ++m) A::fma(a, P[i][m], e[m]);
+    A::zero(b);
+#pragma unroll
+    for (int m = 0; m < H; ++m) A::fma(b, Q[i][m], o[m]);
+    if (N % 2 && i == H) {
+      y[i] = A::finish(b);
+    } else {
+      y[i] = A::finish(a) + A::finish(b);
+      y[N - 1 - i] = A::finish(b) - A::finish(a);
+    }
+  }
+}
 
 }  // namespace mfgb

@@ -1,5 +1,8 @@
 // mfgb_dispatch.cuh -- runtime degree dispatch for the BK5 kernels.
 #pragma once
+#include <cmath>
+#include <type_traits>
+
 #include "mfgb_launch.cuh"
 
 namespace mfgb {
@@ -21,12 +24,44 @@ template <> struct BasisValue<ArithDF> {
 };
 template <> struct BasisValue<ArithDFG64> : BasisValue<ArithDF> {};
 
+// Fills the even-odd tables of a basis and sets b.eo when D64 is the
+// derivative of nodes symmetric about the cell centre (D[N-1-i][N-1-m] = -D[i][m]
+// to rounding), for the plain arithmetics; caller-supplied matrices of the
+// kernel seams need not have that symmetry and keep the dense form.
+template <int N, class A>
+void fill_even_odd(Basis<N, A> &b, const double *D64) {
+  b.eo = 0;
+  if constexpr (std::is_same<A, ArithF64>::value || std::is_same<A, ArithF32>::value) {
+    double big = 0.0, asym = 0.0;
+    for (int q = 0; q < N * N; ++q) big = std::max(big, std::fabs(D64[q]));
+    for (int i = 0; i < N; ++i)
+      for (int m = 0; m < N; ++m)
+        asym = std::max(asym, std::fabs(D64[(N - 1 - i) * N + (N - 1 - m)] + D64[i * N + m]));
+    if (asym > 1e-13 * big) return;
+    constexpr int H = N / 2;
+    for (int i = 0; i < (N + 1) / 2; ++i) {
+      for (int m = 0; m < H; ++m) {
+        b.Pg[i][m] = BasisValue<A>::from(0.5 * (D64[i * N + m] + D64[i * N + N - 1 - m]));
+        b.Qg[i][m] = BasisValue<A>::from(0.5 * (D64[i * N + m] - D64[i * N + N - 1 - m]));
+        b.Pt[i][m] = BasisValue<A>::from(0.5 * (D64[m * N + i] + D64[(N - 1 - m) * N + i]));
+        b.Qt[i][m] = BasisValue<A>::from(0.5 * (D64[m * N + i] - D64[(N - 1 - m) * N + i]));
+      }
+      if (N % 2) {
+        b.Pg[i][H] = BasisValue<A>::from(D64[i * N + H]);
+        b.Pt[i][H] = BasisValue<A>::from(D64[H * N + i]);
+      }
+    }
+    b.eo = 1;
+  }
+}
+
 template <int N, class A, bool EVEC, bool EN>
 cudaError_t bk5_with_basis(int64_t n_cells, const uint32_t *map, const typename A::GType *G,
                            const typename A::VecT *src, typename A::VecT *dst, const double *D64,
                            double *partials, int *grid, cudaStream_t s, const int *done) {
-  Basis<N, A> b;
+  Basis<N, A> b{};
   for (int q = 0; q < N * N; ++q) b.D[q] = BasisValue<A>::from(D64[q]);
+  fill_even_odd(b, D64);
   return bk5_launch<N, A, EVEC, EN>(n_cells, map, G, src, dst, b, partials, grid, s, done);
 }
 
@@ -126,7 +161,7 @@ cudaError_t bk6_with_basis(int64_t n_cells, const uint32_t *map, const typename 
                            const typename A::VecT *src, typename A::VecT *dst, const double *D64,
                            cudaStream_t s) {
   constexpr int E = ElemsPerCta<N>::value;
-  Basis<N, A> b;
+  Basis<N, A> b{};
   for (int q = 0; q < N * N; ++q) b.D[q] = BasisValue<A>::from(D64[q]);
   const size_t smem = sizeof(typename A::GType) * E * 6 * N * N * N +
                       3 * sizeof(typename A::V) * E * N * N * N;

@@ -17,6 +17,7 @@
 
 #include "mfgb_common.cuh"
 #include "mfgb_internal.h"
+#include "mfgb_mg_internal.h"
 
 namespace mfgb {
 namespace {
@@ -441,11 +442,110 @@ cudaError_t weighted_diagonal(const mfgb_operator *op, const double *w, double *
   return cudaGetLastError();
 }
 
+// Per-cell squared norms of two vectors over the cell's (unconstrained) DoFs:
+// one 64-thread block per cell at a time, sums added into na / nb.
+__global__ void __launch_bounds__(64)
+    cell_sq_norms_kernel(int64_t n_cells, int n3, const uint32_t *__restrict__ map,
+                         const double *__restrict__ a, const double *__restrict__ b,
+                         double *__restrict__ na, double *__restrict__ nb) {
+  __shared__ double s_a[64], s_b[64];
+  for (int64_t c = blockIdx.x; c < n_cells; c += gridDim.x) {
+    double sa = 0.0, sb = 0.0;
+    for (int l = threadIdx.x; l < n3; l += 64) {
+      const uint32_t d = map[c * n3 + l];
+      if (d != MFGB_INVALID_DOF) {
+        sa = __fma_rn(a[d], a[d], sa);
+        sb = __fma_rn(b[d], b[d], sb);
+      }
+    }
+    s_a[threadIdx.x] = sa;
+    s_b[threadIdx.x] = sb;
+    __syncthreads();
+    for (int o = 32; o > 0; o >>= 1) {
+      if (threadIdx.x < o) {
+        s_a[threadIdx.x] += s_a[threadIdx.x + o];
+        s_b[threadIdx.x] += s_b[threadIdx.x + o];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      na[c] += s_a[0];
+      nb[c] += s_b[0];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void error_propagate_kernel(int64_t n, const double *__restrict__ e,
+                                       const double *__restrict__ z, double *__restrict__ out) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = e[t] - z[t];
+}
+
+__global__ void ratio_sqrt_kernel(int64_t n, const double *__restrict__ before,
+                                  const double *__restrict__ after, double *__restrict__ rho) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    rho[t] = before[t] > 0.0 ? sqrt(after[t] / before[t]) : 0.0;
+}
+
 }  // namespace mfgb
 
 using namespace mfgb;
 
 extern "C" {
+
+// Training data the FP64 multigrid generates for the learned smoother: the
+// per-cell error reduction of one V-cycle, rho_c = |E e|_c / |e|_c with
+// E = I - M A the V-cycle's error propagation, over n_vectors seeded random
+// errors e (U[-1,1] from mt19937_64(seed + k), zero on Dirichlet DoFs); the
+// norms sum the cell's unconstrained DoFs over all vectors.
+mfgb_status mfgb_cell_error_reduction(const mfgb_operator *op, mfgb_mg *mg, int n_vectors,
+                                      uint64_t seed, double *d_rho, void *stream) {
+  if (!op || !mg || op->quadrature || n_vectors < 1 || (op->n_cells > 0 && !d_rho)) {
+    set_error("mfgb_cell_error_reduction: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  if (mg->levels.empty() || mg->levels[0].n != op->n_dofs) {
+    set_error("mfgb_cell_error_reduction: the hierarchy is not the operator's");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  const int64_t n = op->n_dofs, nc = op->n_cells;
+  const int n3 = op->n * op->n * op->n;
+  cudaStream_t s = (cudaStream_t)stream;
+  double *e = nullptr, *w = nullptr, *z = nullptr, *na = nullptr, *nb = nullptr;
+  auto freeall = [&]() {
+    cudaFree(e); cudaFree(w); cudaFree(z); cudaFree(na); cudaFree(nb);
+  };
+  mfgb_status st;
+  if ((st = dalloc((void **)&e, sizeof(double) * n)) || (st = dalloc((void **)&w, sizeof(double) * n)) ||
+      (st = dalloc((void **)&z, sizeof(double) * n)) ||
+      (st = dalloc((void **)&na, sizeof(double) * std::max<int64_t>(nc, 1))) ||
+      (st = dalloc((void **)&nb, sizeof(double) * std::max<int64_t>(nc, 1)))) {
+    freeall();
+    return st;
+  }
+  cudaMemsetAsync(na, 0, sizeof(double) * std::max<int64_t>(nc, 1), s);
+  cudaMemsetAsync(nb, 0, sizeof(double) * std::max<int64_t>(nc, 1), s);
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+  const unsigned gc = (unsigned)std::min<int64_t>(std::max<int64_t>(nc, 1), 152 * 32);
+  for (int k = 0; k < n_vectors && !st; ++k) {
+    if ((st = mfgb_rhs_uniform(op, seed + (uint64_t)k, e, s)) ||
+        (st = mfgb_vmult(op, w, e, MFGB_ARITH_FP64_DF, s)) || (st = mfgb_mg_vmult(mg, z, w, s)))
+      break;
+    error_propagate_kernel<<<g, 256, 0, s>>>(n, e, z, w);
+    if (nc > 0) cell_sq_norms_kernel<<<gc, 64, 0, s>>>(nc, n3, op->d_map, e, w, na, nb);
+    st = cuda_status(cudaGetLastError(), "mfgb_cell_error_reduction");
+  }
+  if (!st && nc > 0) {
+    ratio_sqrt_kernel<<<gc, 256, 0, s>>>(nc, na, nb, d_rho);
+    st = cuda_status(cudaGetLastError(), "mfgb_cell_error_reduction");
+  }
+  if (!st) st = cuda_status(cudaStreamSynchronize(s), "mfgb_cell_error_reduction");
+  freeall();
+  return st;
+}
 
 int mfgb_mlp_n_params(void) { return NP; }
 

@@ -368,6 +368,12 @@ int mfgb_mlp_n_params(void);
 mfgb_status mfgb_cell_features(const mfgb_operator *op, float *d_features, void *stream);
 mfgb_status mfgb_cell_lambda(const mfgb_operator *op, double *d_lambda, int iterations,
                              void *stream);
+/* per-cell error reduction of one V-cycle of mg (the hierarchy of op's mesh),
+   the multigrid's own training data for the smoother weights:
+   rho_c = |E e|_c / |e|_c, E = I - M A, summed over n_vectors seeded random
+   errors (U[-1,1] from mt19937_64(seed + k), 0 on Dirichlet DoFs) */
+mfgb_status mfgb_cell_error_reduction(const mfgb_operator *op, mfgb_mg *mg, int n_vectors,
+                                      uint64_t seed, double *d_rho, void *stream);
 mfgb_status mfgb_mlp_loss_grad(const float *d_params, const float *d_X, const float *d_t, int n,
                                float *h_grad, float *h_loss);
 mfgb_status mfgb_mlp_train(float *d_params, const float *d_X, const float *d_t, int64_t n,
