@@ -138,7 +138,8 @@ def traffic_from_profile(arith: str):
     summary for this workload (None if not captured)."""
     if not is_headline():
         return None
-    path = os.path.join(ROOT, "profiles", f"bk5_{arith}_p4_67M.md")
+    path = os.path.join(ROOT, "profiles", "bk5fx_p4_67M.md" if arith == "df" else
+                        f"bk5_{arith}_p4_67M.md")
     try:
         with open(path) as f:
             for line in f:
