@@ -51,10 +51,13 @@ int main(int argc, char **argv) {
     mfgb::SolverCG cg(control);
     cudaDeviceSynchronize();
     auto t0 = Clock::now();
+    double el_mid = 0.0;
     if (precond == "none") {
       cg.solve(A, x, b, mfgb::PreconditionIdentity());
     } else if (precond == "jacobi") {
       A.compute_diagonal();
+      el_mid = A.el(A.m() / 2, A.m() / 2);  // bp5_kokkos's el(row, row)
+      t0 = Clock::now();
       cg.solve(A, x, b, *A.get_matrix_diagonal_inverse());
     } else if (precond == "helmholtz") {
       mfgb::HelmholtzOperator<3, 4, double> H(box);
@@ -73,6 +76,7 @@ int main(int argc, char **argv) {
     std::printf("%lld %lld %.3e %.3e %.3e %d %.3e\n", (long long)A.n_cells(), (long long)A.m(),
                 best_mv, t_cg, its ? t_cg / its : 0.0, its, red);
     std::printf("GDoF/s %.3f\n", A.m() / best_mv * 1e-9);
+    if (el_mid != 0.0) std::printf("el_mid %.17e\n", el_mid);
     // the host-buffer apply against the device apply (pinned host vectors)
     double *hs = nullptr, *hd = nullptr;
     const size_t bytes = sizeof(double) * A.m();

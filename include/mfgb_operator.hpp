@@ -158,6 +158,19 @@ class LaplaceOperatorBK35 {
   }
   std::shared_ptr<DiagonalMatrix> get_matrix_diagonal_inverse() const { return inverse_diagonal_; }
 
+  // el(row, col) of bp5_kokkos (benchmark.cc:283-292): a diagonal entry, 1 / the
+  // inverse diagonal of compute_diagonal(); only row == col is defined
+  double el(int64_t row, int64_t col) const {
+    if (row != col || row < 0 || row >= n_dofs_)
+      throw std::invalid_argument("el: only diagonal entries inside the matrix");
+    if (!inverse_diagonal_) throw std::logic_error("el: call compute_diagonal() first");
+    double v = 0.0;
+    if (cudaMemcpy(&v, inverse_diagonal_->get_vector().get_values() + row, sizeof(double),
+                   cudaMemcpyDeviceToHost) != cudaSuccess)
+      throw std::runtime_error("el: device read failed");
+    return 1.0 / v;
+  }
+
   const mfgb_operator *handle() const { return op_.get(); }
   int arith() const { return arith_; }
 

@@ -38,8 +38,14 @@ def test_cpp_adapter_matches_python_api(example):
     b = A.rhs_uniform(1)
     x = A.initialize_dof_vector()
     ctl = mf.ReductionControl(1000000, 1e-300, 1e-8)
-    mf.SolverCG(ctl).solve(A, x, b, A.get_matrix_diagonal_inverse())
+    P = A.get_matrix_diagonal_inverse()
+    mf.SolverCG(ctl).solve(A, x, b, P)
     assert its == ctl.last_step() and 0 < red < 1 and mv > 0
+    # el(row, row): the diagonal entry, 1 / the inverse diagonal
+    out = subprocess.run([example, "8", "8", "4", "jacobi", "1e-8"], capture_output=True, text=True,
+                         timeout=600)
+    el = float([l for l in out.stdout.splitlines() if l.startswith("el_mid")][0].split()[1])
+    assert el == pytest.approx(1.0 / float(P.vector[A.m() // 2]), rel=1e-15)
     _, _, _, its_mg, _ = run(example, 8, 8, 4, "mg32", 1e-10)
     assert 0 < its_mg < 30
 
