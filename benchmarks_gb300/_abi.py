@@ -121,6 +121,7 @@ def lib():
         "mfgb_batch_precondition": ([P, P, P, P], I32),
         "mfgb_batch_cg_solve": ([P, P, P, ctypes.POINTER(CgControl), P, P], I32),
         "mfgb_batch_last_solve_stats": ([P, ctypes.POINTER(I32)], I32),
+        "mfgb_batch_last_solve_launches": ([P, ctypes.POINTER(I32)], I32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)

@@ -115,6 +115,8 @@ class BatchSolver:
         r = ctypes.c_int()
         _abi.check(lib().mfgb_batch_last_solve_stats(self._b, ctypes.byref(r)))
         self.replans = r.value
+        _abi.check(lib().mfgb_batch_last_solve_launches(self._b, ctypes.byref(r)))
+        self.launches = r.value
         _abi.check(st)
         return x
 

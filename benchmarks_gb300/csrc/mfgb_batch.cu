@@ -261,20 +261,43 @@ __global__ void __launch_bounds__(T256)
 __global__ void __launch_bounds__(T256)
     kb_sum_check(const int *__restrict__ cbeg, const int *__restrict__ pid,
                  const double *__restrict__ part, BScal *__restrict__ sc, int max_steps,
-                 int *__restrict__ active) {
+                 int *__restrict__ active, const int64_t *__restrict__ pdofs,
+                 unsigned long long *__restrict__ active_dofs) {
   __shared__ double sh[T256 / 32];
   const double rr = problem_sum(cbeg, part, sh);
   if (threadIdx.x == 0) {
-    BScal &q = sc[pid[blockIdx.x]];
+    const int p = pid[blockIdx.x];
+    BScal &q = sc[p];
     if (!q.done) {
       const double res = sqrt(rr);
       q.res = res;
       q.its += 1;
-      if (res <= q.tol_eff) q.done = 1;
-      else if (q.its >= max_steps || isnan(res)) q.done = 2;
-      else atomicAdd(active, 1);
+      if (res <= q.tol_eff) {
+        q.done = 1;
+      } else if (q.its >= max_steps || isnan(res)) {
+        q.done = 2;
+      } else {
+        atomicAdd(active, 1);
+        atomicAdd(active_dofs, (unsigned long long)pdofs[p]);
+      }
     }
   }
+}
+
+__global__ void kb_zero_active(int *active, unsigned long long *active_dofs) {
+  *active = 0;
+  *active_dofs = 0ull;
+}
+
+// the while-loop condition of a launch plan's graph: go on while problems run,
+// they still hold more than `threshold` DoFs (else the host gathers a smaller
+// plan), and the launch has run fewer than max_iter iterations (a hard bound)
+__global__ void kb_continue(cudaGraphConditionalHandle h, const int *active,
+                            const unsigned long long *active_dofs, unsigned long long threshold,
+                            int *iter, int max_iter) {
+  const int it = *iter + 1;
+  *iter = it;
+  cudaGraphSetConditional(h, (*active > 0 && *active_dofs > threshold && it < max_iter) ? 1u : 0u);
 }
 
 // p = z + beta p (beta = rz_new / rz) for running problems
@@ -457,6 +480,12 @@ struct mfgb_batch {
   mfgb::BScal *d_scal = nullptr;
   int *d_active = nullptr;
   int *h_active = nullptr;  // pinned
+  // device-side loop of the solve: DoFs of each problem, DoFs of the running
+  // problems, iterations of the current graph launch
+  int64_t *d_pdofs = nullptr;
+  unsigned long long *d_active_dofs = nullptr;
+  int *d_iter = nullptr;
+  int last_launches = 0;  // graph launches of the last solve
   int last_replans = 0;     // plans gathered during the last solve
 };
 
@@ -476,6 +505,7 @@ void free_batch(mfgb_batch *B) {
   cudaFree(B->d_all); cudaFree(B->d_cbeg); cudaFree(B->d_pid);
   cudaFree(B->r); cudaFree(B->z); cudaFree(B->p); cudaFree(B->v); cudaFree(B->part);
   cudaFree(B->d_scal); cudaFree(B->d_active);
+  cudaFree(B->d_pdofs); cudaFree(B->d_active_dofs); cudaFree(B->d_iter);
   if (B->h_active) cudaFreeHost(B->h_active);
   delete B;
 }
@@ -915,8 +945,13 @@ mfgb_status build_batch(mfgb_batch *B, const mfgb_box_desc *boxes, int n,
         (st = dalloc((void **)&B->v, sizeof(double) * D.n)) ||
         (st = dalloc((void **)&B->part, sizeof(double) * std::max(1, B->n_all))) ||
         (st = dalloc((void **)&B->d_scal, sizeof(BScal) * n)) ||
-        (st = dalloc((void **)&B->d_active, sizeof(int))))
+        (st = dalloc((void **)&B->d_active, sizeof(int))) ||
+        (st = dalloc((void **)&B->d_active_dofs, sizeof(unsigned long long))) ||
+        (st = dalloc((void **)&B->d_iter, sizeof(int))))
       return st;
+    std::vector<int64_t> pd(n, 0);
+    for (const Part &P : D.parts) pd[P.problem] = P.n;
+    if ((st = upload(&B->d_pdofs, pd))) return st;
     if ((st = cuda_status(cudaMallocHost((void **)&B->h_active, sizeof(int)), "pinned flag")))
       return st;
   }
@@ -1204,6 +1239,15 @@ mfgb_status mfgb_batch_last_solve_stats(const mfgb_batch *B, int *n_replans) {
   return MFGB_OK;
 }
 
+mfgb_status mfgb_batch_last_solve_launches(const mfgb_batch *B, int *n_launches) {
+  if (!B || !n_launches) {
+    set_error("mfgb_batch_last_solve_launches: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  *n_launches = B->last_launches;
+  return MFGB_OK;
+}
+
 mfgb_status mfgb_batch_vmult(mfgb_batch *B, double *d_dst, const double *d_src, void *stream) {
   if (!B || !d_dst || !d_src || d_dst == d_src) {
     set_error("mfgb_batch_vmult: invalid argument");
@@ -1264,21 +1308,17 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
   int running = 0;
   for (const BScal &q : hs) running += q.done == 0;
 
-  // one iteration of the plan's problems as a graph
-  auto capture = [&](const Plan &P, cudaGraphExec_t *exec) -> mfgb_status {
-    cudaGraph_t graph = nullptr;
-    mfgb_status e;
-    if ((e = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture")))
-      return e;
+  // one CG iteration of the plan's problems, issued on s (in capture)
+  auto iteration = [&](const Plan &P) -> mfgb_status {
     const int nb = P.n_prob;
     mfgb_status cap = apply64(B, P, B->p, B->v, s);
     if (!cap) {
       kb_dot<<<P.n_all, T256, 0, s>>>(P.d_all, B->p, B->v, B->part);
       kb_sum_pap<<<nb, T256, 0, s>>>(P.d_cbeg, P.d_pid, B->part, B->d_scal);
       kb_update<<<P.n_all, T256, 0, s>>>(P.d_all, d_x, B->r, B->p, B->v, B->d_scal, B->part);
-      cudaMemsetAsync(B->d_active, 0, sizeof(int), s);
+      kb_zero_active<<<1, 1, 0, s>>>(B->d_active, B->d_active_dofs);
       kb_sum_check<<<nb, T256, 0, s>>>(P.d_cbeg, P.d_pid, B->part, B->d_scal, ctl->max_steps,
-                                       B->d_active);
+                                       B->d_active, B->d_pdofs, B->d_active_dofs);
       cap = precondition_b(B, P, B->z, B->r, s);
     }
     if (!cap) {
@@ -1286,8 +1326,66 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
       kb_sum_rz<<<nb, T256, 0, s>>>(P.d_cbeg, P.d_pid, B->part, B->d_scal);
       kb_direction<<<P.n_all, T256, 0, s>>>(P.d_all, B->z, B->p, B->d_scal);
       kb_roll<<<gp, 128, 0, s>>>(np, B->d_scal);
-      cudaMemcpyAsync(B->h_active, B->d_active, sizeof(int), cudaMemcpyDeviceToHost, s);
     }
+    return cap;
+  };
+  // The plan's iterations as one graph: a conditional while node whose body is
+  // one iteration plus the condition kernel (kb_continue), so one launch runs
+  // until every problem is done, the running problems hold at most 75 % of the
+  // plan's DoFs, or max_steps iterations (device-side loop; the host only
+  // gathers new plans).  Where the body cannot be built as a conditional graph
+  // the plan falls back to one graph launch per iteration (*looped = false).
+  auto capture = [&](const Plan &P, cudaGraphExec_t *exec, bool *looped) -> mfgb_status {
+    mfgb_status e;
+    *looped = false;
+    {
+      cudaGraph_t graph = nullptr;
+      cudaGraphConditionalHandle h;
+      cudaGraphNodeParams cp{};
+      cudaGraphNode_t node;
+      bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess &&
+                cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault) ==
+                    cudaSuccess;
+      if (ok) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        ok = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp) == cudaSuccess;
+      }
+      if (ok) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+          mfgb_status cap = iteration(P);
+          const unsigned long long threshold = (unsigned long long)(0.75 * (double)P.dofs);
+          if (!cap)
+            kb_continue<<<1, 1, 0, s>>>(h, B->d_active, B->d_active_dofs, threshold, B->d_iter,
+                                        ctl->max_steps);
+          cudaGraph_t out = nullptr;
+          const cudaError_t ce = cudaStreamEndCapture(s, &out);
+          if (cap) {
+            cudaGraphDestroy(graph);
+            return cap;
+          }
+          ok = ce == cudaSuccess && cudaGraphInstantiate(exec, graph, 0) == cudaSuccess;
+        }
+      }
+      if (graph) cudaGraphDestroy(graph);
+      if (ok) {
+        *looped = true;
+        return MFGB_OK;
+      }
+      cudaGetLastError();
+      *exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    if ((e = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture")))
+      return e;
+    mfgb_status cap = iteration(P);
+    if (!cap)
+      cudaMemcpyAsync(B->h_active, B->d_active, sizeof(int), cudaMemcpyDeviceToHost, s);
     const cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (cap) {
       if (graph) cudaGraphDestroy(graph);
@@ -1303,26 +1401,33 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
   struct FreeSub { Plan *p; ~FreeSub() { free_plan(*p); } } free_sub{&sub};
   const Plan *cur = &F;
   B->last_replans = 0;
+  B->last_launches = 0;
   if (running > 0 && ctl->max_steps > 0) {
     cudaGraphExec_t exec = nullptr;
-    if ((st = capture(*cur, &exec))) return st;
+    bool looped = false;
+    if ((st = capture(*cur, &exec, &looped))) return st;
     for (int it = 0; it < ctl->max_steps; ++it) {
-      cudaError_t e = cudaGraphLaunch(exec, s);
+      cudaError_t e = cudaSuccess;
+      if (looped) e = cudaMemsetAsync(B->d_iter, 0, sizeof(int), s);
+      if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      ++B->last_launches;
       if (e != cudaSuccess) {
         st = cuda_status(e, "batch cg iteration");
         break;
       }
-      if (*B->h_active == 0) break;
-      // re-plan for the running problems once they hold <= 60 % of the plan's DoFs
       if ((st = read_scalars())) break;
       std::vector<char> active(np, 0);
       int64_t dofs = 0;
+      int n_run = 0;
       for (int i = 0; i < np; ++i)
         if (!hs[i].done) {
           active[i] = 1;
+          ++n_run;
           dofs += B->depth[0].parts[i].n;
         }
+      if (n_run == 0) break;
+      // re-plan for the running problems once they hold <= 75 % of the plan's DoFs
       if (dofs <= 0.75 * (double)cur->dofs) {
         Plan next;
         if ((st = gather_plan(B, active, next, s))) break;
@@ -1332,7 +1437,7 @@ mfgb_status mfgb_batch_cg_solve(mfgb_batch *B, const double *d_b, double *d_x,
         sub = next;
         cur = &sub;
         ++B->last_replans;
-        if ((st = capture(*cur, &exec))) break;
+        if ((st = capture(*cur, &exec, &looped))) break;
       }
     }
     if (exec) cudaGraphExecDestroy(exec);

@@ -34,7 +34,17 @@ struct CgScalars {
   int done;         // 0 running, 1 converged, 2 failed
   int final_its;
   double final_res;
+  int loop_runs;    // body runs of the device-side loop (mfgb_cg_solve)
 };
+
+// condition of the device-side solve loop: repeat the captured block of
+// iterations while the solve runs, at most max_runs times (a hard bound; the
+// done flag is set at max_steps anyway)
+__global__ void cg_continue_kernel(cudaGraphConditionalHandle h, CgScalars *sc, int max_runs) {
+  const int r = sc->loop_runs + 1;
+  sc->loop_runs = r;
+  cudaGraphSetConditional(h, (!sc->done && r < max_runs) ? 1u : 0u);
+}
 
 constexpr int VEC_THREADS = 256;
 constexpr int VEC_BLOCKS = 152 * 8;
@@ -342,37 +352,77 @@ extern "C" mfgb_status mfgb_cg_solve(const mfgb_operator *cop, const double *d_b
     return st;
   if ((st = cuda_status(cudaMemsetAsync(v, 0, sizeof(double) * n, s), "v = 0"))) return st;
 
-  // capture K iterations into a graph (parity alternates, K even)
+  // K iterations (parity alternates, K even) captured as the body of a
+  // conditional while node: one graph launch runs the whole solve on the device
+  // (cg_continue_kernel ends it once the done flag is set).  Where the driver
+  // cannot build that graph, the K iterations form a plain graph the host
+  // relaunches until done.
   const int K = 16;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  if ((st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
-                        "begin capture")))
-    return st;
-  mfgb_status cap_st = MFGB_OK;
-  for (int k = 0; k < K && cap_st == MFGB_OK; ++k) {
-    const int parity = k & 1;
-    cap_st = apply_add_impl(op, v, p, ctl->arith, s, &sc->done);
-    if (cap_st) break;
-    if (op->n_constrained)
-      cg_constrained_copy_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(op->n_constrained,
-                                                                    op->d_constrained, p, v, sc);
-    cg_dot_pv_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, p, v, pap_part, sc);
-    cg_update_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_x, r, p, v, dinv, pap_part,
-                                                        VEC_BLOCKS, vec_part, sc, parity);
-    cg_direction_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, r, p, v, dinv, vec_part, VEC_BLOCKS,
-                                                           sc, parity);
-  }
-  const cudaError_t ce = cudaStreamEndCapture(s, &graph);
-  if (cap_st) {
-    if (graph) cudaGraphDestroy(graph);
+  bool looped = false;
+  // capture the K iterations into `graph` (as the body of a while node when
+  // try_loop) and instantiate it
+  auto build = [&](bool try_loop) -> mfgb_status {
+    mfgb_status bst;
+    graph = nullptr;
+    exec = nullptr;
+    looped = false;
+    cudaGraphConditionalHandle cond_h{};
+    if (try_loop) {
+      cudaGraphNodeParams cp{};
+      cudaGraphNode_t node;
+      looped = cudaGraphCreate(&graph, 0) == cudaSuccess &&
+               cudaGraphConditionalHandleCreate(&cond_h, graph, 1, cudaGraphCondAssignDefault) ==
+                   cudaSuccess;
+      if (looped) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond_h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        looped = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp) == cudaSuccess &&
+                 cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr,
+                                               0, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      }
+      if (!looped) {
+        cudaGetLastError();
+        if (graph) cudaGraphDestroy(graph);
+        graph = nullptr;
+        return MFGB_ERR_UNSUPPORTED;
+      }
+    } else if ((bst = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                                  "begin capture"))) {
+      return bst;
+    }
+    mfgb_status cap_st = MFGB_OK;
+    for (int k = 0; k < K && cap_st == MFGB_OK; ++k) {
+      const int parity = k & 1;
+      cap_st = apply_add_impl(op, v, p, ctl->arith, s, &sc->done);
+      if (cap_st) break;
+      if (op->n_constrained)
+        cg_constrained_copy_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(op->n_constrained,
+                                                                      op->d_constrained, p, v, sc);
+      cg_dot_pv_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, p, v, pap_part, sc);
+      cg_update_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, d_x, r, p, v, dinv, pap_part,
+                                                          VEC_BLOCKS, vec_part, sc, parity);
+      cg_direction_kernel<<<VEC_BLOCKS, VEC_THREADS, 0, s>>>(n, r, p, v, dinv, vec_part,
+                                                             VEC_BLOCKS, sc, parity);
+    }
+    if (looped && !cap_st)
+      cg_continue_kernel<<<1, 1, 0, s>>>(cond_h, sc, ctl->max_steps / K + 2);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &captured);
+    if (!looped) graph = captured;
+    if (!cap_st) cap_st = cuda_status(ce, "end capture");
+    if (!cap_st) cap_st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+    if (cap_st) {
+      if (graph) cudaGraphDestroy(graph);
+      graph = nullptr;
+      exec = nullptr;
+    }
     return cap_st;
-  }
-  if ((st = cuda_status(ce, "end capture"))) return st;
-  if ((st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate"))) {
-    cudaGraphDestroy(graph);
-    return st;
-  }
+  };
+  if (build(true) && (st = build(false))) return st;
   CgScalars out{};
   for (;;) {
     cudaError_t e = cudaGraphLaunch(exec, s);

@@ -350,11 +350,18 @@ mfgb_status mfgb_batch_precondition(mfgb_batch *batch, double *d_dst, const doub
    MFGB_ERR_NOT_CONVERGED if any problem reached max_steps (infos filled).
    Once the problems still running hold at most 75 % of the DoFs of the current
    launch plan, the union operators and tables are gathered again for them
-   (converged problems stop costing work). */
+   (converged problems stop costing work).  Each plan's iterations run as one
+   CUDA graph launch: a conditional while node repeats one iteration until no
+   problem runs, the running ones hold at most 75 % of the plan's DoFs, or
+   max_steps iterations; the host only gathers the next plan. */
 mfgb_status mfgb_batch_cg_solve(mfgb_batch *batch, const double *d_b, double *d_x,
                                 const mfgb_cg_control *ctl, mfgb_solve_info *h_info, void *stream);
 /* number of launch plans gathered during the last mfgb_batch_cg_solve */
 mfgb_status mfgb_batch_last_solve_stats(const mfgb_batch *batch, int *n_replans);
+/* number of graph launches of the last mfgb_batch_cg_solve (one per launch
+   plan with the device-side loop; one per iteration where a CUDA driver cannot
+   build the conditional graph) */
+mfgb_status mfgb_batch_last_solve_launches(const mfgb_batch *batch, int *n_launches);
 
 /* ---- learned part: features, targets, MLP (no counterpart in the reference)
  * features: per cell, dx/dxi at the 8 corner nodes (72 values, scaled by
