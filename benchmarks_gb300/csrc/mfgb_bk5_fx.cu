@@ -19,6 +19,16 @@ template <int N> struct FxAltElems { static constexpr int value = AltElemsN<N>::
 template <int N> struct FxAltMinBlocks {
   static constexpr int value = AltMinBlocks<N, FxAltElems<N>::value, ArithDF>::value;
 };
+// n = 7..9: fewer cells per CTA and more resident CTAs (registers from -Xptxas
+// -v: n = 7, 2 cells, 3 CTAs: 158, no spill; n = 8, 1 cell, 4 CTAs: 179, no
+// spill; n = 9, 2 cells, 2 CTAs: 168 with a 48-byte spill, 1 cell, 3 CTAs: 168
+// with 32 bytes), where the wide cells of 1-CTA shapes left too few warps
+template <> struct FxElems<7> { static constexpr int value = 2; };
+template <> struct FxMinBlocks<7> { static constexpr int value = 3; };
+template <> struct FxAltMinBlocks<8> { static constexpr int value = 4; };
+template <> struct FxMinBlocks<9> { static constexpr int value = 2; };
+template <> struct FxAltElems<9> { static constexpr int value = 1; };
+template <> struct FxAltMinBlocks<9> { static constexpr int value = 3; };
 
 // test hook: applications left whose first copy wait is made to run out
 static std::atomic<int> g_expire{0};

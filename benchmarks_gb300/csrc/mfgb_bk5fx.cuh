@@ -127,6 +127,20 @@ __device__ __forceinline__ double fx_f2d(float f, int sc) {
                                           ((unsigned long long)(u & 0x7FFFFFu) << 29)));
 }
 
+// The same for a cell whose scale keeps every result in the double range
+// (|sc| <= 896, k = (896 + sc) << 20): the exponent is rebased on the high word
+// by one integer addition; zero and subnormal floats give a signed zero,
+// inf and NaN stay inf and NaN.
+__device__ __forceinline__ double fx_f2d_fast(float f, unsigned k) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned a = u & 0x7FFFFFFFu, sgn = u & 0x80000000u;
+  unsigned hi = ((a >> 3) + k) | sgn;
+  unsigned lo = u << 29;
+  if (a < 0x00800000u) hi = sgn, lo = 0u;
+  if (a >= 0x7F800000u) hi = sgn | 0x7FF00000u | ((a & 0x7FFFFFu) >> 3);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
 // the scale offset of a cell from its largest biased exponent
 __device__ __forceinline__ int fx_offset(int emax) { return emax > 0 ? emax - 1022 : 0; }
 
@@ -238,6 +252,8 @@ __global__ void __launch_bounds__(E * N * N, MB)
     T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase by barrier B
     const int su = fx_offset(s_emax[slot][el]);
     const int sc = su + ge;  // the cell's result scale
+    const bool fast_out = (unsigned)(sc + 896) <= 1792u;
+    const unsigned kout = (unsigned)(896 + sc) << 20;
     df u[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -353,7 +369,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
         fx_fma(a, Dtkh[m], Dtkl[m], lt[m].hi, lt[m].lo);
       }
       const df y = fx_finish(a, C);
-      if (cur[i] != MFGB_INVALID_DOF) atomicAdd(dst + cur[i], fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
+      if (cur[i] != MFGB_INVALID_DOF)
+        atomicAdd(dst + cur[i], fast_out ? fx_f2d_fast(y.hi, kout) + fx_f2d_fast(y.lo, kout)
+                                         : fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
     }
     // the prefetched gather's largest exponent per cell, once its loads have
     // landed (read after the next barrier A)

@@ -218,3 +218,30 @@ def test_cell_chain_at_p4_matches_extended_precision():
           np.einsum('mk,eijm->eijk', De, vt))
     rel = float(np.sqrt(((y - ye) ** 2).sum() / (ye ** 2).sum()))
     assert rel < 2.0 ** -42, np.log2(rel)
+
+
+def fx_f2d_fast(f, sc):
+    """restatement of fx_f2d_fast: float * 2^sc to double by integer operations
+    on the high word (cells with |sc| <= 896)"""
+    u = np.asarray(f, np.float32).view(np.uint32).astype(np.uint64)
+    a = u & np.uint64(0x7FFFFFFF)
+    sgn = u & np.uint64(0x80000000)
+    hi = ((a >> np.uint64(3)) + np.uint64((896 + sc) << 20)) | sgn
+    lo = (u << np.uint64(29)) & np.uint64(0xFFFFFFFF)
+    small = a < 0x00800000
+    hi = np.where(small, sgn, hi)
+    lo = np.where(small, np.uint64(0), lo)
+    big = a >= 0x7F800000
+    hi = np.where(big, sgn | np.uint64(0x7FF00000) | ((a & np.uint64(0x7FFFFF)) >> np.uint64(3)), hi)
+    return ((hi << np.uint64(32)) | lo).view(np.float64)
+
+
+@pytest.mark.parametrize("sc", [-896, -500, 0, 300, 896])
+def test_fast_output_conversion_is_exact(sc):
+    rng = np.random.default_rng(0)
+    f = (rng.standard_normal(50000) * 10.0 ** rng.integers(-30, 30, 50000)).astype(f32)
+    want = np.where(np.abs(f) < np.finfo(f32).tiny, 0.0, f.astype(np.float64) * 2.0 ** sc)
+    assert np.array_equal(fx_f2d_fast(f, sc), want)
+    special = fx_f2d_fast(np.array([np.inf, -np.inf, np.nan, 0.0, -0.0], f32), sc)
+    assert special[0] == np.inf and special[1] == -np.inf and np.isnan(special[2])
+    assert special[3] == 0.0 and special[4] == 0.0
