@@ -54,6 +54,19 @@ def cell_lambda(A, iterations=200):
     return lam
 
 
+def cell_error_reduction(A, M, n_vectors=4, seed=11):
+    """Per-cell error reduction of one V-cycle of the multigrid M over A's mesh,
+    rho_c = |(I - M A) e|_c / |e|_c over n_vectors seeded random errors: the
+    training data the FP64 multigrid itself generates (mfgb_cell_error_reduction);
+    float64 [n_cells] on the device."""
+    torch = _torch()
+    from . import _stream_ptr
+    r = torch.empty(A.n_cells, dtype=torch.float64, device="cuda")
+    _abi.check(lib().mfgb_cell_error_reduction(A.handle, M.handle, int(n_vectors),
+                                               ctypes.c_uint64(seed), _ptr(r), _stream_ptr()))
+    return r
+
+
 class LearnedSmoother:
     def __init__(self, params=None, seed=0):
         torch = _torch()

@@ -137,3 +137,40 @@ def test_smoother_weights_gain_on_deformed_mesh(mf):
     S = LearnedSmoother.load(path)
     used, p0, learned, alpha = S.attach(M, A, calibrate=True, reduce=1e-10, seed=3)
     assert p0 == plain and its() == (learned if used else plain) <= plain
+
+
+def test_multigrid_error_reduction_data(mf, orc):
+    """The FP64 multigrid's own training data (mfgb_cell_error_reduction): per-cell
+    reduction of one V-cycle on seeded random errors.  Checked against a CPU
+    computation from the library's own vectors (E e = e - M A e, cell norms over
+    the exported dof map), reproducible, in (0, 1), and strongly correlated with
+    the cell spectra lambda_max(D_e^-1 A_e) on a deformed mesh."""
+    import ctypes
+    import torch
+    from benchmarks_gb300.learned import cell_error_reduction, cell_lambda
+    mesh = mf.BoxMesh(6, 5, 4, degree=3, amplitude=0.1)
+    A = mf.LaplaceOperator(mesh)
+    M = mf.MGPreconditioner(mesh, precision=64, operator=A)
+    rho = cell_error_reduction(A, M, n_vectors=2, seed=5)
+    assert torch.equal(rho, cell_error_reduction(A, M, n_vectors=2, seed=5))
+    r = rho.cpu().numpy()
+    assert np.all(r > 0) and np.all(r < 1)
+    dof_map, _, _ = A.export()
+    n3 = (mesh.degree + 1) ** 3
+    cmap = dof_map.reshape(-1, n3)
+    na = np.zeros(A.n_cells)
+    nb = np.zeros(A.n_cells)
+    for k in range(2):
+        e = A.rhs_uniform(5 + k)
+        w = A.initialize_dof_vector()
+        A.vmult(w, e)
+        z = A.initialize_dof_vector()
+        M.vmult(z, w)
+        eh, ph = e.cpu().numpy(), (e - z).cpu().numpy()
+        for c in range(A.n_cells):
+            d = cmap[c][cmap[c] != 0xFFFFFFFF]
+            na[c] += np.sum(eh[d] ** 2)
+            nb[c] += np.sum(ph[d] ** 2)
+    np.testing.assert_allclose(r, np.sqrt(nb / na), rtol=1e-9)
+    lam = cell_lambda(A, 200).cpu().numpy()
+    assert np.corrcoef(np.log(r), np.log(lam))[0, 1] > 0.5
