@@ -598,7 +598,7 @@ def bk1_bk3_rates(degree=4, target_dofs=6.7e7):
     for name, fn, coef_bytes in (
             ("bk1", lambda a: mf.bk1_evector(degree, basis, jxw, u, y, arith=a), 8 * nq ** 3),
             ("bk3", lambda a: mf.bk3_evector(degree, basis, dbasis, G, u, y, arith=a), 48 * nq ** 3)):
-        for arith in ("df", "fp64"):
+        for arith in ("df", "fp64") + (("tc",) if name == "bk1" and degree <= 6 else ()):
             for _ in range(3):
                 fn(arith)
             torch.cuda.synchronize()

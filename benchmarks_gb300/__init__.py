@@ -17,7 +17,6 @@ import os
 from dataclasses import dataclass
 
 from . import _abi
-from . import _abi  # noqa: F401
 from ._abi import MfgbError, ARITH_FP64, ARITH_FP64_DF, lib, library_path  # noqa: F401
 
 __all__ = [
@@ -28,7 +27,9 @@ __all__ = [
 ]
 
 _ARITH = {"fp64": ARITH_FP64, "df": ARITH_FP64_DF, "fp64_df": ARITH_FP64_DF,
-          ARITH_FP64: ARITH_FP64, ARITH_FP64_DF: ARITH_FP64_DF}
+          "tc": _abi.ARITH_FP64_TC, "fp64_tc": _abi.ARITH_FP64_TC,
+          ARITH_FP64: ARITH_FP64, ARITH_FP64_DF: ARITH_FP64_DF,
+          _abi.ARITH_FP64_TC: _abi.ARITH_FP64_TC}
 
 
 def _arith(a) -> int:
@@ -399,7 +400,8 @@ def bk5_evector(degree, dbasis, G, u, out, arith="fp64"):
 
 def bk1_evector(degree, basis, JxW, u, out, arith="fp64"):
     """E-vector seam of the CEED BK1 mass operator (BK1::Parallel::MassOperator),
-    nq = degree + 2 points: basis [nq * nm], JxW [e][nq^3], u/out [e][nm^3]."""
+    nq = degree + 2 points: basis [nq * nm], JxW [e][nq^3], u/out [e][nm^3].
+    arith "fp64", "df", or "tc" (FP64 tensor cores, degree 1..6)."""
     nm3 = (degree + 1) ** 3
     _abi.check(lib().mfgb_bk1_evector(
         int(degree), u.numel() // nm3, ctypes.c_void_p(basis.data_ptr()),

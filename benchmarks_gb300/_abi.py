@@ -10,7 +10,7 @@ _LIB = None
 OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_NOT_CONVERGED = 0, 1, 2, 3
 ERR_TIMEOUT, ERR_NONFINITE, ERR_CUDA, ERR_UNSUPPORTED = 4, 5, 6, 7
 ERR_RANGE = 8
-ARITH_FP64, ARITH_FP64_DF, ARITH_FP32 = 0, 1, 2
+ARITH_FP64, ARITH_FP64_DF, ARITH_FP32, ARITH_FP64_TC = 0, 1, 2, 3
 INVALID_DOF = 0xFFFFFFFF
 
 

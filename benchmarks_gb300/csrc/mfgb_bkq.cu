@@ -54,13 +54,19 @@ mfgb_status bkq_entry(const char *name, bool laplace, int degree, int64_t nelmt,
                       const double *in, double *out, int arith, void *stream) {
   if (degree < 1 || degree > 8 || nelmt < 0 || (nelmt > 0 && (!basis || !coef || !in || !out)) ||
       (laplace && nelmt > 0 && !dbasis) ||
-      (arith != MFGB_ARITH_FP64 && arith != MFGB_ARITH_FP64_DF)) {
-    set_error(std::string(name) + ": invalid argument (degree 1..8, arith FP64 or FP64_DF)");
+      (arith != MFGB_ARITH_FP64 && arith != MFGB_ARITH_FP64_DF && arith != MFGB_ARITH_FP64_TC)) {
+    set_error(std::string(name) + ": invalid argument (degree 1..8, arith FP64, FP64_DF or FP64_TC)");
     return MFGB_ERR_INVALID_ARG;
+  }
+  if (arith == MFGB_ARITH_FP64_TC && (laplace || degree > 6)) {
+    set_error(std::string(name) + ": FP64_TC is the BK1 mass operator at degree 1..6");
+    return MFGB_ERR_UNSUPPORTED;
   }
   if (nelmt == 0) return MFGB_OK;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
+  if (arith == MFGB_ARITH_FP64_TC)
+    return cuda_status(bk1_dmma(degree, nelmt, basis, coef, in, out, s), name);
   if (arith == MFGB_ARITH_FP64_DF) {
     // the double-float range of the inputs and of the caller's coefficients,
     // reported through the device error word (mfgb_check_device_errors)

@@ -124,6 +124,10 @@ int dot_partials_count();
 cudaError_t dot_to_device(int64_t n, const double *a, const double *b, double *partials,
                           double *out, cudaStream_t s);
 
+// BK1 E-vector mass operator on the FP64 tensor cores (mfgb_bk1_dmma.cu),
+// degree 1..6, the layouts of mfgb_bk1_evector
+cudaError_t bk1_dmma(int degree, int64_t nelmt, const double *basis, const double *JxW,
+                     const double *in, double *out, cudaStream_t s);
 // BP3 operator (mfgb_bkq.cu): dst += A src, q = p + 2 Gauss points, G[cell][6][nq^3]
 // in FP64 (G) and, for double-float arithmetic, as pairs (Gdf); the bases on the
 // device (d_B, d_DG) and on the host (h_B, h_DG)

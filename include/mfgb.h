@@ -50,7 +50,9 @@ enum {
 enum {
   MFGB_ARITH_FP64 = 0,    /* native FP64 (DFMA) */
   MFGB_ARITH_FP64_DF = 1, /* FP64-accurate double-float on the FP32 pipes */
-  MFGB_ARITH_FP32 = 2     /* FP32 operator on FP32 vectors (multigrid levels) */
+  MFGB_ARITH_FP32 = 2,    /* FP32 operator on FP32 vectors (multigrid levels) */
+  MFGB_ARITH_FP64_TC = 3  /* native FP64 on the tensor cores (mma m8n8k4 .f64):
+                             mfgb_bk1_evector at degree 1..6 only */
 };
 
 #define MFGB_INVALID_DOF_INDEX 0xFFFFFFFFu
@@ -213,7 +215,10 @@ mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, 
    out_e = B^T (JxW_e o (B x B x B) in_e); d_basis[q*nm + i], d_JxW[e][nq^3],
    d_in/d_out[e][nm^3], point and mode indices with direction 0 slowest (the
    reference serial kernel's order, CEED_BK/include/kernels/BK1/serial_kernels.hpp;
-   its CUDA kernel indexes JxW with direction 2 slowest).  arith FP64 or FP64_DF. */
+   its CUDA kernel indexes JxW with direction 2 slowest).  arith FP64, FP64_DF,
+   or FP64_TC (degree 1..6: the six 1D contractions as 8x8x4 FP64 tensor-core
+   tiles, one warp per element, the comparison of the reference's
+   sum_factorization/include/kernels/BK1/templated_cuda_mma_kernels.cuh). */
 mfgb_status mfgb_bk1_evector(int degree, int64_t nelmt, const double *d_basis, const double *d_JxW,
                              const double *d_in, double *d_out, int arith, void *stream);
 

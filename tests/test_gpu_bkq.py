@@ -1,6 +1,7 @@
 """CEED BK1 (mass) and BK3 (Laplacian, q = p + 2) E-vector seams on the GPU
 against the reference's serial outputs and the CPU oracle.  Tolerance: 1e-12
-relative for both FP64 arithmetics."""
+relative for the three FP64 arithmetics (DFMA, double-float on the FP32
+pipes, DMMA tensor-core tiles for BK1)."""
 import numpy as np
 import pytest
 
@@ -69,6 +70,48 @@ def test_bk1_bk3_many_elements_match_oracle(mf, orc, p, arith):
     assert rel(y3.cpu().numpy(), orc.bk3_evector(nm, nq, basis, dbasis, G.reshape(-1), u)) <= 1e-12
 
 
+@pytest.mark.parametrize("p", range(1, 7))
+def test_bk1_tensor_cores_match_reference_and_oracle(mf, golden13, orc, p):
+    """The FP64 tensor-core BK1 (mma m8n8k4 .f64 tiles) on the reference's own
+    serial outputs and on 37 / 1000 elements against the oracle: the grid
+    strides over warps, so a partial last CTA and several elements per warp
+    are both exercised."""
+    import torch
+    c = golden13["bk1_cases"][str(p)]
+    u = cuda(c["in"])
+    y = torch.zeros_like(u)
+    mf.bk1_evector(p, cuda(c["basis"]), cuda(c["JxW"]), u, y, arith="tc")
+    assert rel(y.cpu().numpy(), np.array(c["out"])) <= 1e-12
+    nq, nm = p + 2, p + 1
+    g = np.random.default_rng(10 + p)
+    xg, _ = orc.gll(nm)
+    xq, _ = orc.gauss(nq)
+    basis = orc.interpolation_matrix(xg, xq)
+    for nel in (37, 1000):
+        jxw = g.uniform(0.5, 2.0, nel * nq ** 3)
+        u = g.uniform(-1, 1, nel * nm ** 3)
+        y = torch.zeros(u.size, dtype=torch.float64, device="cuda")
+        mf.bk1_evector(p, cuda(basis), cuda(jxw), cuda(u), y, arith="tc")
+        assert rel(y.cpu().numpy(), orc.bk1_evector(nm, nq, basis, jxw, u)) <= 1e-12
+
+
+def test_bk1_tensor_cores_large_grid(mf):
+    """More elements than one wave of warps: agreement with the DFMA kernel
+    element by element."""
+    import torch
+    p, nel = 4, 300000
+    nq, nm = p + 2, p + 1
+    g = torch.Generator(device="cuda").manual_seed(3)
+    basis = torch.rand(nq * nm, dtype=torch.float64, device="cuda", generator=g)
+    jxw = torch.rand(nel * nq ** 3, dtype=torch.float64, device="cuda", generator=g)
+    u = torch.rand(nel * nm ** 3, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    y0, y1 = torch.zeros_like(u), torch.zeros_like(u)
+    mf.bk1_evector(p, basis, jxw, u, y0, arith="fp64")
+    mf.bk1_evector(p, basis, jxw, u, y1, arith="tc")
+    d = (y1 - y0).view(nel, -1).norm(dim=1) / y0.view(nel, -1).norm(dim=1)
+    assert float(d.max()) <= 1e-12
+
+
 def test_bk_verification_norms_on_gpu(mf, golden13):
     import torch
     p, nel = 4, 1000
@@ -89,3 +132,7 @@ def test_bkq_invalid_arguments(mf):
     assert L.mfgb_bk1_evector(9, 1, None, None, None, None, 0, None) == _abi.ERR_INVALID_ARG
     assert L.mfgb_bk3_evector(2, 1, None, None, None, None, None, 2, None) == _abi.ERR_INVALID_ARG
     assert L.mfgb_bk1_evector(2, 0, None, None, None, None, 0, None) == _abi.OK
+    # tensor-core BK1: degree 1..6, mass operator only
+    assert L.mfgb_bk1_evector(7, 0, None, None, None, None, 3, None) == _abi.ERR_UNSUPPORTED
+    assert L.mfgb_bk3_evector(2, 0, None, None, None, None, None, 3, None) == _abi.ERR_UNSUPPORTED
+    assert L.mfgb_bk1_evector(2, 0, None, None, None, None, 3, None) == _abi.OK
