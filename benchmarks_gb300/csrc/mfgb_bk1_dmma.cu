@@ -1,6 +1,9 @@
-// CEED BK1 (mass) E-vector operator on the FP64 tensor cores: the comparison the
-// reference's sum_factorization/include/kernels/BK1/cuda_mma_kernels.cuh:94-100
-// makes (mma.sync m8n8k4 f64 tiles over the 1D contractions), restated for GB300.
+// CEED BK1 (mass) E-vector operator on the FP64 tensor cores.  The reference's
+// BwdTransHexKernel_mma (sum_factorization/include/kernels/BK1/
+// templated_cuda_mma_kernels.cuh:123-240) runs the direction-1 and -2
+// contractions of both passes as mma.sync m8n8k4 f64 tiles (the instruction at
+// cuda_mma_kernels.cuh:94-100) and direction 0 on the FMA pipe; here all six
+// contractions are tiles.
 //
 //   out_e = B^T (JxW_e o (B x B x B) in_e),  B[q*NM + i] (NQ x NM), JxW[e][NQ^3],
 //   in/out[e][NM^3], indices with direction 0 slowest (the serial kernel's order,

@@ -141,6 +141,17 @@ __device__ __forceinline__ double fx_f2d_fast(float f, unsigned k) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// a float pair from shared memory, kept at its place in the batch loop (the
+// compiler would otherwise hoist loop-invariant rows of D into registers for
+// the whole kernel)
+__device__ __forceinline__ float2 lds_pair(const float2 *p) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+               : "=f"(v.x), "=f"(v.y)
+               : "r"((unsigned)__cvta_generic_to_shared(p)));
+  return v;
+}
+
 // the scale offset of a cell from its largest biased exponent
 __device__ __forceinline__ int fx_offset(int emax) { return emax > 0 ? emax - 1022 : 0; }
 
@@ -184,19 +195,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
   int64_t batch = blockIdx.x;
   if (batch >= n_batches) return;  // uniform across the CTA
 
-  // rows / columns of D this thread needs with a runtime index, and their bounds
-  float Djh[N], Djl[N], Dkh[N], Dkl[N], Dtjh[N], Dtjl[N], Dtkh[N], Dtkl[N];
-#pragma unroll
-  for (int m = 0; m < N; ++m) {
-    Djh[m] = basis.Dh[j * N + m];
-    Djl[m] = basis.Dl[j * N + m];
-    Dkh[m] = basis.Dh[k * N + m];
-    Dkl[m] = basis.Dl[k * N + m];
-    Dtjh[m] = basis.Dh[m * N + j];
-    Dtjl[m] = basis.Dl[m * N + j];
-    Dtkh[m] = basis.Dh[m * N + k];
-    Dtkl[m] = basis.Dl[m * N + k];
-  }
+  // D as (hi, lo) pairs: the rows and columns this thread needs with a runtime
+  // index are read from here at the start of the phase that uses them, so only
+  // one phase's 4N of them are live at a time
+  __shared__ float2 s_D[N * N];
+  for (int t = tid; t < N * N; t += blockDim.x) s_D[t] = make_float2(basis.Dh[t], basis.Dl[t]);
   const float cgj = basis.cg[j], cgk = basis.cg[k], cij = basis.ci[j], cik = basis.ci[k];
 
   TmaTiles<N, E, ArithDF> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
@@ -268,6 +271,12 @@ __global__ void __launch_bounds__(E * N * N, MB)
     }
 
     const bool valid = el < T.cells_of(batch);
+    float Djh[N], Djl[N], Dkh[N], Dkl[N];
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const float2 a = lds_pair(s_D + j * N + m), b = lds_pair(s_D + k * N + m);
+      Djh[m] = a.x, Djl[m] = a.y, Dkh[m] = b.x, Dkl[m] = b.y;
+    }
     df vr[N];
     const float2 *Gc = sG + el * 6 * N3 + jk;
 #pragma unroll
@@ -343,6 +352,12 @@ __global__ void __launch_bounds__(E * N * N, MB)
     // ---- transpose: y = sum_m D[m][i] v_r(m,j,k) + D[m][j] v_s(i,m,k) + D[m][k] v_t(i,j,m);
     // the bound of output i: max |v_r| of the own column and the maxima of the
     // s- and t-lines it reads
+    float Dtjh[N], Dtjl[N], Dtkh[N], Dtkl[N];
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const float2 a = lds_pair(s_D + m * N + j), b = lds_pair(s_D + m * N + k);
+      Dtjh[m] = a.x, Dtjl[m] = a.y, Dtkh[m] = b.x, Dtkl[m] = b.y;
+    }
     float mr = 0.f;
 #pragma unroll
     for (int m = 0; m < N; ++m) mr = fmaxf(mr, fabsf(vr[m].hi));

@@ -50,6 +50,57 @@ __global__ void __launch_bounds__(256) ffma_kernel(int iters, double *out) {
   out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
 }
 
+// packed dual FP32 FMA (fma.rn.f32x2, __ffma2_rn): two FMAs per instruction
+__global__ void __launch_bounds__(256) ffma2_kernel(int iters, double *out) {
+  float2 a[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c)
+    a[c] = make_float2(1.f + 1e-3f * (threadIdx.x + c), 1.f - 1e-3f * (threadIdx.x + c));
+  const float2 x = make_float2(0.9999f, 0.9998f), y = make_float2(1e-7f, 2e-7f);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) a[c] = __ffma2_rn(a[c], x, y);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) s += a[c].x + a[c].y;
+  out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+// FP32 FMAs interleaved with one integer logic instruction (lop3) per chain
+// step: PAIRED = false issues two scalar FMAs per step, PAIRED = true one
+// packed FMA.  Against pipes 1 / 4 this shows whether the integer work finds
+// issue slots that the FMAs leave free.
+template <bool PAIRED>
+__global__ void __launch_bounds__(256) fma_alu_kernel(int iters, double *out) {
+  float2 a[kChains];
+  uint32_t h[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) {
+    a[c] = make_float2(1.f + 1e-3f * (threadIdx.x + c), 1.f - 1e-3f * (threadIdx.x + c));
+    h[c] = threadIdx.x * 2654435761u + c;
+  }
+  const float2 x = make_float2(0.9999f, 0.9998f), y = make_float2(1e-7f, 2e-7f);
+  const uint32_t m1 = threadIdx.x | 1u, m2 = threadIdx.x * 7u;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) {
+      if (PAIRED) {
+        a[c] = __ffma2_rn(a[c], x, y);
+      } else {
+        a[c].x = __fmaf_rn(a[c].x, x.x, y.x);
+        a[c].y = __fmaf_rn(a[c].y, x.y, y.y);
+      }
+      asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(h[c]) : "r"(m1), "r"(m2));
+    }
+  }
+  float s = 0.f;
+  uint32_t t = 0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) s += a[c].x + a[c].y, t ^= h[c];
+  out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s + (double)(t & 1u);
+}
+
 // D(8x8) += A(8x4) B(4x8) in FP64: per thread one A and one B element, two
 // accumulator elements; 4 independent accumulators per warp
 __global__ void __launch_bounds__(256) dmma_kernel(int iters, double *out) {
@@ -99,10 +150,12 @@ __global__ void __launch_bounds__(256) hmma_kernel(int iters, double *out) {
 
 using namespace mfgb;
 
-// pipe: 0 DFMA, 1 FFMA, 2 DMMA m8n8k4 f64, 3 BF16 mma.sync m16n8k16.
-// *ops_per_s = floating-point operations per second (FMA = 2, MMA = 2 m n k).
+// pipe: 0 DFMA, 1 FFMA, 2 DMMA m8n8k4 f64, 3 BF16 mma.sync m16n8k16,
+// 4 packed FFMA2, 5 FFMA + lop3, 6 FFMA2 + lop3.
+// *ops_per_s = floating-point operations per second (FMA = 2, MMA = 2 m n k;
+// the lop3 of pipes 5 / 6 counts nothing).
 extern "C" mfgb_status mfgb_pipe_rate(int pipe, int iters, int reps, double *ops_per_s) {
-  if (pipe < 0 || pipe > 3 || iters < 1 || reps < 1 || !ops_per_s) {
+  if (pipe < 0 || pipe > 6 || iters < 1 || reps < 1 || !ops_per_s) {
     set_error("mfgb_pipe_rate: invalid argument");
     return MFGB_ERR_INVALID_ARG;
   }
@@ -121,7 +174,10 @@ extern "C" mfgb_status mfgb_pipe_rate(int pipe, int iters, int reps, double *ops
       case 0: dfma_kernel<<<blocks, threads>>>(iters, out); break;
       case 1: ffma_kernel<<<blocks, threads>>>(iters, out); break;
       case 2: dmma_kernel<<<blocks, threads>>>(iters, out); break;
-      default: hmma_kernel<<<blocks, threads>>>(iters, out); break;
+      case 3: hmma_kernel<<<blocks, threads>>>(iters, out); break;
+      case 4: ffma2_kernel<<<blocks, threads>>>(iters, out); break;
+      case 5: fma_alu_kernel<false><<<blocks, threads>>>(iters, out); break;
+      default: fma_alu_kernel<true><<<blocks, threads>>>(iters, out); break;
     }
   };
   cudaEvent_t e0, e1;
@@ -144,7 +200,8 @@ extern "C" mfgb_status mfgb_pipe_rate(int pipe, int iters, int reps, double *ops
     case 0:
     case 1: flops_per_iter = 2.0 * kChains; break;
     case 2: flops_per_iter = 4.0 * 2.0 * 8 * 8 * 4 / 32.0; break;   // 4 MMAs per warp
-    default: flops_per_iter = 4.0 * 2.0 * 16 * 8 * 16 / 32.0; break;
+    case 3: flops_per_iter = 4.0 * 2.0 * 16 * 8 * 16 / 32.0; break;
+    default: flops_per_iter = 4.0 * kChains; break;                  // two FMAs per chain
   }
   *ops_per_s = threads_total * flops_per_iter * iters * reps / (ms * 1e-3);
   return MFGB_OK;

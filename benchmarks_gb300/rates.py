@@ -1,6 +1,7 @@
 """Arithmetic-pipe throughput of the running GPU (mfgb_pipe_rate): FP64 FMA,
-FP32 FMA, FP64 tensor-core MMA (m8n8k4) and BF16 tensor-core mma.sync, in
-FLOP/s.  These rates decide the operator kernels' arithmetic: FP64-accurate
+FP32 FMA, FP64 tensor-core MMA (m8n8k4), BF16 tensor-core mma.sync and the
+packed dual FP32 FMA (fma.rn.f32x2), alone and interleaved with one integer
+logic instruction per FMA step, in FLOP/s.  These rates decide the operator kernels' arithmetic: FP64-accurate
 applies run as float pairs on the FP32 pipes because the FP64 pipes, scalar
 and tensor, are far slower on this part.
 
@@ -15,7 +16,8 @@ import json
 from . import _abi
 from ._abi import lib
 
-PIPES = {"fp64_fma": 0, "fp32_fma": 1, "fp64_mma_m8n8k4": 2, "bf16_mma_m16n8k16": 3}
+PIPES = {"fp64_fma": 0, "fp32_fma": 1, "fp64_mma_m8n8k4": 2, "bf16_mma_m16n8k16": 3,
+         "fp32x2_fma": 4, "fp32_fma_with_lop3": 5, "fp32x2_fma_with_lop3": 6}
 
 
 def pipe_rates(iters=4096, reps=5):

@@ -399,7 +399,9 @@ mfgb_status mfgb_mlp_infer(const float *d_params, const float *d_X, int64_t n, d
  * GPU, from independent register-only chains on 8 CTAs of 256 threads per SM:
  * pipe 0 FP64 FMA, 1 FP32 FMA, 2 FP64 tensor-core MMA (mma.sync m8n8k4 f64, the
  * instruction of sum_factorization/include/kernels/BK1/cuda_mma_kernels.cuh:94-100),
- * 3 BF16 tensor-core mma.sync m16n8k16 with FP32 accumulation.  An FMA counts 2,
+ * 3 BF16 tensor-core mma.sync m16n8k16 with FP32 accumulation, 4 packed dual
+ * FP32 FMA (fma.rn.f32x2), 5 / 6 scalar / packed FP32 FMAs with one integer
+ * lop3 per FMA step (the lop3 counts nothing).  An FMA counts 2,
  * an m x n x k MMA 2 m n k.  The operator kernels' choice of arithmetic rests on
  * these rates. */
 mfgb_status mfgb_pipe_rate(int pipe, int iters, int reps, double *ops_per_s);
