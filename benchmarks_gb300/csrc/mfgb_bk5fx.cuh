@@ -32,6 +32,8 @@
 // A float32 restatement of this arithmetic with its error bound is in
 // tests/test_fx_arith.py.
 #pragma once
+#include <type_traits>
+
 #include "mfgb_bk5.cuh"
 
 namespace mfgb {
@@ -88,7 +90,8 @@ __device__ __forceinline__ int dexp(double x) {
 // x * 2^-off as a float pair by integer operations (off chosen so that the
 // cell's largest value lands in [0.5, 1)): hi = the top 24 significant bits,
 // lo = the next 29 bits rounded to float.  Values below 2^-126 after scaling
-// (126 binades under the cell's largest) flush to zero; inf and NaN give NaN.
+// (126 binades under the cell's largest), zeros and double subnormals flush to
+// zero; inf and NaN give NaN.
 __device__ __forceinline__ df fx_from_double(double x, int off) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
@@ -97,7 +100,7 @@ __device__ __forceinline__ df fx_from_double(double x, int off) {
   df r;
   if (e == 0x7FF) { r.hi = __uint_as_float(0x7FC00000u); r.lo = 0.f; return r; }
   const int es = e - off;
-  if (es <= 896) { r.hi = 0.f; r.lo = 0.f; return r; }
+  if (e == 0 || es <= 896) { r.hi = 0.f; r.lo = 0.f; return r; }
   const unsigned hm = ((hw & 0xFFFFFu) << 3) | (lw >> 29);
   r.hi = __uint_as_float(sign | ((unsigned)(es - 896) << 23) | hm);
   const unsigned rem = lw & 0x1FFFFFFFu;
@@ -178,11 +181,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
   constexpr int N2 = N * N, N3 = N * N * N;
   extern __shared__ __align__(128) unsigned char smem[];
   float2 *sG = reinterpret_cast<float2 *>(smem);
-  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
-  df *s_u = reinterpret_cast<df *>(smem + L::g_bytes + L::map_bytes);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::map_off);
+  df *s_u = reinterpret_cast<df *>(smem + L::work_off);
   df *s_vs = s_u + E * N3;
   df *s_vt = s_vs + E * N3;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::mbar_off);
   uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
   __shared__ int s_emax[2][E];
 
@@ -270,7 +273,6 @@ __global__ void __launch_bounds__(E * N * N, MB)
       T.issue_map(next);
     }
 
-    const bool valid = el < T.cells_of(batch);
     float Djh[N], Djl[N], Dkh[N], Dkl[N];
 #pragma unroll
     for (int m = 0; m < N; ++m) {
@@ -298,16 +300,12 @@ __global__ void __launch_bounds__(E * N * N, MB)
         fx_fma(at, Dkh[m], Dkl[m], b.hi, b.lo);
       }
       const df qr = fx_finish(ar, cr), qs = fx_finish(as, cgj), qt = fx_finish(at, cgk);
-      // ---- metric, bound per point: max |q| times the row sums of |G|
-      float2 grr = make_float2(0.f, 0.f), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
-      if (valid) {
-        grr = Gc[0 * N3 + i * N2];
-        grs = Gc[1 * N3 + i * N2];
-        grt = Gc[2 * N3 + i * N2];
-        gss = Gc[3 * N3 + i * N2];
-        gst = Gc[4 * N3 + i * N2];
-        gtt = Gc[5 * N3 + i * N2];
-      }
+      // ---- metric, bound per point: max |q| times the row sums of |G|.  The
+      // cells past the end of a last batch read whatever the tile holds: their
+      // results stay in their own rows of shared memory and are not scattered.
+      const float2 grr = Gc[0 * N3 + i * N2], grs = Gc[1 * N3 + i * N2],
+                   grt = Gc[2 * N3 + i * N2], gss = Gc[3 * N3 + i * N2],
+                   gst = Gc[4 * N3 + i * N2], gtt = Gc[5 * N3 + i * N2];
       const float kq = basis.K * fmaxf(fmaxf(fabsf(qr.hi), fabsf(qs.hi)), fabsf(qt.hi));
       const float Cr = (fabsf(grr.x) + fabsf(grs.x) + fabsf(grt.x)) * kq;
       const float Cs = (fabsf(grs.x) + fabsf(gss.x) + fabsf(gst.x)) * kq;
@@ -326,7 +324,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
       s_vs[el * N3 + i * N2 + jk] = fx_finish(bs, Cs);
       s_vt[el * N3 + i * N2 + jk] = fx_finish(bt, Ct);
     }
-    __syncthreads();  // barrier C: G tile consumed, s_vs / s_vt ready
+    // barrier C: G tile consumed, s_vs / s_vt ready; whether every cell of the
+    // batch converts its results by the one-addition exponent rebase
+    const bool all_fast = __syncthreads_and(fast_out);
     if (tid == 0 && has_next) {
       fence_proxy_async_smem();
       T.issue_g(next);
@@ -361,6 +361,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
     float mr = 0.f;
 #pragma unroll
     for (int m = 0; m < N; ++m) mr = fmaxf(mr, fabsf(vr[m].hi));
+    // one copy of the loop per conversion, chosen once per batch
+    auto transpose = [&](auto fast_tag) {
+      constexpr bool FAST = decltype(fast_tag)::value;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       df ls[N], lt[N];
@@ -385,9 +388,14 @@ __global__ void __launch_bounds__(E * N * N, MB)
       }
       const df y = fx_finish(a, C);
       if (cur[i] != MFGB_INVALID_DOF)
-        atomicAdd(dst + cur[i], fast_out ? fx_f2d_fast(y.hi, kout) + fx_f2d_fast(y.lo, kout)
-                                         : fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
+        atomicAdd(dst + cur[i], FAST ? fx_f2d_fast(y.hi, kout) + fx_f2d_fast(y.lo, kout)
+                                     : fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
     }
+    };
+    if (all_fast)
+      transpose(std::integral_constant<bool, true>{});
+    else
+      transpose(std::integral_constant<bool, false>{});
     // the prefetched gather's largest exponent per cell, once its loads have
     // landed (read after the next barrier A)
     if (has_next) reduce_exp(slot ^ 1);

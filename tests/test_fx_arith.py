@@ -103,7 +103,8 @@ def fx_from_double(x, off):
     lo_bits = (sign | (fb + ((es - 1075).astype(np.int64) << 23).astype(np.uint32))).astype(np.uint32)
     lo = np.where((rem == 0) | (es < 949), np.uint32(0), lo_bits).view(f32)
     hi = np.where(e == 0x7FF, np.float32(np.nan), hi)
-    return hi, np.where(es <= 896, f32(0), lo)
+    zero = (e == 0) | (es <= 896)
+    return np.where(zero, f32(0), hi), np.where(zero, f32(0), lo)
 
 
 @pytest.mark.parametrize("scale", [1.0, 2.0 ** -100, 1e-30, 1e30, 2.0 ** 300])
@@ -117,6 +118,20 @@ def test_scaled_conversion_keeps_48_bits(scale):
     back = (hi.astype(EXT) + lo.astype(EXT)) * EXT(2.0) ** off
     rel = np.abs(back - x.astype(EXT)) / np.abs(x).max()
     assert float(rel.max()) < 2.0 ** -47  # hi: 24 bits, lo: the next 29 rounded to 24
+
+
+@pytest.mark.parametrize("scale", [1.0, 1e-280, 2.0 ** -1000])
+def test_zeros_convert_to_zero_in_tiny_cells(scale):
+    """A cell whose largest value is below 2^-897 has a scale offset below -896:
+    its exact zeros (and double subnormals) must stay zero, not take the offset
+    as an exponent."""
+    x = np.array([0.0, -0.0, 0.75, -0.5, 5e-324]) * np.array([1, 1, scale, scale, 1])
+    emax = int(((np.abs(x).view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)).max())
+    off = emax - 1022
+    hi, lo = fx_from_double(x, off)
+    assert hi[0] == 0 and hi[1] == 0 and hi[4] == 0 and lo[4] == 0
+    back = (hi[2:4].astype(EXT) + lo[2:4].astype(EXT)) * EXT(2.0) ** off
+    assert np.all(np.abs(back - x[2:4].astype(EXT)) <= 2.0 ** -47 * np.abs(x[2:4]))
 
 
 def gll_derivative(n):

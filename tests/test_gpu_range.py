@@ -53,6 +53,20 @@ def test_gll_df_carries_any_source_scale(mf, box, scale):
     assert rel(y.cpu().numpy(), want * scale) <= TOL
 
 
+@pytest.mark.parametrize("scale", [1e-280, 2.0 ** -960])
+def test_gll_df_tiny_cells_keep_exact_zeros(mf, box, scale):
+    """Every cell's values below 2^-897: the cell scale offset is below -896, and
+    source entries that are exactly zero must convert to zero."""
+    ref, src, _ = box
+    s = src.copy()
+    s[::5] = 0.0
+    A = mf.LaplaceOperator(mf.BoxMesh(4, 3, 3, degree=4, amplitude=0.1))
+    y = A.initialize_dof_vector()
+    A.vmult(y, cuda(s * scale), arith="df")
+    mf.check_device_errors()
+    assert rel(y.cpu().numpy(), ref.apply(s) * scale) <= TOL
+
+
 @pytest.mark.parametrize("gscale", [2.0 ** -100, 1e-30, 1e30])
 def test_gll_df_carries_any_geometry_scale(mf, box, gscale):
     ref, src, want = box
