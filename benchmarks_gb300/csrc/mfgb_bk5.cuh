@@ -330,21 +330,18 @@ __global__ void __launch_bounds__(E * N * N * N)
 namespace mfgb {
 
 // Shared-memory layout of a bulk-TMA kernel's batch of E cells: G tile (6
-// components at NQ^3 points per cell), dof-map tile (NM^3 per cell, plus 16
-// bytes for the aligned window around it), NW work arrays of NQ^3 values per
-// cell, two mbarriers; every part starts on a 16-byte boundary.
+// components at NQ^3 points per cell), dof-map tile (NM^3 per cell), NW work
+// arrays of NQ^3 values per cell, two mbarriers.
 template <int NM, int NQ, int E, class A, int NW = 3>
 struct TmaLayoutQ {
   static constexpr int M3 = NM * NM * NM, Q3 = NQ * NQ * NQ;
   static constexpr size_t g_bytes = sizeof(typename A::GType) * E * 6 * Q3;
-  static constexpr size_t map_off = (g_bytes + 15) / 16 * 16;
-  static constexpr size_t map_bytes = ((size_t)E * M3 * 4 + 12 + 15) / 16 * 16;
-  static constexpr size_t work_off = map_off + map_bytes;
+  static constexpr size_t map_bytes = ((size_t)E * M3 * 4 + 15) / 16 * 16;
   static constexpr size_t work_bytes = NW * sizeof(typename A::V) * E * Q3;
-  static constexpr size_t mbar_off = (work_off + work_bytes + 15) / 16 * 16;
-  static constexpr size_t total = mbar_off + 16;
-  // G tiles start at batch * (full tile): bulk copies only when every full
-  // tile is a 16-byte multiple (then every batch's start is 16-byte aligned)
+  static constexpr size_t total = g_bytes + map_bytes + work_bytes + 16;
+  // tiles start at batch * (full tile): bulk copies only when every full tile
+  // is a 16-byte multiple (then every batch's start is 16-byte aligned)
+  static constexpr bool map_tma = (E * M3 * 4) % 16 == 0;
   static constexpr bool g_tma = g_bytes % 16 == 0;
 };
 template <int N, int E, class A> using TmaLayout = TmaLayoutQ<N, N, E, A>;
@@ -371,25 +368,8 @@ struct TmaTilesQ {
   __device__ __forceinline__ int cells_of(int64_t b) const {
     return (int)min((int64_t)E, n_cells - b * E);
   }
-  // The map slice of batch b is copied as the 16-byte aligned window that
-  // contains it (a bulk copy needs aligned ends; a slice of E * NM^3 indices
-  // need not be a 16-byte multiple nor start on a boundary).  The window must
-  // lie inside the map array: a last batch whose window would end past it is
-  // loaded by plain loads.  map_word(b) is the slice's first index within the
-  // window.
-  __device__ __forceinline__ uintptr_t map_lo(int64_t b) const {
-    return reinterpret_cast<uintptr_t>(map + b * E * M3) & ~(uintptr_t)15;
-  }
-  __device__ __forceinline__ uintptr_t map_hi(int64_t b) const {
-    return (reinterpret_cast<uintptr_t>(map + b * E * M3 + (int64_t)cells_of(b) * M3) + 15) &
-           ~(uintptr_t)15;
-  }
-  __device__ __forceinline__ bool map_by_tma(int64_t b) const {
-    return map_ok && map_lo(b) >= reinterpret_cast<uintptr_t>(map) &&
-           map_hi(b) <= reinterpret_cast<uintptr_t>(map + n_cells * M3);
-  }
-  __device__ __forceinline__ int map_word(int64_t b) const {
-    return (int)((reinterpret_cast<uintptr_t>(map + b * E * M3) - map_lo(b)) >> 2);
+  __device__ __forceinline__ bool map_by_tma(int cells) const {
+    return map_ok && L::map_tma && ((cells * M3 * 4) % 16 == 0);
   }
   // a bulk copy needs a 16-byte aligned start and a 16-byte multiple: 4-byte G
   // tiles of an odd number of cells with odd NQ^3 (an odd E, or the last batch)
@@ -404,9 +384,10 @@ struct TmaTilesQ {
     if (gb) bulk_g2s(sG, G + b * E * 6 * Q3, gb, mbar_g);
   }
   __device__ __forceinline__ void issue_map(int64_t b) const {
-    const uint32_t mb = map_by_tma(b) ? (uint32_t)(map_hi(b) - map_lo(b)) : 0u;
+    const int cells = cells_of(b);
+    const uint32_t mb = map_by_tma(cells) ? (uint32_t)(cells * M3 * 4) : 0u;
     mbar_arrive_expect_tx(mbar_m, mb);
-    if (mb) bulk_g2s(sMap, reinterpret_cast<const void *>(map_lo(b)), mb, mbar_m);
+    if (mb) bulk_g2s(sMap, map + b * E * M3, mb, mbar_m);
   }
   // after the G wait: the tile of a batch that had no bulk copy, by plain loads
   // (to be ordered before its readers by a barrier)
@@ -423,11 +404,10 @@ struct TmaTilesQ {
                                          bool has_col = true) const {
     const int cells = cells_of(b);
     const bool valid = has_col && el < cells;
-    const bool mt = map_by_tma(b);
-    const uint32_t *sm = sMap + (mt ? map_word(b) : 0);
+    const bool mt = map_by_tma(cells);
 #pragma unroll
     for (int i = 0; i < NM; ++i) {
-      idx[i] = valid ? (mt ? sm[el * M3 + i * M2 + jk] : __ldg(map + (b * E + el) * M3 + i * M2 + jk))
+      idx[i] = valid ? (mt ? sMap[el * M3 + i * M2 + jk] : __ldg(map + (b * E + el) * M3 + i * M2 + jk))
                      : MFGB_INVALID_DOF;
       raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + idx[i]) : VT(0);
     }
@@ -470,11 +450,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
   constexpr int N2 = N * N, N3 = N * N * N;
   extern __shared__ __align__(128) unsigned char smem[];
   GT *sG = reinterpret_cast<GT *>(smem);
-  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::map_off);
-  V *s_u = reinterpret_cast<V *>(smem + L::work_off);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *s_u = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
   V *s_vs = s_u + E * N3;
   V *s_vt = s_vs + E * N3;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::mbar_off);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
   uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
 
   const int tid = threadIdx.x;
@@ -854,11 +834,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
   constexpr int N2 = N * N, N3 = N * N * N;
   extern __shared__ __align__(128) unsigned char smem[];
   GT *sG = reinterpret_cast<GT *>(smem);
-  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::map_off);
-  V *w0 = reinterpret_cast<V *>(smem + L::work_off);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *w0 = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
   V *w1 = w0 + E * N3;
   V *w2 = w1 + E * N3;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::mbar_off);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
   uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
 
   const int tid = threadIdx.x;
@@ -1201,11 +1181,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
   constexpr int N2 = N * N, N3 = N * N * N;
   extern __shared__ __align__(128) unsigned char smem[];
   GT *sG = reinterpret_cast<GT *>(smem);
-  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::map_off);
-  V *s_u = reinterpret_cast<V *>(smem + L::work_off);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *s_u = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
   V *s_vs = s_u + E * N3;
   V *s_vt = s_vs + E * N3;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::mbar_off);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
   uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
 
   const int tid = threadIdx.x;
@@ -1230,11 +1210,10 @@ __global__ void __launch_bounds__(E * N * N, MB)
   auto indices = [&](int64_t b, uint32_t *idx) {
     const int cells = T.cells_of(b);
     const bool valid = el < cells;
-    const bool mt = T.map_by_tma(b);
-    const uint32_t *sm = sMap + (mt ? T.map_word(b) : 0);
+    const bool mt = T.map_by_tma(cells);
 #pragma unroll
     for (int i = 0; i < N; ++i)
-      idx[i] = valid ? (mt ? sm[el * N3 + i * N2 + jk] : __ldg(map + (b * E + el) * N3 + i * N2 + jk))
+      idx[i] = valid ? (mt ? sMap[el * N3 + i * N2 + jk] : __ldg(map + (b * E + el) * N3 + i * N2 + jk))
                      : MFGB_INVALID_DOF;
   };
   auto gather = [&](const uint32_t *idx, int c, VT *raw) {

@@ -32,8 +32,6 @@
 // A float32 restatement of this arithmetic with its error bound is in
 // tests/test_fx_arith.py.
 #pragma once
-#include <type_traits>
-
 #include "mfgb_bk5.cuh"
 
 namespace mfgb {
@@ -181,11 +179,11 @@ __global__ void __launch_bounds__(E * N * N, MB)
   constexpr int N2 = N * N, N3 = N * N * N;
   extern __shared__ __align__(128) unsigned char smem[];
   float2 *sG = reinterpret_cast<float2 *>(smem);
-  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::map_off);
-  df *s_u = reinterpret_cast<df *>(smem + L::work_off);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  df *s_u = reinterpret_cast<df *>(smem + L::g_bytes + L::map_bytes);
   df *s_vs = s_u + E * N3;
   df *s_vt = s_vs + E * N3;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::mbar_off);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
   uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
   __shared__ int s_emax[2][E];
 
@@ -273,6 +271,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
       T.issue_map(next);
     }
 
+    const bool valid = el < T.cells_of(batch);
     float Djh[N], Djl[N], Dkh[N], Dkl[N];
 #pragma unroll
     for (int m = 0; m < N; ++m) {
@@ -300,12 +299,16 @@ __global__ void __launch_bounds__(E * N * N, MB)
         fx_fma(at, Dkh[m], Dkl[m], b.hi, b.lo);
       }
       const df qr = fx_finish(ar, cr), qs = fx_finish(as, cgj), qt = fx_finish(at, cgk);
-      // ---- metric, bound per point: max |q| times the row sums of |G|.  The
-      // cells past the end of a last batch read whatever the tile holds: their
-      // results stay in their own rows of shared memory and are not scattered.
-      const float2 grr = Gc[0 * N3 + i * N2], grs = Gc[1 * N3 + i * N2],
-                   grt = Gc[2 * N3 + i * N2], gss = Gc[3 * N3 + i * N2],
-                   gst = Gc[4 * N3 + i * N2], gtt = Gc[5 * N3 + i * N2];
+      // ---- metric, bound per point: max |q| times the row sums of |G|
+      float2 grr = make_float2(0.f, 0.f), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+      if (valid) {
+        grr = Gc[0 * N3 + i * N2];
+        grs = Gc[1 * N3 + i * N2];
+        grt = Gc[2 * N3 + i * N2];
+        gss = Gc[3 * N3 + i * N2];
+        gst = Gc[4 * N3 + i * N2];
+        gtt = Gc[5 * N3 + i * N2];
+      }
       const float kq = basis.K * fmaxf(fmaxf(fabsf(qr.hi), fabsf(qs.hi)), fabsf(qt.hi));
       const float Cr = (fabsf(grr.x) + fabsf(grs.x) + fabsf(grt.x)) * kq;
       const float Cs = (fabsf(grs.x) + fabsf(gss.x) + fabsf(gst.x)) * kq;
@@ -324,9 +327,7 @@ __global__ void __launch_bounds__(E * N * N, MB)
       s_vs[el * N3 + i * N2 + jk] = fx_finish(bs, Cs);
       s_vt[el * N3 + i * N2 + jk] = fx_finish(bt, Ct);
     }
-    // barrier C: G tile consumed, s_vs / s_vt ready; whether every cell of the
-    // batch converts its results by the one-addition exponent rebase
-    const bool all_fast = __syncthreads_and(fast_out);
+    __syncthreads();  // barrier C: G tile consumed, s_vs / s_vt ready
     if (tid == 0 && has_next) {
       fence_proxy_async_smem();
       T.issue_g(next);
@@ -361,9 +362,6 @@ __global__ void __launch_bounds__(E * N * N, MB)
     float mr = 0.f;
 #pragma unroll
     for (int m = 0; m < N; ++m) mr = fmaxf(mr, fabsf(vr[m].hi));
-    // one copy of the loop per conversion, chosen once per batch
-    auto transpose = [&](auto fast_tag) {
-      constexpr bool FAST = decltype(fast_tag)::value;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       df ls[N], lt[N];
@@ -388,14 +386,9 @@ __global__ void __launch_bounds__(E * N * N, MB)
       }
       const df y = fx_finish(a, C);
       if (cur[i] != MFGB_INVALID_DOF)
-        atomicAdd(dst + cur[i], FAST ? fx_f2d_fast(y.hi, kout) + fx_f2d_fast(y.lo, kout)
-                                     : fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
+        atomicAdd(dst + cur[i], fast_out ? fx_f2d_fast(y.hi, kout) + fx_f2d_fast(y.lo, kout)
+                                         : fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
     }
-    };
-    if (all_fast)
-      transpose(std::integral_constant<bool, true>{});
-    else
-      transpose(std::integral_constant<bool, false>{});
     // the prefetched gather's largest exponent per cell, once its loads have
     // landed (read after the next barrier A)
     if (has_next) reduce_exp(slot ^ 1);

@@ -266,9 +266,9 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
   constexpr int M2 = NM * NM, Q2 = NQ * NQ, Q3 = NQ * NQ * NQ, MQ = NM * NQ;
   extern __shared__ __align__(128) unsigned char smem[];
   GT *sG = reinterpret_cast<GT *>(smem);
-  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::map_off);
-  V *w0 = reinterpret_cast<V *>(smem + L::work_off);
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::mbar_off);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  V *w0 = reinterpret_cast<V *>(smem + L::g_bytes + L::map_bytes);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
   uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
   __shared__ V sB[NQ * NM], sD[NQ * NQ];
 
