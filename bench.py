@@ -307,7 +307,11 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     err = float(torch.linalg.norm(h_dst.cuda() - dst) / torch.linalg.norm(dst))
     assert err <= 1e-14, err
-    return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk)
+    # the link's own bound for the step: every DoF once each way at the pinned
+    # copy rate with both directions busy
+    from benchmarks_gb300.rates import link_rates
+    link = link_rates(8 * n, 3)
+    return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk, link)
 
 
 def operator_kernel_ms(L, op, d_dst, d_src, arith, sp, stream, steps):
@@ -376,7 +380,7 @@ def degree_sweep(args, degrees=(3, 4, 5, 6, 7, 8), target_dofs=4.0e7):
     return out
 
 
-def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk):
+def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk, link=None):
     w = WORKLOAD
     if rank != 0:
         return
@@ -420,6 +424,12 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
+    if link:
+        bound = world * n / (16 * n / link["both"]) / 1e9  # GDoF/s, 8 B each way a DoF
+        line["e2e"]["link"] = {"h2d_gbs": link["h2d"] / 1e9, "d2h_gbs": link["d2h"] / 1e9,
+                               "both_gbs": link["both"] / 1e9, "bound_gdofs": bound,
+                               "frac": line["e2e"]["value"] / bound,
+                               "call": "mfgb_link_rate (pinned buffers of one vector)"}
     if cpu:
         line["cpu_baseline"] = cpu
     if not args.no_degrees and world == 1 and is_headline():

@@ -93,6 +93,7 @@ def lib():
                                    ctypes.POINTER(SolveInfo), P], I32),
         "mfgb_dot": ([I64, P, P, ctypes.POINTER(D), P], I32),
         "mfgb_pipe_rate": ([I32, I32, I32, ctypes.POINTER(D)], I32),
+        "mfgb_link_rate": ([I32, I64, I32, ctypes.POINTER(D)], I32),
         "mfgb_cell_error_reduction": ([P, P, I32, ctypes.c_uint64, P, P], I32),
         "mfgb_test_fail_allocation": ([I32], I32),
         "mfgb_test_expire_copy_wait": ([I32], I32),

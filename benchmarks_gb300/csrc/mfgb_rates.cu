@@ -1,4 +1,5 @@
-// mfgb_rates.cu -- arithmetic-pipe throughput on the running GPU, the numbers the
+// mfgb_rates.cu -- arithmetic-pipe and host-link throughput on the running GPU,
+// the numbers the
 // operator kernels' choice of arithmetic rests on: FP64 FMA (DFMA), FP32 FMA,
 // FP64 tensor-core MMA (mma.sync m8n8k4 f64, the instruction of the reference's
 // sum_factorization/include/kernels/BK1/cuda_mma_kernels.cuh:94-100) and the
@@ -11,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "mfgb.h"
 #include "mfgb_internal.h"
@@ -145,10 +147,94 @@ __global__ void __launch_bounds__(256) hmma_kernel(int iters, double *out) {
   out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
 }
 
+// 16-byte copy by the SMs (host memory read or written through its device
+// mapping), four independent loads in flight per thread
+__global__ void __launch_bounds__(512) link_copy_kernel(const int4 *__restrict__ s,
+                                                        int4 *__restrict__ d, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t st = (size_t)gridDim.x * blockDim.x;
+  for (; i + 3 * st < n; i += 4 * st) {
+    const int4 a = s[i], b = s[i + st], c = s[i + 2 * st], e = s[i + 3 * st];
+    d[i] = a, d[i + st] = b, d[i + 2 * st] = c, d[i + 3 * st] = e;
+  }
+  for (; i < n; i += st) d[i] = s[i];
+}
+
 }  // namespace
 }  // namespace mfgb
 
 using namespace mfgb;
+
+// Host link throughput with pinned host buffers of `bytes` (a multiple of 16):
+// mode 0 host->device, 1 device->host, 2 both directions at once, by the copy
+// engines (cudaMemcpyAsync); modes 3 / 4 / 5 the same by an SM copy kernel (64
+// CTAs per direction).  *bytes_per_s = bytes moved (both directions summed) per
+// second, best of `reps`.
+extern "C" mfgb_status mfgb_link_rate(int mode, int64_t bytes, int reps, double *bytes_per_s) {
+  if (mode < 0 || mode > 5 || bytes < 16 || bytes % 16 || reps < 1 || !bytes_per_s) {
+    set_error("mfgb_link_rate: invalid argument");
+    return MFGB_ERR_INVALID_ARG;
+  }
+  void *h_a = nullptr, *h_b = nullptr, *d_a = nullptr, *d_b = nullptr;
+  cudaStream_t s0 = nullptr, s1 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, ej = nullptr;
+  mfgb_status st = MFGB_OK;
+  if ((st = cuda_status(cudaHostAlloc(&h_a, bytes, cudaHostAllocDefault), "link host buffer")) ||
+      (st = cuda_status(cudaHostAlloc(&h_b, bytes, cudaHostAllocDefault), "link host buffer")) ||
+      (st = cuda_status(cudaMalloc(&d_a, bytes), "link device buffer")) ||
+      (st = cuda_status(cudaMalloc(&d_b, bytes), "link device buffer")) ||
+      (st = cuda_status(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking), "link stream")) ||
+      (st = cuda_status(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking), "link stream")) ||
+      (st = cuda_status(cudaEventCreate(&e0), "link event")) ||
+      (st = cuda_status(cudaEventCreate(&e1), "link event")) ||
+      (st = cuda_status(cudaEventCreateWithFlags(&ej, cudaEventDisableTiming), "link event"))) {
+  } else {
+    memset(h_a, 0, bytes);
+    const size_t n16 = (size_t)bytes / 16;
+    const bool up = mode == 0 || mode == 2 || mode == 3 || mode == 5;
+    const bool down = mode == 1 || mode == 2 || mode == 4 || mode == 5;
+    const bool sm = mode >= 3;
+    auto once = [&]() {
+      cudaEventRecord(e0, s0);
+      cudaStreamWaitEvent(s1, e0, 0);
+      if (up) {
+        if (sm)
+          link_copy_kernel<<<64, 512, 0, s0>>>((const int4 *)h_a, (int4 *)d_a, n16);
+        else
+          cudaMemcpyAsync(d_a, h_a, bytes, cudaMemcpyHostToDevice, s0);
+      }
+      if (down) {
+        if (sm)
+          link_copy_kernel<<<64, 512, 0, s1>>>((const int4 *)d_b, (int4 *)h_b, n16);
+        else
+          cudaMemcpyAsync(h_b, d_b, bytes, cudaMemcpyDeviceToHost, s1);
+      }
+      cudaEventRecord(ej, s1);
+      cudaStreamWaitEvent(s0, ej, 0);
+      cudaEventRecord(e1, s0);
+      return cudaEventSynchronize(e1);
+    };
+    float best = 0.f;
+    for (int r = -1; r < reps && !st; ++r) {  // one warm-up
+      float ms = 0.f;
+      cudaError_t e = once();
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      st = cuda_status(e, "mfgb_link_rate");
+      if (!st && r >= 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    if (!st) *bytes_per_s = (double)bytes * ((up ? 1 : 0) + (down ? 1 : 0)) / (best * 1e-3);
+  }
+  if (ej) cudaEventDestroy(ej);
+  if (e1) cudaEventDestroy(e1);
+  if (e0) cudaEventDestroy(e0);
+  if (s1) cudaStreamDestroy(s1);
+  if (s0) cudaStreamDestroy(s0);
+  cudaFree(d_b);
+  cudaFree(d_a);
+  cudaFreeHost(h_b);
+  cudaFreeHost(h_a);
+  return st;
+}
 
 // pipe: 0 DFMA, 1 FFMA, 2 DMMA m8n8k4 f64, 3 BF16 mma.sync m16n8k16,
 // 4 packed FFMA2, 5 FFMA + lop3, 6 FFMA2 + lop3.

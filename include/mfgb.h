@@ -406,6 +406,13 @@ mfgb_status mfgb_mlp_infer(const float *d_params, const float *d_X, int64_t n, d
  * these rates. */
 mfgb_status mfgb_pipe_rate(int pipe, int iters, int reps, double *ops_per_s);
 
+/* Host link throughput with pinned host buffers of `bytes` (a multiple of 16):
+ * mode 0 host->device, 1 device->host, 2 both directions at once, by the copy
+ * engines; 3 / 4 / 5 the same by an SM copy kernel.  *bytes_per_s = bytes moved
+ * (both directions summed) per second, best of `reps`.  The bound of
+ * mfgb_vmult_host, which moves every DoF once each way. */
+mfgb_status mfgb_link_rate(int mode, int64_t bytes, int reps, double *bytes_per_s);
+
 /* ---- vector kernels used by the solver (exposed for tests) -------------- */
 /* result[0] = sum a_i b_i (deterministic two-stage reduction) */
 mfgb_status mfgb_dot(int64_t n, const double *d_a, const double *d_b, double *h_result,
