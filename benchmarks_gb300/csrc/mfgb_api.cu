@@ -87,7 +87,8 @@ mfgb_status ensure_df(mfgb_operator *op) {
 
 mfgb_status ensure_fx(mfgb_operator *op) {
   if (op->d_Gfx) return MFGB_OK;
-  const int64_t n3 = (int64_t)op->n * op->n * op->n;
+  const int64_t nq = op->nq > 0 ? op->nq : op->n;  // G points per direction
+  const int64_t n3 = nq * nq * nq;
   mfgb_status st;
   if ((st = dev_alloc((void **)&op->d_Gfx, sizeof(float2) * op->n_cells * 6 * n3,
                       "G (scaled double-float)")) ||
@@ -114,7 +115,9 @@ mfgb_status ensure_arith(mfgb_operator *op, int arith) {
     set_error("operator has no geometric factors");
     return MFGB_ERR_INVALID_ARG;
   }
-  return op->quadrature == 0 && kernel_shape(1, op->n) >= kShapeFx ? ensure_fx(op) : ensure_df(op);
+  // the scaled pairs for GLL collocation (shapes 5 / 6) and the BP3 operator
+  const bool fx = (op->quadrature == 0 && kernel_shape(1, op->n) >= kShapeFx) || op->quadrature == 2;
+  return fx ? ensure_fx(op) : ensure_df(op);
 }
 
 // dst += A src over cells [cell0, cell0 + n) (the map keeps global DoF indices);
@@ -127,6 +130,9 @@ static cudaError_t apply_range(mfgb_operator *op, int64_t cell0, int64_t n, doub
   const uint32_t *map = op->d_map + cell0 * n3;
   if (op->quadrature == 2) {
     if (partials || done) return cudaErrorNotSupported;
+    if (arith == MFGB_ARITH_FP64_DF && op->d_Gfx)
+      return bp3_fx(op->degree, n, map, op->d_Gfx + cell0 * 6 * q3, op->d_Gexp + cell0, src, dst,
+                    op->Bq, op->DG, s);
     return bp3_apply(op->degree, n, map, op->d_Bq, op->d_DGq, op->Bq, op->DG,
                      op->d_G + cell0 * 6 * q3, op->d_Gdf ? op->d_Gdf + cell0 * 6 * q3 : nullptr,
                      src, dst, arith, s);
@@ -337,6 +343,7 @@ mfgb_status range_check_sync(int64_t n, const double *v, int64_t n_cells, int pe
 }
 
 bool uses_fx(const mfgb_operator *op) {
+  if (op->quadrature == 2) return op->d_Gfx != nullptr;
   return op->quadrature == 0 && op->d_Gfx && (kernel_shape(1, op->n) >= kShapeFx || !op->d_Gdf);
 }
 

@@ -130,6 +130,19 @@ def test_bp3_operator_matches_oracle(mf, orc, p, arith):
         assert rel(A.compute_diagonal().cpu().numpy(), dr) <= 1e-13
 
 
+@pytest.mark.parametrize("p", [2, 4, 7])
+def test_bp3_many_batches_match_oracle(mf, orc, p):
+    """More cells than one wave of CTAs (every CTA runs several batches of the
+    pipeline, the last one partial), double-float against the oracle."""
+    cells = {2: (14, 12, 11), 4: (12, 11, 9), 7: (8, 7, 7)}[p]
+    A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.06), quadrature="bp3")
+    ref = orc.GaussProblem(*cells, p, nq=p + 2, amplitude=0.06)
+    src = np.random.default_rng(10 + p).uniform(-1, 1, ref.n_dofs)
+    y = A.initialize_dof_vector()
+    A.vmult(y, torch_from(src), arith="df")
+    assert rel(y.cpu().numpy(), ref.apply(src)) <= 1e-12
+
+
 def test_bp3_cg_counts_match_oracle(mf, orc):
     mesh = mf.BoxMesh(4, 3, 3, degree=3, amplitude=0.05)
     A = mf.LaplaceOperator(mesh, quadrature="bp3")

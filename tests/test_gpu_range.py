@@ -1,6 +1,6 @@
 """Range of the FP64-accurate double-float arithmetic (MFGB_ARITH_FP64_DF).
 
-* GLL collocation operators scale every cell by a power of two: source vectors
+* GLL collocation and BP3 operators scale every cell by a power of two: source vectors
   and geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
   oracle result to the operator's 1e-12 bar.
 * The double-float kernels without per-cell scaling (the Gauss form here, the
@@ -51,6 +51,20 @@ def test_gll_df_carries_any_source_scale(mf, box, scale):
     A.vmult(y, cuda(src * scale), arith="df")
     mf.check_device_errors()
     assert rel(y.cpu().numpy(), want * scale) <= TOL
+
+
+@pytest.mark.parametrize("scale", [2.0 ** -100, 1e-30, 1e30, 2.0 ** 300, 1e-280])
+def test_bp3_df_carries_any_source_scale(mf, orc, scale):
+    """The BP3 operator (QGauss(p+2)) scales every cell like the collocation
+    kernels: any source range meets the 1e-12 bar, exact zeros included."""
+    ref = orc.GaussProblem(3, 3, 2, 3, nq=5, amplitude=0.05)
+    A = mf.LaplaceOperator(mf.BoxMesh(3, 3, 2, degree=3, amplitude=0.05), quadrature="bp3")
+    src = np.random.default_rng(6).uniform(-1, 1, ref.n_dofs)
+    src[::7] = 0.0
+    y = A.initialize_dof_vector()
+    A.vmult(y, cuda(src * scale), arith="df")
+    mf.check_device_errors()
+    assert rel(y.cpu().numpy(), ref.apply(src) * scale) <= TOL
 
 
 @pytest.mark.parametrize("scale", [1e-280, 2.0 ** -960])
