@@ -115,8 +115,10 @@ mfgb_status ensure_arith(mfgb_operator *op, int arith) {
     set_error("operator has no geometric factors");
     return MFGB_ERR_INVALID_ARG;
   }
-  // the scaled pairs for GLL collocation (shapes 5 / 6) and the BP3 operator
-  const bool fx = (op->quadrature == 0 && kernel_shape(1, op->n) >= kShapeFx) || op->quadrature == 2;
+  // the scaled pairs for GLL collocation (shapes 5 / 6), the BP3 operator and
+  // the Gauss p+1 Laplacian without mass term
+  const bool fx = (op->quadrature == 0 && kernel_shape(1, op->n) >= kShapeFx) ||
+                  op->quadrature == 2 || (op->quadrature == 1 && !op->d_JxW);
   return fx ? ensure_fx(op) : ensure_df(op);
 }
 
@@ -128,11 +130,12 @@ static cudaError_t apply_range(mfgb_operator *op, int64_t cell0, int64_t n, doub
   const int64_t n3 = (int64_t)op->n * op->n * op->n;
   const int64_t q3 = (int64_t)op->nq * op->nq * op->nq;
   const uint32_t *map = op->d_map + cell0 * n3;
+  // the Gauss-point forms by the offset-accumulation kernel (no energy partials)
+  if (op->quadrature >= 1 && arith == MFGB_ARITH_FP64_DF && op->d_Gfx && !partials)
+    return bp3_fx(op->degree, op->nq, n, map, op->d_Gfx + cell0 * 6 * q3, op->d_Gexp + cell0, src,
+                  dst, op->Bq, op->DG, s, done);
   if (op->quadrature == 2) {
     if (partials || done) return cudaErrorNotSupported;
-    if (arith == MFGB_ARITH_FP64_DF && op->d_Gfx)
-      return bp3_fx(op->degree, n, map, op->d_Gfx + cell0 * 6 * q3, op->d_Gexp + cell0, src, dst,
-                    op->Bq, op->DG, s);
     return bp3_apply(op->degree, n, map, op->d_Bq, op->d_DGq, op->Bq, op->DG,
                      op->d_G + cell0 * 6 * q3, op->d_Gdf ? op->d_Gdf + cell0 * 6 * q3 : nullptr,
                      src, dst, arith, s);
@@ -343,7 +346,7 @@ mfgb_status range_check_sync(int64_t n, const double *v, int64_t n_cells, int pe
 }
 
 bool uses_fx(const mfgb_operator *op) {
-  if (op->quadrature == 2) return op->d_Gfx != nullptr;
+  if (op->quadrature >= 1) return op->d_Gfx != nullptr;
   return op->quadrature == 0 && op->d_Gfx && (kernel_shape(1, op->n) >= kShapeFx || !op->d_Gdf);
 }
 

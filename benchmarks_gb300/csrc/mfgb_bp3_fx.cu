@@ -1,5 +1,6 @@
-// The FP64-accurate BP3 operator with offset double-float accumulation
-// (mfgb_bp3fx.cuh): basis split and bound factors, launcher.
+// The FP64-accurate BP3 operator and Gauss p+1 Laplacian with offset
+// double-float accumulation (mfgb_bp3fx.cuh): basis split and bound factors,
+// launcher.
 #include <algorithm>
 #include <cmath>
 
@@ -21,7 +22,7 @@ template <int NQ> struct Bp3FxMinBlocks { static constexpr int value = NQ <= 6 ?
 template <int NM, int NQ, bool MT>
 cudaError_t bp3fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
                          const double *src, double *dst, const double *hB, const double *hDG,
-                         cudaStream_t s) {
+                         cudaStream_t s, const int *done) {
   constexpr int E = Bp3FxElems<NQ>::value, MB = Bp3FxMinBlocks<NQ>::value;
   constexpr int threads = E * NQ * NQ;
   constexpr size_t smem = TmaLayoutQ<NM, NQ, E, ArithDF, 4>::total;
@@ -60,26 +61,32 @@ cudaError_t bp3fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, 
   const int64_t batches = (n_cells + E - 1) / E;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(batches, (int64_t)per_sm * num_sms()));
   bp3fx_tma_kernel<NM, NQ, E, MB, MT><<<grid, threads, smem, s>>>(n_cells, map, G, gexp, src, dst,
-                                                                    b, device_error_flag());
+                                                                    b, done, device_error_flag());
   return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t bp3_fx(int degree, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
+cudaError_t bp3_fx(int degree, int nq, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
                    const int *gexp, const double *src, double *dst, const double *hB,
-                   const double *hDG, cudaStream_t s) {
+                   const double *hDG, cudaStream_t s, const int *done) {
   if (n_cells <= 0) return cudaSuccess;
   if (map == nullptr || (reinterpret_cast<uintptr_t>(Gfx) & 15u)) return cudaErrorInvalidValue;
   // bulk copies of the dof-map tiles need a 16-byte aligned map
   const bool mt = (reinterpret_cast<uintptr_t>(map) & 15u) == 0;
-  switch (degree) {
-#define MFGB_BP3FX(P)                                                                      \
-  case P:                                                                                  \
-    return mt ? bp3fx_launch<P + 1, P + 2, true>(n_cells, map, Gfx, gexp, src, dst, hB, hDG, s) \
-              : bp3fx_launch<P + 1, P + 2, false>(n_cells, map, Gfx, gexp, src, dst, hB, hDG, s);
-    MFGB_BP3FX(1) MFGB_BP3FX(2) MFGB_BP3FX(3) MFGB_BP3FX(4) MFGB_BP3FX(5) MFGB_BP3FX(6)
-    MFGB_BP3FX(7) MFGB_BP3FX(8)
+  const int extra = nq - degree - 1;  // 1: BP3 (q = p + 2), 0: Gauss p + 1
+  if (extra != 0 && extra != 1) return cudaErrorInvalidValue;
+  switch (degree * 2 + extra) {
+#define MFGB_BP3FX(P, X)                                                                         \
+  case 2 * P + X:                                                                                \
+    return mt ? bp3fx_launch<P + 1, P + 1 + X, true>(n_cells, map, Gfx, gexp, src, dst, hB, hDG, s, \
+                                                     done)                                        \
+              : bp3fx_launch<P + 1, P + 1 + X, false>(n_cells, map, Gfx, gexp, src, dst, hB, hDG,  \
+                                                      s, done);
+    MFGB_BP3FX(1, 1) MFGB_BP3FX(2, 1) MFGB_BP3FX(3, 1) MFGB_BP3FX(4, 1) MFGB_BP3FX(5, 1)
+    MFGB_BP3FX(6, 1) MFGB_BP3FX(7, 1) MFGB_BP3FX(8, 1)
+    MFGB_BP3FX(1, 0) MFGB_BP3FX(2, 0) MFGB_BP3FX(3, 0) MFGB_BP3FX(4, 0) MFGB_BP3FX(5, 0)
+    MFGB_BP3FX(6, 0) MFGB_BP3FX(7, 0) MFGB_BP3FX(8, 0)
 #undef MFGB_BP3FX
     default: return cudaErrorInvalidValue;
   }

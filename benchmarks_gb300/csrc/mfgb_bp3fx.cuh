@@ -1,6 +1,8 @@
 // mfgb_bp3fx.cuh -- FP64-accurate BP3 operator (L-vector, NM = p + 1 GLL nodes
 // interpolated to NQ = p + 2 Gauss points per direction; reference
-// CEED_bp/include/bk3_kokkos_kernel.h:146-354) on the FP32 pipes with the
+// CEED_bp/include/bk3_kokkos_kernel.h:146-354), and with NQ = p + 1 the Gauss
+// form of the BP5 Laplacian (bakeoff_problems_dealii/include/
+// portable_laplace_operator.h, QGauss(p+1)), on the FP32 pipes with the
 // offset accumulation and per-cell exponent scaling of the collocation kernel
 // (mfgb_bk5fx.cuh), in the bulk-TMA pipeline of bp3_tma_kernel (mfgb_bkq.cuh).
 //
@@ -43,7 +45,9 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
     bp3fx_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
                      const float2 *__restrict__ G, const int *__restrict__ gexp,
                      const double *__restrict__ src, double *__restrict__ dst,
-                     const BasisQFX<NM, NQ> basis, int *__restrict__ err_flag) {
+                     const BasisQFX<NM, NQ> basis, const int *__restrict__ done_flag,
+                     int *__restrict__ err_flag) {
+  if (done_flag != nullptr && *done_flag) return;
   using L = TmaLayoutQ<NM, NQ, E, ArithDF, 4>;
   constexpr int M2 = NM * NM, Q2 = NQ * NQ, Q3 = NQ * NQ * NQ, MQ = NM * NQ;
   extern __shared__ __align__(128) unsigned char smem[];

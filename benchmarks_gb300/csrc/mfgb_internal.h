@@ -124,13 +124,14 @@ int dot_partials_count();
 cudaError_t dot_to_device(int64_t n, const double *a, const double *b, double *partials,
                           double *out, cudaStream_t s);
 
-// BP3 operator with offset double-float accumulation (mfgb_bp3_fx.cu): dst +=
-// A src over n_cells cells, scaled G pairs Gfx[cell][6][nq^3] with per-cell
-// exponent offsets gexp, host copies of the basis hB[q*nm+i] and the Gauss-point
-// derivative hDG[q*nq+m]
-cudaError_t bp3_fx(int degree, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
+// BP3 operator (nq = degree + 2) and Gauss p+1 Laplacian (nq = degree + 1)
+// with offset double-float accumulation (mfgb_bp3_fx.cu): dst += A src over
+// n_cells cells, scaled G pairs Gfx[cell][6][nq^3] with per-cell exponent
+// offsets gexp, host copies of the basis hB[q*nm+i] and the Gauss-point
+// derivative hDG[q*nq+m]; done (may be null): skip when *done is set
+cudaError_t bp3_fx(int degree, int nq, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
                    const int *gexp, const double *src, double *dst, const double *hB,
-                   const double *hDG, cudaStream_t s);
+                   const double *hDG, cudaStream_t s, const int *done);
 // BK1 E-vector mass operator on the FP64 tensor cores (mfgb_bk1_dmma.cu),
 // degree 1..6, the layouts of mfgb_bk1_evector
 cudaError_t bk1_dmma(int degree, int64_t nelmt, const double *basis, const double *JxW,

@@ -1,10 +1,10 @@
 """Range of the FP64-accurate double-float arithmetic (MFGB_ARITH_FP64_DF).
 
-* GLL collocation and BP3 operators scale every cell by a power of two: source vectors
+* GLL collocation, Gauss p+1 and BP3 Laplacians scale every cell by a power of two: source vectors
   and geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
   oracle result to the operator's 1e-12 bar.
-* The double-float kernels without per-cell scaling (the Gauss form here, the
-  E-vector seam) take inputs whose largest magnitude lies in [2^-40, 2^55]:
+* The double-float kernels without per-cell scaling (the Helmholtz form here,
+  the E-vector seam) take inputs whose largest magnitude lies in [2^-40, 2^55]:
   inside it they meet 1e-12, outside it they report MFGB_ERR_RANGE (the seam on
   the call, an operator application through the device error word).
 * A NaN in the right-hand side ends conjugate gradients with MFGB_ERR_NONFINITE.
@@ -95,25 +95,41 @@ def test_gll_df_carries_any_geometry_scale(mf, box, gscale):
         assert rel(y.cpu().numpy(), want_s) <= TOL
 
 
-def test_gauss_df_range_window(mf, orc):
+def test_helmholtz_df_range_window(mf, orc):
+    """The Helmholtz form (mass + stiffness at QGauss(p+1)) keeps the TwoSum
+    kernel without per-cell scaling: inside the window 1e-12, outside it the
+    device range word reports MFGB_ERR_RANGE; native FP64 has no window."""
     from benchmarks_gb300 import MfgbError, _abi
-    ref = orc.GaussProblem(3, 3, 2, 3, amplitude=0.05)
-    A = mf.LaplaceOperator(mf.BoxMesh(3, 3, 2, degree=3, amplitude=0.05), quadrature="gauss")
+    ref = orc.HelmholtzProblem(3, 3, 2, 3, amplitude=0.05)
+    H = mf.HelmholtzOperator(mf.BoxMesh(3, 3, 2, degree=3, amplitude=0.05))
     src = np.random.default_rng(5).uniform(-1, 1, ref.n_dofs)
-    y = A.initialize_dof_vector()
+    y = H.initialize_dof_vector()
     for scale in (2.0 ** -30, 2.0 ** 40):  # inside the window
-        A.vmult(y, cuda(src * scale), arith="df")
+        H.vmult(y, cuda(src * scale), arith="df")
         mf.check_device_errors()
         assert rel(y.cpu().numpy(), ref.apply(src) * scale) <= TOL
     for scale in (2.0 ** -100, 1e-30, 2.0 ** 300):  # outside: reported, not silent
-        A.vmult(y, cuda(src * scale), arith="df")
+        H.vmult(y, cuda(src * scale), arith="df")
         with pytest.raises(MfgbError) as e:
             mf.check_device_errors()
         assert e.value.status == _abi.ERR_RANGE
     mf.check_device_errors()  # the word was cleared
-    A.vmult(y, cuda(src * 1e-30), arith="fp64")  # native FP64 has no window
+    H.vmult(y, cuda(src * 1e-30), arith="fp64")  # native FP64 has no window
     mf.check_device_errors()
     assert rel(y.cpu().numpy(), ref.apply(src) * 1e-30) <= TOL
+
+
+@pytest.mark.parametrize("scale", [2.0 ** -100, 1e-30, 2.0 ** 300])
+def test_gauss_df_carries_any_source_scale(mf, orc, scale):
+    """The Gauss p+1 Laplacian runs the scaled offset-accumulation kernel:
+    any source range meets the 1e-12 bar."""
+    ref = orc.GaussProblem(3, 3, 2, 3, amplitude=0.05)
+    A = mf.LaplaceOperator(mf.BoxMesh(3, 3, 2, degree=3, amplitude=0.05), quadrature="gauss")
+    src = np.random.default_rng(5).uniform(-1, 1, ref.n_dofs)
+    y = A.initialize_dof_vector()
+    A.vmult(y, cuda(src * scale), arith="df")
+    mf.check_device_errors()
+    assert rel(y.cpu().numpy(), ref.apply(src) * scale) <= TOL
 
 
 def test_evector_seam_df_range_is_reported_on_the_call(mf, orc):
