@@ -89,12 +89,13 @@ inline int num_sms() {
   return sms;
 }
 
-// CTAs per SM of one kernel instantiation (queried once)
+// CTAs per SM of one kernel instantiation (queried once).  Sets the kernel's
+// dynamic shared-memory limit to smem: without it, dynamic plus static shared
+// memory above 48 KB fails at launch.
 template <class K>
 int ctas_per_sm(K kernel, int threads, size_t smem) {
   int ps = 0;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 0) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, kernel, threads, smem) != cudaSuccess) {
     cudaGetLastError();
     ps = 0;
