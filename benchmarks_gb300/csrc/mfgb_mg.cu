@@ -394,24 +394,67 @@ mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
     return st;
   }
   double lam = 0;
-  for (int it = 0; it < iters; ++it) {
-    if ((st = cuda_status(dot_to_device(n, v, v, scr, d_nv, nullptr), "lmax |v|"))) return st;
-    k_normalize<<<grid1d(n), T256>>>(n, d_nv, v);  // v *= 1 / |v|
+  // the iterations on a stream of their own; after one plain iteration (which
+  // also runs the kernels' one-time set-up), pairs of iterations (v -> w,
+  // w -> v) are replayed from one CUDA graph: the set-up of a batch of
+  // problems was bound by the launch latency of these small kernels
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    s = nullptr;
+  }
+  struct Stream {
+    cudaStream_t s;
+    ~Stream() { if (s) cudaStreamDestroy(s); }
+  } sg{s};
+  if ((st = cuda_status(cudaDeviceSynchronize(), "lmax set-up"))) return st;
+  auto body = [&](double *vi, double *wo) -> mfgb_status {
+    mfgb_status e;
+    if ((e = cuda_status(dot_to_device(n, vi, vi, scr, d_nv, s), "lmax |v|"))) return e;
+    k_normalize<<<grid1d(n), T256, 0, s>>>(n, d_nv, vi);  // v *= 1 / |v|
     if (prec == 32) {  // the smoother's own FP32 operator, on a float copy
-      k_convert<float, double><<<grid1d(n), T256>>>(n, v, (float *)L.t);
-      if ((st = level_vmult(L.op, 32, L.d, L.t, nullptr))) return st;
-      k_convert<double, float><<<grid1d(n), T256>>>(n, (const float *)L.d, w);
-    } else if ((st = vmult_impl(L.op, w, v, MFGB_ARITH_FP64_DF, nullptr, nullptr, nullptr))) {
-      return st;
+      k_convert<float, double><<<grid1d(n), T256, 0, s>>>(n, vi, (float *)L.t);
+      if ((e = level_vmult(L.op, 32, L.d, L.t, s))) return e;
+      k_convert<double, float><<<grid1d(n), T256, 0, s>>>(n, (const float *)L.d, wo);
+    } else if ((e = vmult_impl(L.op, wo, vi, MFGB_ARITH_FP64_DF, nullptr, nullptr, s))) {
+      return e;
     }
     if (L.op->n_constrained)  // power iteration on the unconstrained block
-      k_set_constrained<double><<<grid1d(L.op->n_constrained), T256>>>(L.op->n_constrained,
-                                                                        L.op->d_constrained, w, 0.0);
-    k_scale_by<double><<<grid1d(n), T256>>>(n, dinv, w);
+      k_set_constrained<double><<<grid1d(L.op->n_constrained), T256, 0, s>>>(
+          L.op->n_constrained, L.op->d_constrained, wo, 0.0);
+    k_scale_by<double><<<grid1d(n), T256, 0, s>>>(n, dinv, wo);
     // Rayleigh quotient (|v| = 1)
-    if ((st = cuda_status(dot_to_device(n, v, w, scr, d_vw, nullptr), "lmax v.w"))) return st;
+    return cuda_status(dot_to_device(n, vi, wo, scr, d_vw, s), "lmax v.w");
+  };
+  int it = 0;
+  if (iters > 0) {
+    if ((st = body(v, w))) return st;
+    std::swap(v, w);
+    ++it;
+  }
+  if (s && iters - it >= 2) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      mfgb_status b = body(v, w);
+      if (!b) b = body(w, v);
+      const cudaError_t ec = cudaStreamEndCapture(s, &g);
+      if (!b && ec == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
+        for (; it + 2 <= iters; it += 2)
+          if ((st = cuda_status(cudaGraphLaunch(ge, s), "lmax graph"))) break;
+        if (!st) st = cuda_status(cudaStreamSynchronize(s), "lmax graph");
+      }
+      if (ge) cudaGraphExecDestroy(ge);
+      if (g) cudaGraphDestroy(g);
+    }
+    cudaGetLastError();  // a capture that did not work leaves the plain loop below
+    if (st) return st;
+  }
+  for (; it < iters; ++it) {
+    if ((st = body(v, w))) return st;
     std::swap(v, w);
   }
+  if ((st = cuda_status(s ? cudaStreamSynchronize(s) : cudaDeviceSynchronize(), "lmax"))) return st;
   fr.a = v; fr.b = w;
   if (iters > 0 &&
       (st = cuda_status(cudaMemcpy(&lam, d_vw, sizeof(double), cudaMemcpyDeviceToHost), "lmax")))
