@@ -189,6 +189,43 @@ __global__ void __launch_bounds__(T256)
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// ---- power iterations for lambda_max(Dinv A) of every part of a depth -------
+// (the single-problem estimate of mfgb_mg.cu on all parts at once; per-part
+// sums accumulate by atomics into acc[part])
+__global__ void __launch_bounds__(T256)
+    kb_pi_start(const Chunk *__restrict__ ch, const int64_t *__restrict__ poff, double *__restrict__ v) {
+  CHUNK_LOOP(c, t) v[t] = power_start_value((uint64_t)(t - poff[c.part]));
+}
+
+__global__ void __launch_bounds__(T256)
+    kb_pi_dot(const Chunk *__restrict__ ch, const double *__restrict__ a,
+              const double *__restrict__ b, double *__restrict__ acc) {
+  __shared__ double sh[T256 / 32];
+  double s = 0;
+  CHUNK_LOOP(c, t) s = fma(a[t], b[t], s);
+  s = cta_sum(s, sh);
+  if (threadIdx.x == 0) atomicAdd(acc + ch[blockIdx.x].part, s);
+}
+
+// v /= |v| per part (the single-problem normalisation), and its float copy
+__global__ void __launch_bounds__(T256)
+    kb_pi_normalize(const Chunk *__restrict__ ch, const double *__restrict__ nv,
+                    double *__restrict__ v, float *__restrict__ vf) {
+  const double q = nv[ch[blockIdx.x].part];
+  const double a = (q > 0 ? 1.0 / sqrt(q) : 0.0) - 1.0;
+  CHUNK_LOOP(c, t) {
+    v[t] += a * v[t];
+    vf[t] = (float)v[t];
+  }
+}
+
+// w = Dinv (A v) from the FP32 apply
+__global__ void __launch_bounds__(T256)
+    kb_pi_post(const Chunk *__restrict__ ch, const float *__restrict__ av,
+               const float *__restrict__ inv_diag, double *__restrict__ w) {
+  CHUNK_LOOP(c, t) w[t] = (double)av[t] * (double)inv_diag[t];
+}
+
 // CTA b handles problem pid[b]: the sum of its chunk partials cbeg[b] .. cbeg[b+1]
 __device__ __forceinline__ double problem_sum(const int *__restrict__ cbeg,
                                               const double *__restrict__ part, double *sh) {
@@ -963,7 +1000,7 @@ mfgb_status build_batch(mfgb_batch *B, const mfgb_box_desc *boxes, int n,
   mfgb_mg_params p1 = *prm;
   for (int i = 0; i < n; ++i) {
     mfgb_mg *mg = nullptr;
-    if ((st = mfgb_mg_setup(&boxes[i], &p1, &mg))) return st;
+    if ((st = mg_setup_without_lmax(&boxes[i], &p1, &mg))) return st;
     struct Guard { mfgb_mg *m; ~Guard() { mfgb_mg_destroy(m); } } guard{mg};
     if (mg->levels.size() != part_at[i].size()) {
       set_error("mfgb_batch_create: level plan mismatch");
@@ -1054,6 +1091,49 @@ mfgb_status build_batch(mfgb_batch *B, const mfgb_box_desc *boxes, int n,
       }
     }
     if ((st = cuda_status(cudaDeviceSynchronize(), "batch copy"))) return st;
+  }
+  // ---- lambda_max of every smoothed part: one power iteration per depth -----
+  // over all its parts (the start, normalisation, FP32 operator, constrained
+  // rows and Jacobi scaling of the single-problem estimate)
+  for (size_t l = 0; l < B->depth.size(); ++l) {
+    Depth &D = B->depth[l];
+    if (!D.n_cheb) continue;
+    const int np = (int)D.parts.size();
+    std::vector<int64_t> poff(np);
+    for (int k = 0; k < np; ++k) poff[k] = D.parts[k].off;
+    int64_t *d_poff = nullptr;
+    double *acc = nullptr;  // [2][np]: |v|^2, v.w
+    if ((st = upload(&d_poff, poff)) || (st = dalloc((void **)&acc, sizeof(double) * 2 * np))) {
+      cudaFree(d_poff);
+      return st;
+    }
+    struct Free2 { void *a, *b; ~Free2() { cudaFree(a); cudaFree(b); } } f2{d_poff, acc};
+    double *v = B->r, *w = B->z;  // depth-0-sized FP64 work vectors, free until the first solve
+    DepthPlan DP;
+    DP.groups = D.groups;
+    DP.d_cons = D.d_cons;
+    DP.n_cons = D.n_cons;
+    if ((st = cuda_status(cudaMemset(D.t, 0, sizeof(float) * D.n), "batch lmax"))) return st;
+    kb_pi_start<<<D.n_cheb, T256>>>(D.d_cheb, d_poff, v);
+    if (D.n_cons) k_set_constrained<double><<<grid1d(D.n_cons), T256>>>(D.n_cons, D.d_cons, v, 0.0);
+    for (int it = 0; it < prm->eig_iterations && !st; ++it) {
+      cudaMemsetAsync(acc, 0, sizeof(double) * 2 * np, nullptr);
+      kb_pi_dot<<<D.n_cheb, T256>>>(D.d_cheb, v, v, acc);
+      kb_pi_normalize<<<D.n_cheb, T256>>>(D.d_cheb, acc, v, D.t);
+      if ((st = apply32(D, DP, D.t, D.d, nullptr))) break;
+      kb_pi_post<<<D.n_cheb, T256>>>(D.d_cheb, D.d, D.inv_diag, w);
+      if (D.n_cons) k_set_constrained<double><<<grid1d(D.n_cons), T256>>>(D.n_cons, D.d_cons, w, 0.0);
+      kb_pi_dot<<<D.n_cheb, T256>>>(D.d_cheb, v, w, acc + np);
+      std::swap(v, w);
+    }
+    if (st) return st;
+    std::vector<double> lam(np, 0.0);
+    if ((st = cuda_status(cudaMemcpy(lam.data(), acc + np, sizeof(double) * np,
+                                     cudaMemcpyDeviceToHost),
+                          "batch lmax")))
+      return st;
+    for (int k = 0; k < np; ++k)
+      if (D.parts[k].kind != 0) D.parts[k].lmax = 1.2 * lam[k];
   }
   // ---- Chebyshev coefficients per part (the single-problem recurrence) ------
   for (auto &D : B->depth) {

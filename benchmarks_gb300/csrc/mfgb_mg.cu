@@ -358,12 +358,6 @@ __global__ void k_normalize(int64_t n, const double *__restrict__ nv, double *__
 mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
                           const double *dinv_given = nullptr) {
   const int64_t n = L.n;
-  std::vector<double> h(n);
-  uint64_t st64 = 0x9E3779B97F4A7C15ull;
-  for (int64_t i = 0; i < n; ++i) {  // deterministic pseudo-random start
-    st64 ^= st64 << 13; st64 ^= st64 >> 7; st64 ^= st64 << 17;
-    h[i] = 0.5 + (double)(st64 >> 11) * (1.0 / 9007199254740992.0);
-  }
   // scratch: dot partials, then |v|^2 and the Rayleigh quotient (device scalars:
   // the iteration runs without host synchronisation, one read at the end)
   const int np = dot_partials_count();
@@ -380,8 +374,7 @@ mfgb_status estimate_lmax(MgLevel &L, int prec, int iters, double *lmax,
     ~Free() { cudaFree(a); cudaFree(b); cudaFree(c); cudaFree(d); }
   } fr{v, w, dinv, scr};
   double *d_nv = scr + np, *d_vw = scr + np + 1;
-  if ((st = cuda_status(cudaMemcpy(v, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "lmax init")))
-    return st;
+  k_power_start<<<grid1d(n), T256>>>(n, v);  // deterministic pseudo-random start
   if (L.op->n_constrained)
     k_set_constrained<double><<<grid1d(L.op->n_constrained), T256>>>(L.op->n_constrained,
                                                                       L.op->d_constrained, v, 0.0);
@@ -483,7 +476,7 @@ void free_mg(mfgb_mg *mg) {
 using namespace mfgb;
 
 static mfgb_status mg_setup_impl(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
-                                 mfgb_mg **out, mfgb_operator *fine_op);
+                                 mfgb_mg **out, mfgb_operator *fine_op, bool lmax = true);
 
 extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
                                      mfgb_mg **out) {
@@ -492,6 +485,15 @@ extern "C" mfgb_status mfgb_mg_setup(const mfgb_box_desc *fine, const mfgb_mg_pa
 
 // The finest level borrows the caller's operator (its geometric factors are
 // not computed a second time); the operator must outlive the hierarchy.
+namespace mfgb {
+// the hierarchy without the lambda_max estimates (levels[l].lmax = 0): the
+// batched set-up estimates them for all problems at once
+mfgb_status mg_setup_without_lmax(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
+                                  mfgb_mg **out) {
+  return mg_setup_impl(fine, prm, out, nullptr, false);
+}
+}  // namespace mfgb
+
 extern "C" mfgb_status mfgb_mg_setup_shared(const mfgb_operator *fine_op,
                                             const mfgb_mg_params *prm, mfgb_mg **out) {
   if (!fine_op || !fine_op->is_box || fine_op->quadrature != 0 ||
@@ -505,7 +507,7 @@ extern "C" mfgb_status mfgb_mg_setup_shared(const mfgb_operator *fine_op,
 }
 
 static mfgb_status mg_setup_impl(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
-                                 mfgb_mg **out, mfgb_operator *fine_op) {
+                                 mfgb_mg **out, mfgb_operator *fine_op, bool lmax) {
   if (!fine || !prm || !out || (prm->precision != 32 && prm->precision != 64) ||
       prm->chebyshev_degree < 1 || prm->smoothing_range <= 1.0 || prm->eig_iterations < 1 ||
       prm->coarse_cells < 1) {
@@ -573,7 +575,7 @@ static mfgb_status mg_setup_impl(const mfgb_box_desc *fine, const mfgb_mg_params
       }
       if ((st = cuda_status(cudaDeviceSynchronize(), "valence"))) break;
     }
-    if (M.to_coarse != 0) {
+    if (M.to_coarse != 0 && lmax) {
       double lam = 0;
       if ((st = estimate_lmax(M, prm->precision, prm->eig_iterations, &lam))) break;
       M.lmax = 1.2 * lam;

@@ -35,6 +35,10 @@ mfgb_status ensure_g32(mfgb_operator *op);
 // coarse_cells; kinds[l] = 1 (p-transfer to l+1), 2 (h-transfer), 0 (coarsest)
 void mg_plan_levels(const mfgb_box_desc &fine, int coarse_cells, std::vector<mfgb_box_desc> &boxes,
                     std::vector<int> &kinds, std::vector<int> &strides);
+// mfgb_mg_setup without the lambda_max power iterations (every level's lmax
+// stays 0): the batched set-up runs them for all its problems at once
+mfgb_status mg_setup_without_lmax(const mfgb_box_desc *fine, const mfgb_mg_params *prm,
+                                  mfgb_mg **out);
 
 }  // namespace mfgb
 

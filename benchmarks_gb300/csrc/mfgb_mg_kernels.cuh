@@ -22,6 +22,21 @@ inline unsigned grid1d(int64_t n) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (n); \
        t += (int64_t)gridDim.x * blockDim.x)
 
+// Start vector of the lambda_max power iterations, entry i of a level:
+// 0.5 + U[0, 1) from SplitMix64 (Steele, Lea, Flood 2014) of i, so that the
+// batched set-up can generate every problem's start on the GPU in parallel.
+__device__ __forceinline__ double power_start_value(uint64_t i) {
+  uint64_t z = (i + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return 0.5 + (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__global__ void k_power_start(int64_t n, double *v) {
+  GRID_STRIDE(t, n) v[t] = power_start_value((uint64_t)t);
+}
+
 template <class T>
 __global__ void k_fill(int64_t n, T *x, T v) {
   GRID_STRIDE(t, n) x[t] = v;

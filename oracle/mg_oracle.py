@@ -26,16 +26,16 @@ from . import oracle as orc
 
 
 def _power_start(n: int) -> np.ndarray:
-    """The deterministic xorshift64 start vector the library uses."""
-    s = 0x9E3779B97F4A7C15
-    out = np.empty(n)
-    mask = (1 << 64) - 1
-    for i in range(n):
-        s ^= (s << 13) & mask
-        s ^= s >> 7
-        s ^= (s << 17) & mask
-        out[i] = 0.5 + (s >> 11) * (1.0 / 9007199254740992.0)
-    return out
+    """The deterministic start vector the library uses: entry i is 0.5 + the top
+    53 bits of SplitMix64 (Steele, Lea, Flood 2014) of the state (i + 1) * golden
+    as a fraction of 2^53 (power_start_value, mfgb_mg_kernels.cuh)."""
+    z = np.arange(1, n + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = z * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    z = z ^ (z >> np.uint64(31))
+    return 0.5 + (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
 
 
 class Level:
