@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "mfgb_bk1fx.cuh"
 #include "mfgb_bp3fx.cuh"
 #include "mfgb_internal.h"
 #include "mfgb_launch.cuh"
@@ -19,22 +20,18 @@ template <int NQ> struct Bp3FxElems {
 };
 template <int NQ> struct Bp3FxMinBlocks { static constexpr int value = NQ <= 6 ? 2 : 1; };
 
-template <int NM, int NQ, bool MT>
-cudaError_t bp3fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
-                         const double *src, double *dst, const double *hB, const double *hDG,
-                         cudaStream_t s, const int *done) {
-  constexpr int E = Bp3FxElems<NQ>::value, MB = Bp3FxMinBlocks<NQ>::value;
-  constexpr int threads = E * NQ * NQ;
-  constexpr size_t smem = TmaLayoutQ<NM, NQ, E, ArithDF, 4>::total;
-  BasisQFX<NM, NQ> b;
+// B (and D, when given) as float pairs with the bound factors of the offset
+// accumulation: K = 2 (1 + 2^-20) times the row and column sums of |B|, |D|
+template <int NM, int NQ>
+void fill_basis(const double *hB, const double *hDG, BasisQFX<NM, NQ> &b) {
   const double K = 2.0 * (1.0 + std::ldexp(1.0, -20));
   for (int t = 0; t < NQ * NM; ++t) {
     b.Bh[t] = (float)hB[t];
     b.Bl[t] = (float)(hB[t] - (double)b.Bh[t]);
   }
   for (int t = 0; t < NQ * NQ; ++t) {
-    b.Dh[t] = (float)hDG[t];
-    b.Dl[t] = (float)(hDG[t] - (double)b.Dh[t]);
+    b.Dh[t] = hDG ? (float)hDG[t] : 0.f;
+    b.Dl[t] = hDG ? (float)(hDG[t] - (double)b.Dh[t]) : 0.f;
   }
   double LB = 0.0;
   for (int q = 0; q < NQ; ++q) {
@@ -56,6 +53,17 @@ cudaError_t bp3fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, 
   }
   b.LB = (float)(LB * (1.0 + std::ldexp(1.0, -20)));
   b.K = (float)K;
+}
+
+template <int NM, int NQ, bool MT>
+cudaError_t bp3fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
+                         const double *src, double *dst, const double *hB, const double *hDG,
+                         cudaStream_t s, const int *done) {
+  constexpr int E = Bp3FxElems<NQ>::value, MB = Bp3FxMinBlocks<NQ>::value;
+  constexpr int threads = E * NQ * NQ;
+  constexpr size_t smem = TmaLayoutQ<NM, NQ, E, ArithDF, 4>::total;
+  BasisQFX<NM, NQ> b;
+  fill_basis(hB, hDG, b);
   static int per_sm = -1;
   if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bp3fx_tma_kernel<NM, NQ, E, MB, MT>, threads, smem));
   const int64_t batches = (n_cells + E - 1) / E;
@@ -65,7 +73,35 @@ cudaError_t bp3fx_launch(int64_t n_cells, const uint32_t *map, const float2 *G, 
   return cudaGetLastError();
 }
 
+template <int NM, int NQ>
+cudaError_t bk1fx_launch(int64_t nelmt, const double *in, const double *JxW, double *out,
+                         const double *hB, cudaStream_t s) {
+  constexpr int E = Bp3FxElems<NQ>::value, MB = Bp3FxMinBlocks<NQ>::value;
+  constexpr int threads = E * NQ * NQ;
+  BasisQFX<NM, NQ> b;
+  fill_basis(hB, nullptr, b);
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk1fx_kernel<NM, NQ, E, MB>, threads, 0));
+  const int64_t batches = (nelmt + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(batches, (int64_t)per_sm * num_sms()));
+  bk1fx_kernel<NM, NQ, E, MB><<<grid, threads, 0, s>>>(nelmt, in, JxW, out, b);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t bk1_fx(int degree, int64_t nelmt, const double *in, const double *JxW, double *out,
+                   const double *hB, cudaStream_t s) {
+  if (nelmt <= 0) return cudaSuccess;
+  switch (degree) {
+#define MFGB_BK1FX(P) \
+  case P: return bk1fx_launch<P + 1, P + 2>(nelmt, in, JxW, out, hB, s);
+    MFGB_BK1FX(1) MFGB_BK1FX(2) MFGB_BK1FX(3) MFGB_BK1FX(4) MFGB_BK1FX(5) MFGB_BK1FX(6)
+    MFGB_BK1FX(7) MFGB_BK1FX(8)
+#undef MFGB_BK1FX
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t bp3_fx(int degree, int nq, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
                    const int *gexp, const double *src, double *dst, const double *hB,

@@ -132,6 +132,11 @@ cudaError_t dot_to_device(int64_t n, const double *a, const double *b, double *p
 cudaError_t bp3_fx(int degree, int nq, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
                    const int *gexp, const double *src, double *dst, const double *hB,
                    const double *hDG, cudaStream_t s, const int *done);
+// CEED BK1 mass operator on E-vectors with offset double-float accumulation and
+// per-element scaling (mfgb_bp3_fx.cu): out = B^T (JxW o B in) per element,
+// host copy of the basis hB[q*nm+i], nq = degree + 2
+cudaError_t bk1_fx(int degree, int64_t nelmt, const double *in, const double *JxW, double *out,
+                   const double *hB, cudaStream_t s);
 // BK1 E-vector mass operator on the FP64 tensor cores (mfgb_bk1_dmma.cu),
 // degree 1..6, the layouts of mfgb_bk1_evector
 cudaError_t bk1_dmma(int degree, int64_t nelmt, const double *basis, const double *JxW,

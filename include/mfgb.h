@@ -41,9 +41,9 @@ enum {
    significant bits; 1e-12 relative against FP64 on the operator).  On GLL
    collocation operators (shapes 5 / 6 of the kernel shape table, the default
    at every degree), the Gauss p+1 Laplacian and the BP3 operator every cell is
-   scaled by a power of two, so any FP64 input range is carried.  Elsewhere (the
-   Helmholtz form, BK6, the kernel seams, shapes 0-4) inputs must lie in the
-   window of MFGB_ERR_RANGE: the operator's own
+   scaled by a power of two, so any FP64 input range is carried (so is the BK1
+   seam, per element).  Elsewhere (the Helmholtz form, BK6, the BK3 and BK5
+   seams, shapes 0-4) inputs must lie in the window of MFGB_ERR_RANGE: the operator's own
    geometric factors are checked when their pairs are built (the call returns
    MFGB_ERR_RANGE), caller-supplied G and vectors of the seams on every call,
    and the source vectors of operator applications on the device (reported by
@@ -216,8 +216,9 @@ mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, 
    out_e = B^T (JxW_e o (B x B x B) in_e); d_basis[q*nm + i], d_JxW[e][nq^3],
    d_in/d_out[e][nm^3], point and mode indices with direction 0 slowest (the
    reference serial kernel's order, CEED_BK/include/kernels/BK1/serial_kernels.hpp;
-   its CUDA kernel indexes JxW with direction 2 slowest).  arith FP64, FP64_DF,
-   or FP64_TC (degree 1..6: the six 1D contractions as 8x8x4 FP64 tensor-core
+   its CUDA kernel indexes JxW with direction 2 slowest).  arith FP64, FP64_DF
+   (offset double-float with every element's input and JxW scaled by a power of
+   two: any FP64 range), or FP64_TC (degree 1..6: the six 1D contractions as 8x8x4 FP64 tensor-core
    tiles, one warp per element, the comparison of the reference's
    sum_factorization/include/kernels/BK1/templated_cuda_mma_kernels.cuh). */
 mfgb_status mfgb_bk1_evector(int degree, int64_t nelmt, const double *d_basis, const double *d_JxW,

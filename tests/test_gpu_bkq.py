@@ -112,6 +112,28 @@ def test_bk1_tensor_cores_large_grid(mf):
     assert float(d.max()) <= 1e-12
 
 
+@pytest.mark.parametrize("p", [2, 5, 8])
+def test_bk1_df_carries_any_scale(mf, orc, p):
+    """The double-float BK1 seam scales every element's input and JxW by powers
+    of two: inputs and weights far outside the float range, and exact zeros,
+    meet the 1e-12 bar."""
+    import torch
+    nq, nm = p + 2, p + 1
+    g = np.random.default_rng(40 + p)
+    nel = 53
+    xg, _ = orc.gll(nm)
+    xq, _ = orc.gauss(nq)
+    basis = orc.interpolation_matrix(xg, xq)
+    jxw = g.uniform(0.5, 2.0, nel * nq ** 3)
+    u = g.uniform(-1, 1, nel * nm ** 3)
+    u[::9] = 0.0
+    want = orc.bk1_evector(nm, nq, basis, jxw, u)
+    for su, sj in ((1e-280, 1.0), (2.0 ** 300, 2.0 ** -100), (1e-30, 1e30)):
+        y = torch.zeros(u.size, dtype=torch.float64, device="cuda")
+        mf.bk1_evector(p, cuda(basis), cuda(jxw * sj), cuda(u * su), y, arith="df")
+        assert rel(y.cpu().numpy(), want * su * sj) <= 1e-12
+
+
 def test_bk_verification_norms_on_gpu(mf, golden13):
     import torch
     p, nel = 4, 1000
