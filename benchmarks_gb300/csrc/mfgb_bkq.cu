@@ -67,16 +67,24 @@ mfgb_status bkq_entry(const char *name, bool laplace, int degree, int64_t nelmt,
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64_TC)
     return cuda_status(bk1_dmma(degree, nelmt, basis, coef, in, out, s), name);
-  if (arith == MFGB_ARITH_FP64_DF && !laplace) {
-    // the mass operator with per-element scaling: any input range, no check
+  if (arith == MFGB_ARITH_FP64_DF &&
+      (!laplace || (reinterpret_cast<uintptr_t>(coef) & 15u) == 0)) {
+    // offset double-float with per-element scaling: any input range, no check
+    // (the BK3 kernel's bulk copies of G need a 16-byte aligned array)
     const int nm = degree + 1, nq = degree + 2;
-    double hB[100];
+    double hB[100], hD[100];
     mfgb_status st = cuda_status(cudaMemcpyAsync(hB, basis, sizeof(double) * nq * nm,
                                                  cudaMemcpyDeviceToHost, s),
                                  "basis");
+    if (!st && laplace)
+      st = cuda_status(cudaMemcpyAsync(hD, dbasis, sizeof(double) * nq * nq,
+                                       cudaMemcpyDeviceToHost, s),
+                       "derivative");
     if (!st) st = cuda_status(cudaStreamSynchronize(s), "basis");
     if (st) return st;
-    return cuda_status(bk1_fx(degree, nelmt, in, coef, out, hB, s), name);
+    return cuda_status(laplace ? bk3_fx(degree, nelmt, coef, in, out, hB, hD, s)
+                               : bk1_fx(degree, nelmt, in, coef, out, hB, s),
+                       name);
   }
   if (arith == MFGB_ARITH_FP64_DF) {
     // the double-float range of the inputs and of the caller's coefficients,

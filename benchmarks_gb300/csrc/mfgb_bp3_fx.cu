@@ -5,6 +5,7 @@
 #include <cmath>
 
 #include "mfgb_bk1fx.cuh"
+#include "mfgb_bk3fx.cuh"
 #include "mfgb_bp3fx.cuh"
 #include "mfgb_internal.h"
 #include "mfgb_launch.cuh"
@@ -88,7 +89,38 @@ cudaError_t bk1fx_launch(int64_t nelmt, const double *in, const double *JxW, dou
   return cudaGetLastError();
 }
 
+template <int NM, int NQ>
+cudaError_t bk3fx_launch(int64_t nelmt, const double *G, const double *in, double *out,
+                         const double *hB, const double *hDG, cudaStream_t s) {
+  constexpr int E = Bp3FxElems<NQ>::value, MB = Bp3FxMinBlocks<NQ>::value;
+  constexpr int threads = E * NQ * NQ;
+  constexpr size_t smem = TmaLayoutQ<NM, NQ, E, ArithF64, 4>::total;
+  BasisQFX<NM, NQ> b;
+  fill_basis(hB, hDG, b);
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk3fx_tma_kernel<NM, NQ, E, MB>, threads, smem));
+  const int64_t batches = (nelmt + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(batches, (int64_t)per_sm * num_sms()));
+  bk3fx_tma_kernel<NM, NQ, E, MB><<<grid, threads, smem, s>>>(nelmt, G, in, out, b,
+                                                               device_error_flag());
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t bk3_fx(int degree, int64_t nelmt, const double *G, const double *in, double *out,
+                   const double *hB, const double *hDG, cudaStream_t s) {
+  if (nelmt <= 0) return cudaSuccess;
+  if (reinterpret_cast<uintptr_t>(G) & 15u) return cudaErrorInvalidValue;  // bulk copies
+  switch (degree) {
+#define MFGB_BK3FX(P) \
+  case P: return bk3fx_launch<P + 1, P + 2>(nelmt, G, in, out, hB, hDG, s);
+    MFGB_BK3FX(1) MFGB_BK3FX(2) MFGB_BK3FX(3) MFGB_BK3FX(4) MFGB_BK3FX(5) MFGB_BK3FX(6)
+    MFGB_BK3FX(7) MFGB_BK3FX(8)
+#undef MFGB_BK3FX
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t bk1_fx(int degree, int64_t nelmt, const double *in, const double *JxW, double *out,
                    const double *hB, cudaStream_t s) {

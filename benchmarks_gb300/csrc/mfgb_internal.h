@@ -137,6 +137,11 @@ cudaError_t bp3_fx(int degree, int nq, int64_t n_cells, const uint32_t *map, con
 // host copy of the basis hB[q*nm+i], nq = degree + 2
 cudaError_t bk1_fx(int degree, int64_t nelmt, const double *in, const double *JxW, double *out,
                    const double *hB, cudaStream_t s);
+// CEED BK3 Laplacian on E-vectors with offset double-float accumulation and
+// per-element scaling of the input and of the caller's FP64 G[e][6][nq^3]
+// (16-byte aligned; mfgb_bp3_fx.cu), nq = degree + 2
+cudaError_t bk3_fx(int degree, int64_t nelmt, const double *G, const double *in, double *out,
+                   const double *hB, const double *hDG, cudaStream_t s);
 // BK1 E-vector mass operator on the FP64 tensor cores (mfgb_bk1_dmma.cu),
 // degree 1..6, the layouts of mfgb_bk1_evector
 cudaError_t bk1_dmma(int degree, int64_t nelmt, const double *basis, const double *JxW,

@@ -24,7 +24,12 @@ def cuda(a):
 
 
 def rel(a, b):
-    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    """|a - b| / |b|, both divided by max|b| first: the squares inside the norms
+    of vectors near 1e-280 would underflow to zero"""
+    m = float(np.max(np.abs(b)))
+    if m == 0.0:
+        return float(np.max(np.abs(a)))
+    return float(np.linalg.norm((a - b) / m) / np.linalg.norm(b / m))
 
 
 @pytest.mark.parametrize("arith", ["fp64", "df"])
@@ -132,6 +137,32 @@ def test_bk1_df_carries_any_scale(mf, orc, p):
         y = torch.zeros(u.size, dtype=torch.float64, device="cuda")
         mf.bk1_evector(p, cuda(basis), cuda(jxw * sj), cuda(u * su), y, arith="df")
         assert rel(y.cpu().numpy(), want * su * sj) <= 1e-12
+
+
+@pytest.mark.parametrize("p", [2, 5, 8])
+def test_bk3_df_carries_any_scale(mf, orc, p):
+    """The double-float BK3 seam scales every element's input and G by powers
+    of two: both far outside the float range meet the 1e-12 bar."""
+    import torch
+    nq, nm = p + 2, p + 1
+    g = np.random.default_rng(50 + p)
+    nel = 41
+    xg, _ = orc.gll(nm)
+    xq, _ = orc.gauss(nq)
+    basis = orc.interpolation_matrix(xg, xq)
+    dbasis = orc.derivative_matrix(xq)
+    G = g.uniform(-0.3, 0.3, (nel, 6, nq ** 3))
+    G[:, 0] += 2.0
+    G[:, 3] += 2.0
+    G[:, 5] += 2.0
+    u = g.uniform(-1, 1, nel * nm ** 3)
+    u[::11] = 0.0
+    want = orc.bk3_evector(nm, nq, basis, dbasis, G.reshape(-1), u)
+    for su, sg in ((1e-280, 1.0), (2.0 ** 300, 2.0 ** -100), (1e-30, 1e30)):
+        y = torch.zeros(u.size, dtype=torch.float64, device="cuda")
+        mf.bk3_evector(p, cuda(basis), cuda(dbasis), cuda(G.reshape(-1) * sg), cuda(u * su), y,
+                       arith="df")
+        assert rel(y.cpu().numpy(), want * su * sg) <= 1e-12
 
 
 def test_bk_verification_norms_on_gpu(mf, golden13):

@@ -28,7 +28,12 @@ def mf():
 
 
 def rel(a, b):
-    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+    """|a - b| / |b|, both divided by max|b| first: the squares inside the norms
+    of vectors near 1e-280 would underflow to zero"""
+    m = float(np.max(np.abs(b)))
+    if m == 0.0:
+        return float(np.max(np.abs(a)))
+    return float(np.linalg.norm((a - b) / m) / np.linalg.norm(b / m))
 
 
 def cuda(a):
