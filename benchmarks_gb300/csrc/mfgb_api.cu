@@ -762,7 +762,10 @@ mfgb_status mfgb_bk5_evector(int degree, int64_t nelmt, const double *d_dbasis, 
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64)
     e = bk5_f64(degree + 1, nelmt, nullptr, d_G, d_in, d_out, D, nullptr, nullptr, s);
-  else if (arith == MFGB_ARITH_FP64_DF) {
+  else if (arith == MFGB_ARITH_FP64_DF && (reinterpret_cast<uintptr_t>(d_G) & 15u) == 0) {
+    // offset double-float with per-element scaling: any input range, no check
+    e = bk5_fx_evec(degree + 1, nelmt, d_G, d_in, d_out, D, s);
+  } else if (arith == MFGB_ARITH_FP64_DF) {
     const int n3 = (degree + 1) * (degree + 1) * (degree + 1);
     mfgb_status st = range_check_sync(nelmt * n3, d_in, nelmt, 6 * n3, d_G, s, "mfgb_bk5_evector");
     if (st) return st;

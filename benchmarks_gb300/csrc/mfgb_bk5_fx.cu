@@ -103,6 +103,51 @@ static cudaError_t fx_with_basis(int64_t n_cells, const uint32_t *map, const flo
             : fx_launch<N, E, MB, false>(n_cells, map, G, gexp, src, dst, b, s, done);
 }
 
+// the E-vector form: FP64 G (16-byte aligned), contiguous input and output
+template <int N>
+static cudaError_t fx_evec_with_basis(int64_t nelmt, const double *G, const double *src,
+                                      double *dst, const double *D, cudaStream_t s) {
+  BasisFX<N> b;
+  const double K = 2.0 * (1.0 + std::ldexp(1.0, -20));
+  for (int q = 0; q < N * N; ++q) {
+    b.Dh[q] = (float)D[q];
+    b.Dl[q] = (float)(D[q] - (double)b.Dh[q]);
+  }
+  for (int i = 0; i < N; ++i) {
+    double rs = 0.0, cs = 0.0;
+    for (int m = 0; m < N; ++m) {
+      rs += std::fabs((double)b.Dh[i * N + m]);
+      cs += std::fabs((double)b.Dh[m * N + i]);
+    }
+    b.cg[i] = (float)(K * rs);
+    b.ci[i] = (float)(K * cs);
+  }
+  b.K = (float)K;
+  constexpr int E = FxElems<N>::value, MB = FxMinBlocks<N>::value;
+  constexpr size_t smem = TmaLayout<N, E, ArithF64>::total;
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk5fx_evec_kernel<N, E, MB>, E * N * N, smem));
+  const int64_t nb = (nelmt + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)per_sm * num_sms()));
+  bk5fx_evec_kernel<N, E, MB><<<grid, E * N * N, smem, s>>>(nelmt, G, src, dst, b,
+                                                            device_error_flag());
+  return cudaGetLastError();
+}
+
+cudaError_t bk5_fx_evec(int N, int64_t nelmt, const double *G, const double *src, double *dst,
+                        const double *D, cudaStream_t s) {
+  if (nelmt <= 0) return cudaSuccess;
+  if (reinterpret_cast<uintptr_t>(G) & 15u) return cudaErrorInvalidValue;  // bulk copies
+  switch (N) {
+#define MFGB_FXEV(NN) \
+  case NN: return fx_evec_with_basis<NN>(nelmt, G, src, dst, D, s);
+    MFGB_FXEV(2) MFGB_FXEV(3) MFGB_FXEV(4) MFGB_FXEV(5) MFGB_FXEV(6) MFGB_FXEV(7) MFGB_FXEV(8)
+    MFGB_FXEV(9)
+#undef MFGB_FXEV
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t bk5_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
                    const double *src, double *dst, const double *D, cudaStream_t s,
                    const int *done) {

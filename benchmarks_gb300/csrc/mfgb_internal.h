@@ -68,6 +68,11 @@ cudaError_t bk5_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G,
 cudaError_t bk5_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
                    const double *src, double *dst, const double *D, cudaStream_t s,
                    const int *done = nullptr);
+// the E-vector form of bk5_fx for the BK5 E-vector seam: the caller's FP64
+// G[e][6][N^3] (16-byte aligned) scaled per element inside the kernel,
+// contiguous src / dst (dst overwritten)
+cudaError_t bk5_fx_evec(int N, int64_t nelmt, const double *G, const double *src, double *dst,
+                        const double *D, cudaStream_t s);
 cudaError_t g_to_fx(int64_t n_cells, int per_cell, const double *G, float2 *Gfx, int *gexp,
                     cudaStream_t s);
 cudaError_t bk5_df_g64(int N, int64_t n_cells, const uint32_t *map, const double *G,

@@ -3,8 +3,8 @@
 * GLL collocation, Gauss p+1 and BP3 Laplacians scale every cell by a power of two: source vectors
   and geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
   oracle result to the operator's 1e-12 bar.
-* The double-float kernels without per-cell scaling (the Helmholtz form here,
-  the E-vector seam) take inputs whose largest magnitude lies in [2^-40, 2^55]:
+* The double-float kernels without per-cell scaling (the Helmholtz form, the
+  L-vector seam) take inputs whose largest magnitude lies in [2^-40, 2^55]:
   inside it they meet 1e-12, outside it they report MFGB_ERR_RANGE (the seam on
   the call, an operator application through the device error word).
 * A NaN in the right-hand side ends conjugate gradients with MFGB_ERR_NONFINITE.
@@ -137,10 +137,13 @@ def test_gauss_df_carries_any_source_scale(mf, orc, scale):
     assert rel(y.cpu().numpy(), ref.apply(src) * scale) <= TOL
 
 
-def test_evector_seam_df_range_is_reported_on_the_call(mf, orc):
-    from benchmarks_gb300 import MfgbError, _abi
+@pytest.mark.parametrize("scale", [(1e-30, 1.0), (1.0, 2.0 ** 100), (1e30, 1e-280)])
+def test_evector_seam_df_carries_any_scale(mf, orc, scale):
+    """The BK5 E-vector seam scales every element's G and input by powers of
+    two inside the kernel: any FP64 range meets 1e-12."""
     import torch
-    p, nelmt = 3, 20
+    gs, us = scale
+    p, nelmt = 3, 23
     nq = p + 1
     rng = np.random.default_rng(2)
     x, _ = orc.gll(nq)
@@ -148,11 +151,29 @@ def test_evector_seam_df_range_is_reported_on_the_call(mf, orc):
     G = rng.uniform(0.1, 1, nelmt * 6 * nq ** 3)
     u = rng.uniform(-1, 1, nelmt * nq ** 3)
     out = torch.zeros(nelmt * nq ** 3, dtype=torch.float64, device="cuda")
-    mf.bk5_evector(p, cuda(D), cuda(G * 2.0 ** -30), cuda(u), out, arith="df")
-    assert rel(out.cpu().numpy(), orc.evector(nq, D, G, u) * 2.0 ** -30) <= TOL
-    for g, v in ((G * 1e-30, u), (G, u * 2.0 ** 100), (G * 1e30, u)):
+    mf.bk5_evector(p, cuda(D), cuda(G * gs), cuda(u * us), out, arith="df")
+    assert rel(out.cpu().numpy(), orc.evector(nq, D, G, u) * gs * us) <= TOL
+
+
+def test_lvector_seam_df_range_is_reported_on_the_call(mf, orc):
+    """The L-vector seam keeps the TwoSum kernel without scaling: caller G
+    inside the window meets 1e-12, outside it the call reports
+    MFGB_ERR_RANGE."""
+    from benchmarks_gb300 import MfgbError, _abi
+    import torch
+    ref = orc.BoxProblem(3, 3, 2, 3, amplitude=0.1)
+    src = np.random.default_rng(9).uniform(-1, 1, ref.n_dofs)
+    dmap = torch.from_numpy(ref.map.view(np.int32).copy()).cuda()
+    dst = torch.zeros(ref.n_dofs, dtype=torch.float64, device="cuda")
+    mf.bk5_lvector(3, cuda(ref.D.reshape(-1)), cuda(ref.G * 2.0 ** -30), cuda(src), dst, dmap,
+                   arith="df")
+    want = ref.apply(src)
+    want[ref.constrained] = 0.0  # the seam does not write identity rows
+    assert rel(dst.cpu().numpy(), want * 2.0 ** -30) <= TOL
+    for g in (ref.G * 1e-30, ref.G * 1e30):
+        dst.zero_()
         with pytest.raises(MfgbError) as e:
-            mf.bk5_evector(p, cuda(D), cuda(g), cuda(v), out, arith="df")
+            mf.bk5_lvector(3, cuda(ref.D.reshape(-1)), cuda(g), cuda(src), dst, dmap, arith="df")
         assert e.value.status == _abi.ERR_RANGE
 
 
