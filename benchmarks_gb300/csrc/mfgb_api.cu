@@ -734,7 +734,10 @@ mfgb_status mfgb_bk5_lvector(int degree, int64_t n_cells, const double *d_dbasis
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64)
     e = bk5_f64(degree + 1, n_cells, d_dof_indices, d_G, d_src, d_dst, D, nullptr, nullptr, s);
-  else if (arith == MFGB_ARITH_FP64_DF) {
+  else if (arith == MFGB_ARITH_FP64_DF && (reinterpret_cast<uintptr_t>(d_G) & 15u) == 0) {
+    // offset double-float with per-cell scaling: any input range, no check
+    e = bk5_fx_g64(degree + 1, n_cells, d_dof_indices, d_G, d_src, d_dst, D, s);
+  } else if (arith == MFGB_ARITH_FP64_DF) {
     // (the source vector's length is not an argument of this seam: G is checked)
     const int n3 = (degree + 1) * (degree + 1) * (degree + 1);
     mfgb_status st = range_check_sync(0, nullptr, n_cells, 6 * n3, d_G, s, "mfgb_bk5_lvector");

@@ -103,10 +103,9 @@ static cudaError_t fx_with_basis(int64_t n_cells, const uint32_t *map, const flo
             : fx_launch<N, E, MB, false>(n_cells, map, G, gexp, src, dst, b, s, done);
 }
 
-// the E-vector form: FP64 G (16-byte aligned), contiguous input and output
+// the basis pairs and bound factors of the collocation kernels
 template <int N>
-static cudaError_t fx_evec_with_basis(int64_t nelmt, const double *G, const double *src,
-                                      double *dst, const double *D, cudaStream_t s) {
+static BasisFX<N> basis_fx(const double *D) {
   BasisFX<N> b;
   const double K = 2.0 * (1.0 + std::ldexp(1.0, -20));
   for (int q = 0; q < N * N; ++q) {
@@ -123,6 +122,47 @@ static cudaError_t fx_evec_with_basis(int64_t nelmt, const double *G, const doub
     b.ci[i] = (float)(K * cs);
   }
   b.K = (float)K;
+  return b;
+}
+
+// the L-vector form on the caller's FP64 G (16-byte aligned)
+template <int N, bool MT>
+static cudaError_t fx_g64_launch(int64_t n_cells, const uint32_t *map, const double *G,
+                                 const double *src, double *dst, const double *D,
+                                 cudaStream_t s) {
+  const BasisFX<N> b = basis_fx<N>(D);
+  constexpr int E = FxElems<N>::value, MB = FxMinBlocks<N>::value;
+  constexpr size_t smem = TmaLayout<N, E, ArithF64>::total;
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = std::max(1, ctas_per_sm(bk5fx_g64_kernel<N, E, MB, MT>, E * N * N, smem));
+  const int64_t nb = (n_cells + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)per_sm * num_sms()));
+  bk5fx_g64_kernel<N, E, MB, MT><<<grid, E * N * N, smem, s>>>(n_cells, map, G, src, dst, b,
+                                                                device_error_flag());
+  return cudaGetLastError();
+}
+
+cudaError_t bk5_fx_g64(int N, int64_t n_cells, const uint32_t *map, const double *G,
+                       const double *src, double *dst, const double *D, cudaStream_t s) {
+  if (n_cells <= 0) return cudaSuccess;
+  if (map == nullptr || (reinterpret_cast<uintptr_t>(G) & 15u)) return cudaErrorInvalidValue;
+  const bool mt = (reinterpret_cast<uintptr_t>(map) & 15u) == 0;
+  switch (N) {
+#define MFGB_FXG(NN)                                                      \
+  case NN:                                                                \
+    return mt ? fx_g64_launch<NN, true>(n_cells, map, G, src, dst, D, s) \
+              : fx_g64_launch<NN, false>(n_cells, map, G, src, dst, D, s);
+    MFGB_FXG(2) MFGB_FXG(3) MFGB_FXG(4) MFGB_FXG(5) MFGB_FXG(6) MFGB_FXG(7) MFGB_FXG(8) MFGB_FXG(9)
+#undef MFGB_FXG
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// the E-vector form: FP64 G (16-byte aligned), contiguous input and output
+template <int N>
+static cudaError_t fx_evec_with_basis(int64_t nelmt, const double *G, const double *src,
+                                      double *dst, const double *D, cudaStream_t s) {
+  const BasisFX<N> b = basis_fx<N>(D);
   constexpr int E = FxElems<N>::value, MB = FxMinBlocks<N>::value;
   constexpr size_t smem = TmaLayout<N, E, ArithF64>::total;
   static int per_sm = -1;

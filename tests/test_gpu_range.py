@@ -3,8 +3,8 @@
 * GLL collocation, Gauss p+1 and BP3 Laplacians scale every cell by a power of two: source vectors
   and geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
   oracle result to the operator's 1e-12 bar.
-* The double-float kernels without per-cell scaling (the Helmholtz form, the
-  L-vector seam) take inputs whose largest magnitude lies in [2^-40, 2^55]:
+* The double-float kernels without per-cell scaling (the Helmholtz form, a
+  seam given an unaligned G) take inputs whose largest magnitude lies in [2^-40, 2^55]:
   inside it they meet 1e-12, outside it they report MFGB_ERR_RANGE (the seam on
   the call, an operator application through the device error word).
 * A NaN in the right-hand side ends conjugate gradients with MFGB_ERR_NONFINITE.
@@ -155,25 +155,36 @@ def test_evector_seam_df_carries_any_scale(mf, orc, scale):
     assert rel(out.cpu().numpy(), orc.evector(nq, D, G, u) * gs * us) <= TOL
 
 
-def test_lvector_seam_df_range_is_reported_on_the_call(mf, orc):
-    """The L-vector seam keeps the TwoSum kernel without scaling: caller G
-    inside the window meets 1e-12, outside it the call reports
-    MFGB_ERR_RANGE."""
+def test_lvector_seam_df_scale_and_range(mf, orc):
+    """The L-vector seam with a 16-byte aligned G scales every cell inside the
+    kernel (any range); with an unaligned G it runs the TwoSum kernel, whose
+    window the call checks: inside it 1e-12, outside it MFGB_ERR_RANGE."""
     from benchmarks_gb300 import MfgbError, _abi
     import torch
     ref = orc.BoxProblem(3, 3, 2, 3, amplitude=0.1)
     src = np.random.default_rng(9).uniform(-1, 1, ref.n_dofs)
     dmap = torch.from_numpy(ref.map.view(np.int32).copy()).cuda()
-    dst = torch.zeros(ref.n_dofs, dtype=torch.float64, device="cuda")
-    mf.bk5_lvector(3, cuda(ref.D.reshape(-1)), cuda(ref.G * 2.0 ** -30), cuda(src), dst, dmap,
-                   arith="df")
+    D = cuda(ref.D.reshape(-1))
     want = ref.apply(src)
     want[ref.constrained] = 0.0  # the seam does not write identity rows
+    dst = torch.zeros(ref.n_dofs, dtype=torch.float64, device="cuda")
+    for gs in (2.0 ** -30, 1e-30, 1e30):  # aligned G: any scale
+        dst.zero_()
+        mf.bk5_lvector(3, D, cuda(ref.G * gs), cuda(src), dst, dmap, arith="df")
+        assert rel(dst.cpu().numpy(), want * gs) <= TOL
+
+    def unaligned(g):  # the same values 8 bytes past a 16-byte boundary
+        buf = torch.zeros(g.size + 1, dtype=torch.float64, device="cuda")
+        buf[1:] = cuda(g)
+        return buf[1:]
+
+    dst.zero_()
+    mf.bk5_lvector(3, D, unaligned(ref.G * 2.0 ** -30), cuda(src), dst, dmap, arith="df")
     assert rel(dst.cpu().numpy(), want * 2.0 ** -30) <= TOL
     for g in (ref.G * 1e-30, ref.G * 1e30):
         dst.zero_()
         with pytest.raises(MfgbError) as e:
-            mf.bk5_lvector(3, cuda(ref.D.reshape(-1)), cuda(g), cuda(src), dst, dmap, arith="df")
+            mf.bk5_lvector(3, D, unaligned(g), cuda(src), dst, dmap, arith="df")
         assert e.value.status == _abi.ERR_RANGE
 
 
