@@ -188,6 +188,40 @@ cudaError_t bk5_fx_evec(int N, int64_t nelmt, const double *G, const double *src
   }
 }
 
+// the BK6 vector Laplacian: 3 interleaved components per DoF on one scaled G
+template <int N, bool MT>
+static cudaError_t fx_bk6_launch(int64_t n_cells, const uint32_t *map, const float2 *G,
+                                 const int *gexp, const double *src, double *dst, const double *D,
+                                 cudaStream_t s) {
+  const BasisFX<N> b = basis_fx<N>(D);
+  constexpr int E = FxElems<N>::value, MB = FxMinBlocks<N>::value;
+  constexpr size_t smem = TmaLayout<N, E, ArithDF>::total;
+  static int per_sm = -1;
+  if (per_sm < 0)
+    per_sm = std::max(1, ctas_per_sm(bk6fx_tma_kernel<N, E, MB, MT, 3>, E * N * N, smem));
+  const int64_t nb = (n_cells + E - 1) / E;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)per_sm * num_sms()));
+  bk6fx_tma_kernel<N, E, MB, MT, 3><<<grid, E * N * N, smem, s>>>(n_cells, map, G, gexp, src, dst,
+                                                                  b, device_error_flag());
+  return cudaGetLastError();
+}
+
+cudaError_t bk6_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
+                   const double *src, double *dst, const double *D, cudaStream_t s) {
+  if (n_cells <= 0) return cudaSuccess;
+  if (map == nullptr || (reinterpret_cast<uintptr_t>(G) & 15u)) return cudaErrorInvalidValue;
+  const bool mt = (reinterpret_cast<uintptr_t>(map) & 15u) == 0;
+  switch (N) {
+#define MFGB_FX6(NN)                                                              \
+  case NN:                                                                        \
+    return mt ? fx_bk6_launch<NN, true>(n_cells, map, G, gexp, src, dst, D, s) \
+              : fx_bk6_launch<NN, false>(n_cells, map, G, gexp, src, dst, D, s);
+    MFGB_FX6(2) MFGB_FX6(3) MFGB_FX6(4) MFGB_FX6(5) MFGB_FX6(6) MFGB_FX6(7) MFGB_FX6(8) MFGB_FX6(9)
+#undef MFGB_FX6
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t bk5_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
                    const double *src, double *dst, const double *D, cudaStream_t s,
                    const int *done) {

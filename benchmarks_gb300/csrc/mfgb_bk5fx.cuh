@@ -396,6 +396,250 @@ __global__ void __launch_bounds__(E * N * N, MB)
 }
 
 
+// BK6 (NC interleaved components per node sharing one G tile) with the offset
+// accumulation and per-cell scaling of the kernel above: per batch the scaled
+// G pairs arrive once, and the components run one after another, each with its
+// own exponent offset per cell (reduced while the previous component
+// integrates, read after one extra barrier).  The next component's gather is
+// prefetched during the current component's transpose, the next batch's first
+// component during the last one.
+template <int N, int E, int MB, bool MAPTMA, int NC>
+__global__ void __launch_bounds__(E * N * N, MB)
+    bk6fx_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
+                     const float2 *__restrict__ G, const int *__restrict__ gexp,
+                     const double *__restrict__ src, double *__restrict__ dst,
+                     const BasisFX<N> basis, int *__restrict__ err_flag) {
+  using L = TmaLayout<N, E, ArithDF>;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float2 *sG = reinterpret_cast<float2 *>(smem);
+  uint32_t *sMap = reinterpret_cast<uint32_t *>(smem + L::g_bytes);
+  df *s_u = reinterpret_cast<df *>(smem + L::g_bytes + L::map_bytes);
+  df *s_vs = s_u + E * N3;
+  df *s_vt = s_vs + E * N3;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::g_bytes + L::map_bytes + L::work_bytes);
+  uint64_t *mbar_g = mbar, *mbar_m = mbar + 1;
+  __shared__ int s_emax[2][E];
+
+  const int tid = threadIdx.x;
+  const int el = tid / N2;
+  const int jk = tid - el * N2;
+  const int j = jk / N;
+  const int k = jk - j * N;
+  const int64_t n_batches = (n_cells + E - 1) / E;
+  int64_t batch = blockIdx.x;
+  if (batch >= n_batches) return;  // uniform across the CTA
+
+  __shared__ float2 s_D[N * N];
+  for (int t = tid; t < N * N; t += blockDim.x) s_D[t] = make_float2(basis.Dh[t], basis.Dl[t]);
+  const float cgj = basis.cg[j], cgk = basis.cg[k], cij = basis.ci[j], cik = basis.ci[k];
+
+  TmaTiles<N, E, ArithDF> T{n_cells, map, G, src, sG, sMap, mbar_g, mbar_m};
+  T.map_ok = MAPTMA;
+  auto fail = [&](uint32_t pg, uint32_t pm) {
+    if (tid == 0 && err_flag) atomicOr(err_flag, 1);
+    mbar_wait(mbar_g, pg);  // bounded waits for copies still in flight
+    mbar_wait(mbar_m, pm);
+  };
+
+  if (tid < 2 * E) (&s_emax[0][0])[tid] = 0;
+  if (tid == 0) {
+    mbar_init(mbar_g, 1);
+    mbar_init(mbar_m, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    T.issue_g(batch);
+    T.issue_map(batch);
+  }
+  uint32_t ph_g = 0, ph_m = 0;
+  uint32_t idx[N];
+  double raw[N];
+  int ge = 0;  // G exponent offset of this thread's cell in the prefetched batch
+  // dof indices of column (el, jk) of batch b, from the map tile or global
+  auto indices = [&](int64_t b) {
+    const int cells = T.cells_of(b);
+    const bool ok = el < cells;
+    const bool mt = T.map_by_tma(cells);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      idx[i] = ok ? (mt ? sMap[el * N3 + i * N2 + jk] : __ldg(map + (b * E + el) * N3 + i * N2 + jk))
+                  : MFGB_INVALID_DOF;
+  };
+  auto gather = [&](int c) {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      raw[i] = idx[i] != MFGB_INVALID_DOF ? __ldg(src + (size_t)NC * idx[i] + c) : 0.0;
+  };
+  auto reduce_exp = [&](int slot) {
+    int em = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) em = max(em, idx[i] != MFGB_INVALID_DOF ? dexp(raw[i]) : 0);
+    if (em) atomicMax(&s_emax[slot][el], em);
+  };
+  {
+    const bool ok = mbar_wait(mbar_m, ph_m);
+    if (__syncthreads_or(!ok)) { fail(ph_g, ph_m); return; }
+    ph_m ^= 1u;
+    indices(batch);
+    gather(0);
+    reduce_exp(0);
+    if (el < T.cells_of(batch)) ge = __ldg(gexp + batch * E + el);
+  }
+
+  int cnt = 0;  // components run so far: the exponent slot alternates with it
+  for (; batch < n_batches; batch += gridDim.x) {
+    const int64_t next = batch + gridDim.x;
+    const bool has_next = next < n_batches;
+    const bool okg = mbar_wait(mbar_g, ph_g);
+    if (__syncthreads_or(!okg)) { fail(ph_g, ph_m); return; }  // barrier A
+    ph_g ^= 1u;
+    T.load_g_plain(batch, tid, blockDim.x);  // ordered before the metric phase by barrier B
+    const bool valid = el < T.cells_of(batch);
+    const float2 *Gc = sG + el * 6 * N3 + jk;
+    const int ge_batch = ge;
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c, ++cnt) {
+      const int slot = cnt & 1;
+      if (c > 0) __syncthreads();  // this component's exponents are in; s_u is free
+      const int su = fx_offset(s_emax[slot][el]);
+      const int sc = su + ge_batch;  // the cell's result scale for this component
+      const bool fast_out = (unsigned)(sc + 896) <= 1792u;
+      const unsigned kout = (unsigned)(896 + sc) << 20;
+      df u[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        u[i] = idx[i] != MFGB_INVALID_DOF ? fx_from_double(raw[i], su) : df{0.f, 0.f};
+        s_u[el * N3 + i * N2 + jk] = u[i];
+      }
+      __syncthreads();  // barrier B: s_u ready, s_emax[slot] read (c = 0: the map tile is free)
+      if (jk == 0) s_emax[slot][el] = 0;  // next written two components on
+      if (c == 0 && tid == 0 && has_next) {
+        fence_proxy_async_smem();
+        T.issue_map(next);
+      }
+      float Djh[N], Djl[N], Dkh[N], Dkl[N];
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        const float2 a = lds_pair(s_D + j * N + m), b = lds_pair(s_D + k * N + m);
+        Djh[m] = a.x, Djl[m] = a.y, Dkh[m] = b.x, Dkl[m] = b.y;
+      }
+      df vr[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        fxacc ar, as, at;
+        const float cr = basis.cg[i];
+        fx_first(ar, basis.Dh[i * N], basis.Dl[i * N], u[0].hi, u[0].lo, cr);
+        {
+          const df a = s_u[el * N3 + i * N2 + k], b = s_u[el * N3 + i * N2 + j * N];
+          fx_first(as, Djh[0], Djl[0], a.hi, a.lo, cgj);
+          fx_first(at, Dkh[0], Dkl[0], b.hi, b.lo, cgk);
+        }
+#pragma unroll
+        for (int m = 1; m < N; ++m) {
+          fx_fma(ar, basis.Dh[i * N + m], basis.Dl[i * N + m], u[m].hi, u[m].lo);
+          const df a = s_u[el * N3 + i * N2 + m * N + k], b = s_u[el * N3 + i * N2 + j * N + m];
+          fx_fma(as, Djh[m], Djl[m], a.hi, a.lo);
+          fx_fma(at, Dkh[m], Dkl[m], b.hi, b.lo);
+        }
+        const df qr = fx_finish(ar, cr), qs = fx_finish(as, cgj), qt = fx_finish(at, cgk);
+        float2 grr = make_float2(0.f, 0.f), grs = grr, grt = grr, gss = grr, gst = grr, gtt = grr;
+        if (valid) {
+          grr = Gc[0 * N3 + i * N2];
+          grs = Gc[1 * N3 + i * N2];
+          grt = Gc[2 * N3 + i * N2];
+          gss = Gc[3 * N3 + i * N2];
+          gst = Gc[4 * N3 + i * N2];
+          gtt = Gc[5 * N3 + i * N2];
+        }
+        const float kq = basis.K * fmaxf(fmaxf(fabsf(qr.hi), fabsf(qs.hi)), fabsf(qt.hi));
+        const float Cr = (fabsf(grr.x) + fabsf(grs.x) + fabsf(grt.x)) * kq;
+        const float Cs = (fabsf(grs.x) + fabsf(gss.x) + fabsf(gst.x)) * kq;
+        const float Ct = (fabsf(grt.x) + fabsf(gst.x) + fabsf(gtt.x)) * kq;
+        fxacc br, bs, bt;
+        fx_first(br, grr.x, grr.y, qr.hi, qr.lo, Cr);
+        fx_fma(br, grs.x, grs.y, qs.hi, qs.lo);
+        fx_fma(br, grt.x, grt.y, qt.hi, qt.lo);
+        fx_first(bs, grs.x, grs.y, qr.hi, qr.lo, Cs);
+        fx_fma(bs, gss.x, gss.y, qs.hi, qs.lo);
+        fx_fma(bs, gst.x, gst.y, qt.hi, qt.lo);
+        fx_first(bt, grt.x, grt.y, qr.hi, qr.lo, Ct);
+        fx_fma(bt, gst.x, gst.y, qs.hi, qs.lo);
+        fx_fma(bt, gtt.x, gtt.y, qt.hi, qt.lo);
+        vr[i] = fx_finish(br, Cr);
+        s_vs[el * N3 + i * N2 + jk] = fx_finish(bs, Cs);
+        s_vt[el * N3 + i * N2 + jk] = fx_finish(bt, Ct);
+      }
+      __syncthreads();  // barrier C: s_vs / s_vt ready (last component: G tile consumed)
+      if (c == NC - 1 && tid == 0 && has_next) {
+        fence_proxy_async_smem();
+        T.issue_g(next);
+      }
+      // this component's scatter targets; then prefetch the next component
+      // (the next batch's first one after the last)
+      uint32_t cur[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) cur[i] = idx[i];
+      if (c + 1 < NC) {
+        gather(c + 1);
+      } else if (has_next) {
+        const bool okm = mbar_wait(mbar_m, ph_m);
+        if (!okm && err_flag) atomicOr(err_flag, 1);  // the launch's result is void
+        ph_m ^= 1u;
+        if (okm) {
+          indices(next);
+          gather(0);
+        } else {
+#pragma unroll
+          for (int i = 0; i < N; ++i) { idx[i] = MFGB_INVALID_DOF; raw[i] = 0.0; }
+        }
+        ge = el < T.cells_of(next) ? __ldg(gexp + next * E + el) : 0;
+      }
+      float Dtjh[N], Dtjl[N], Dtkh[N], Dtkl[N];
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        const float2 a = lds_pair(s_D + m * N + j), b = lds_pair(s_D + m * N + k);
+        Dtjh[m] = a.x, Dtjl[m] = a.y, Dtkh[m] = b.x, Dtkl[m] = b.y;
+      }
+      float mr = 0.f;
+#pragma unroll
+      for (int m = 0; m < N; ++m) mr = fmaxf(mr, fabsf(vr[m].hi));
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        df ls[N], lt[N];
+        float ms = 0.f, mt = 0.f;
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          ls[m] = s_vs[el * N3 + i * N2 + m * N + k];
+          lt[m] = s_vt[el * N3 + i * N2 + j * N + m];
+          ms = fmaxf(ms, fabsf(ls[m].hi));
+          mt = fmaxf(mt, fabsf(lt[m].hi));
+        }
+        const float C = __fmaf_rn(mt, cik, __fmaf_rn(ms, cij, mr * basis.ci[i]));
+        fxacc a;
+        fx_first(a, basis.Dh[i], basis.Dl[i], vr[0].hi, vr[0].lo, C);
+        fx_fma(a, Dtjh[0], Dtjl[0], ls[0].hi, ls[0].lo);
+        fx_fma(a, Dtkh[0], Dtkl[0], lt[0].hi, lt[0].lo);
+#pragma unroll
+        for (int m = 1; m < N; ++m) {
+          fx_fma(a, basis.Dh[m * N + i], basis.Dl[m * N + i], vr[m].hi, vr[m].lo);
+          fx_fma(a, Dtjh[m], Dtjl[m], ls[m].hi, ls[m].lo);
+          fx_fma(a, Dtkh[m], Dtkl[m], lt[m].hi, lt[m].lo);
+        }
+        const df y = fx_finish(a, C);
+        if (cur[i] != MFGB_INVALID_DOF)
+          atomicAdd(dst + (size_t)NC * cur[i] + c,
+                    fast_out ? fx_f2d_fast(y.hi, kout) + fx_f2d_fast(y.lo, kout)
+                             : fx_f2d(y.hi, sc) + fx_f2d(y.lo, sc));
+      }
+      // the prefetched component's largest exponent per cell (read after the
+      // next component's first barrier, or the next batch's barrier A)
+      if (c + 1 < NC || has_next) reduce_exp(slot ^ 1);
+    }
+  }
+}
+
 // The same kernel on the caller's FP64 G (the BK5 L-vector seam, deal.II's
 // MatrixFree kernel, bakeoff_problems_dealii/include/bk3_kokkos_kernel.h):
 // G[cell][6][n^3] arrives by bulk copies, each cell's largest G exponent is

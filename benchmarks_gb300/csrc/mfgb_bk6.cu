@@ -41,6 +41,10 @@ extern "C" mfgb_status mfgb_vmult_vector(const mfgb_operator *cop, double *d_dst
   cudaError_t e;
   if (arith == MFGB_ARITH_FP64) {
     e = bk6_f64(op->n, op->n_cells, op->d_map, op->d_G, d_src, d_dst, op->D, s);
+  } else if (arith == MFGB_ARITH_FP64_DF && (op->d_Gfx || op->d_G)) {
+    // offset double-float, every component scaled per cell: any input range
+    if ((st = ensure_fx(op))) return st;
+    e = bk6_fx(op->n, op->n_cells, op->d_map, op->d_Gfx, op->d_Gexp, d_src, d_dst, op->D, s);
   } else if (arith == MFGB_ARITH_FP64_DF) {
     if ((st = ensure_df(op)) || (st = range_check_async(op, 3 * op->n_dofs, d_src, s))) return st;
     e = bk6_df(op->n, op->n_cells, op->d_map, op->d_Gdf, d_src, d_dst, op->D, s);

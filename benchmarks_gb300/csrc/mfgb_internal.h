@@ -68,6 +68,10 @@ cudaError_t bk5_df(int N, int64_t n_cells, const uint32_t *map, const float2 *G,
 cudaError_t bk5_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
                    const double *src, double *dst, const double *D, cudaStream_t s,
                    const int *done = nullptr);
+// the BK6 vector Laplacian on the scaled pairs of bk5_fx: src / dst hold 3
+// interleaved components per DoF, each component scaled per cell on its own
+cudaError_t bk6_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G, const int *gexp,
+                   const double *src, double *dst, const double *D, cudaStream_t s);
 // bk5_fx on the caller's FP64 G[cell][6][N^3] (16-byte aligned) scaled per
 // cell inside the kernel, for the BK5 L-vector seam: dst += A src through map
 cudaError_t bk5_fx_g64(int N, int64_t n_cells, const uint32_t *map, const double *G,

@@ -1,8 +1,9 @@
 """Range of the FP64-accurate double-float arithmetic (MFGB_ARITH_FP64_DF).
 
-* GLL collocation, Gauss p+1 and BP3 Laplacians scale every cell by a power of two: source vectors
-  and geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
-  oracle result to the operator's 1e-12 bar.
+* GLL collocation (BK5, and BK6 per component), Gauss p+1 and BP3 Laplacians
+  scale every cell by a power of two: source vectors and geometric factors
+  scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled oracle result to the
+  operator's 1e-12 bar.
 * The double-float kernels without per-cell scaling (the Helmholtz form, a
   seam given an unaligned G) take inputs whose largest magnitude lies in [2^-40, 2^55]:
   inside it they meet 1e-12, outside it they report MFGB_ERR_RANGE (the seam on
@@ -186,6 +187,27 @@ def test_lvector_seam_df_scale_and_range(mf, orc):
         with pytest.raises(MfgbError) as e:
             mf.bk5_lvector(3, D, unaligned(g), cuda(src), dst, dmap, arith="df")
         assert e.value.status == _abi.ERR_RANGE
+
+
+@pytest.mark.parametrize("p", [2, 4, 7])
+def test_bk6_df_components_carry_own_scale(mf, orc, p):
+    """BK6 scales every component of a cell on its own: components 1e-280,
+    1 and 2^300 apart each meet the bar against the scaled oracle."""
+    cells = (3, 4, 2)
+    A = mf.LaplaceOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.1))
+    ref = orc.BoxProblem(*cells, p, amplitude=0.1)
+    base = np.random.default_rng(p + 40).uniform(-1, 1, 3 * ref.n_dofs)
+    scales = (1e-280, 1.0, 2.0 ** 300)
+    src = base.copy()
+    for c, sc in enumerate(scales):
+        src[c::3] *= sc
+    import torch
+    y = torch.zeros(3 * ref.n_dofs, dtype=torch.float64, device="cuda")
+    A.vmult_vector(y, cuda(src), arith="df")
+    mf.check_device_errors()
+    got = y.cpu().numpy()
+    for c, sc in enumerate(scales):
+        assert rel(got[c::3], ref.apply(base[c::3]) * sc) <= TOL
 
 
 @pytest.mark.parametrize("arith", ["df", "fp64"])
