@@ -23,6 +23,7 @@ SOURCES = [
     "mfgb_batch.cu",
     "mfgb_bkq.cu",
     "mfgb_bp3_fx.cu",
+    "mfgb_helmholtz_fx.cu",
     "mfgb_bk1_dmma.cu",
     "mfgb_bk5_f64.cu",
     "mfgb_bk5_df.cu",

@@ -94,14 +94,20 @@ mfgb_status ensure_fx(mfgb_operator *op) {
                       "G (scaled double-float)")) ||
       (st = dev_alloc((void **)&op->d_Gexp, sizeof(int) * std::max<int64_t>(1, op->n_cells),
                       "G exponent offsets")) ||
-      (st = cuda_status(g_to_fx(op->n_cells, (int)(6 * n3), op->d_G, op->d_Gfx, op->d_Gexp, nullptr),
+      // the mass term's JxW shares the cell's offset with G
+      (op->d_JxW && (st = dev_alloc((void **)&op->d_JxWfx, sizeof(float2) * op->n_cells * n3,
+                                    "JxW (scaled double-float)"))) ||
+      (st = cuda_status(g_to_fx(op->n_cells, (int)(6 * n3), op->d_G, op->d_Gfx, op->d_Gexp, nullptr,
+                                op->d_JxW ? (int)n3 : 0, op->d_JxW, op->d_JxWfx),
                         "G -> scaled double-float")) ||
       (st = cuda_status(cudaDeviceSynchronize(), "G -> scaled double-float"))) {
-    // all or nothing: the pair of arrays exists only complete
+    // all or nothing: the arrays exist only complete
     cudaFree(op->d_Gfx);
     cudaFree(op->d_Gexp);
+    cudaFree(op->d_JxWfx);
     op->d_Gfx = nullptr;
     op->d_Gexp = nullptr;
+    op->d_JxWfx = nullptr;
     return st;
   }
   return MFGB_OK;
@@ -115,10 +121,10 @@ mfgb_status ensure_arith(mfgb_operator *op, int arith) {
     set_error("operator has no geometric factors");
     return MFGB_ERR_INVALID_ARG;
   }
-  // the scaled pairs for GLL collocation (shapes 5 / 6), the BP3 operator and
-  // the Gauss p+1 Laplacian without mass term
+  // the scaled pairs for GLL collocation (shapes 5 / 6) and the Gauss-point
+  // forms (BP3, the Gauss p+1 Laplacian and its Helmholtz form)
   const bool fx = (op->quadrature == 0 && kernel_shape(1, op->n) >= kShapeFx) ||
-                  op->quadrature == 2 || (op->quadrature == 1 && !op->d_JxW);
+                  op->quadrature >= 1;
   return fx ? ensure_fx(op) : ensure_df(op);
 }
 
@@ -130,10 +136,12 @@ static cudaError_t apply_range(mfgb_operator *op, int64_t cell0, int64_t n, doub
   const int64_t n3 = (int64_t)op->n * op->n * op->n;
   const int64_t q3 = (int64_t)op->nq * op->nq * op->nq;
   const uint32_t *map = op->d_map + cell0 * n3;
-  // the Gauss-point forms by the offset-accumulation kernel (no energy partials)
-  if (op->quadrature >= 1 && arith == MFGB_ARITH_FP64_DF && op->d_Gfx && !partials)
+  // the Gauss-point forms by the offset-accumulation kernel (no energy partials;
+  // the mass term from the JxW pairs built with the G pairs)
+  if (op->quadrature >= 1 && arith == MFGB_ARITH_FP64_DF && op->d_Gfx && !partials &&
+      (!op->d_JxW || op->d_JxWfx))
     return bp3_fx(op->degree, op->nq, n, map, op->d_Gfx + cell0 * 6 * q3, op->d_Gexp + cell0, src,
-                  dst, op->Bq, op->DG, s, done);
+                  dst, op->Bq, op->DG, s, done, op->d_JxWfx ? op->d_JxWfx + cell0 * q3 : nullptr);
   if (op->quadrature == 2) {
     if (partials || done) return cudaErrorNotSupported;
     return bp3_apply(op->degree, n, map, op->d_Bq, op->d_DGq, op->Bq, op->DG,
@@ -346,7 +354,7 @@ mfgb_status range_check_sync(int64_t n, const double *v, int64_t n_cells, int pe
 }
 
 bool uses_fx(const mfgb_operator *op) {
-  if (op->quadrature >= 1) return op->d_Gfx != nullptr;
+  if (op->quadrature >= 1) return op->d_Gfx != nullptr && (!op->d_JxW || op->d_JxWfx);
   return op->quadrature == 0 && op->d_Gfx && (kernel_shape(1, op->n) >= kShapeFx || !op->d_Gdf);
 }
 
@@ -383,6 +391,7 @@ static void free_operator(mfgb_operator *op) {
   cudaFree(op->d_partials);
   cudaFree(op->d_JxW);
   cudaFree(op->d_JxWdf);
+  cudaFree(op->d_JxWfx);
   cudaFree(op->d_hsrc);
   cudaFree(op->d_hdst);
   cudaFree(op->d_Bq);

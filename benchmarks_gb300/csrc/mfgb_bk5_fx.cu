@@ -238,38 +238,51 @@ cudaError_t bk5_fx(int N, int64_t n_cells, const uint32_t *map, const float2 *G,
 }
 
 // Per-cell scaled split of the FP64 geometric factors: one warp per cell finds
-// the largest biased exponent e among the cell's 6 n^3 values and writes
-// G * 2^-(e - 1022) as float pairs (hi = nearest float, lo = nearest float of
-// the remainder); gexp[cell] = e - 1022 (0 for an all-zero cell).
+// the largest biased exponent e among the cell's 6 n^3 values (and its per_j
+// JxW values, when given) and writes them times 2^-(e - 1022) as float pairs
+// (hi = nearest float, lo = nearest float of the remainder); gexp[cell] =
+// e - 1022 (0 for an all-zero cell).  Values more than 2^126 below the cell's
+// largest lose their low digits or flush to zero, far below the operator's
+// accuracy bar relative to the cell's largest term.
 __global__ void g_to_fx_kernel(int64_t n_cells, int per_cell, const double *__restrict__ G,
-                               float2 *__restrict__ out, int *__restrict__ gexp) {
+                               float2 *__restrict__ out, int *__restrict__ gexp, int per_j,
+                               const double *__restrict__ J, float2 *__restrict__ jout) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  auto split = [](double x, int off) {
+    const double y = scalbn(x, -off);
+    const float hi = __double2float_rn(y);
+    return make_float2(hi, __double2float_rn(y - (double)hi));
+  };
   for (int64_t c = warp; c < n_cells; c += n_warps) {
     const double *g = G + c * per_cell;
+    const double *j = J + c * per_j;
     int em = 0;
     for (int t = lane; t < per_cell; t += 32) {
       const int e = dexp(g[t]);
       em = max(em, e == 0x7FF ? 0 : e);
     }
+    for (int t = lane; t < per_j; t += 32) {
+      const int e = dexp(j[t]);
+      em = max(em, e == 0x7FF ? 0 : e);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, o));
     const int off = fx_offset(em);
-    for (int t = lane; t < per_cell; t += 32) {
-      const double x = scalbn(g[t], -off);
-      const float hi = __double2float_rn(x);
-      out[c * per_cell + t] = make_float2(hi, __double2float_rn(x - (double)hi));
-    }
+    for (int t = lane; t < per_cell; t += 32) out[c * per_cell + t] = split(g[t], off);
+    for (int t = lane; t < per_j; t += 32) jout[c * per_j + t] = split(j[t], off);
     if (lane == 0) gexp[c] = off;
   }
 }
 
 cudaError_t g_to_fx(int64_t n_cells, int per_cell, const double *G, float2 *Gfx, int *gexp,
-                    cudaStream_t s) {
+                    cudaStream_t s, int per_cell_j, const double *J, float2 *Jfx) {
   if (n_cells <= 0) return cudaSuccess;
+  if (per_cell_j > 0 && (!J || !Jfx)) return cudaErrorInvalidValue;
   const int64_t blocks = std::min<int64_t>((n_cells + 7) / 8, 152 * 32);
-  g_to_fx_kernel<<<(int)blocks, 256, 0, s>>>(n_cells, per_cell, G, Gfx, gexp);
+  g_to_fx_kernel<<<(int)blocks, 256, 0, s>>>(n_cells, per_cell, G, Gfx, gexp,
+                                             per_cell_j > 0 ? per_cell_j : 0, J, Jfx);
   return cudaGetLastError();
 }
 

@@ -17,7 +17,8 @@
 //     per cell by 2^-sg)
 //   integrate and the backward interpolations: K colsum|D| or K colsum|B|
 //     times the largest |value| of each line read (the own column's, or the
-//     line loaded into registers first).
+//     line loaded into registers first); the Helmholtz form's mass term adds
+//     K |JxW u| at the point (JxW pairs on the cell's G scale).
 // The cell's result is scaled back by 2^(su + sg) when converted to double.
 #pragma once
 #include "mfgb_bk5fx.cuh"
@@ -40,13 +41,16 @@ struct BasisQFX {
 // unsigned integers), for shared atomicMax
 __device__ __forceinline__ unsigned abs_bits(float x) { return __float_as_uint(fabsf(x)); }
 
-template <int NM, int NQ, int E, int MB, bool MAPTMA>
+// MASS: the Helmholtz form's mass term JxW u at every Gauss point (jxw: the
+// JxW pairs [cell][NQ^3] on the cell's G scale), each point's value loaded one
+// point ahead of its use
+template <int NM, int NQ, int E, int MB, bool MAPTMA, bool MASS = false>
 __global__ void __launch_bounds__(E * NQ * NQ, MB)
     bp3fx_tma_kernel(const int64_t n_cells, const uint32_t *__restrict__ map,
                      const float2 *__restrict__ G, const int *__restrict__ gexp,
                      const double *__restrict__ src, double *__restrict__ dst,
                      const BasisQFX<NM, NQ> basis, const int *__restrict__ done_flag,
-                     int *__restrict__ err_flag) {
+                     int *__restrict__ err_flag, const float2 *__restrict__ jxw) {
   if (done_flag != nullptr && *done_flag) return;
   using L = TmaLayoutQ<NM, NQ, E, ArithDF, 4>;
   constexpr int M2 = NM * NM, Q2 = NQ * NQ, Q3 = NQ * NQ * NQ, MQ = NM * NQ;
@@ -302,6 +306,9 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
     // bound of t_q: colsum|D| times the largest |value| of the own column (r)
     // and of the s- and t-lines it reads
     float tmax = 0.f;
+    const float2 *jxc = MASS ? jxw + (batch * E + el) * Q3 + ab : nullptr;  // this column's JxW
+    float2 jw_next = make_float2(0.f, 0.f);
+    if (MASS && valid) jw_next = __ldg(jxc);
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       df ls[NQ], lt[NQ];
@@ -313,7 +320,17 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
         ms = fmaxf(ms, fabsf(ls[m].hi));
         mt = fmaxf(mt, fabsf(lt[m].hi));
       }
-      const float Cq = s_cD[q] * v3max + s_cD[a] * ms + s_cD[b] * mt;
+      // the mass term JxW u at the point (u: the own column's value at the
+      // Gauss point, still in W0)
+      float2 jw = make_float2(0.f, 0.f);
+      df uq = {0.f, 0.f};
+      if (MASS) {
+        jw = jw_next;
+        if (valid && q + 1 < NQ) jw_next = __ldg(jxc + (q + 1) * Q2);
+        uq = W0[q * Q2 + ab];
+      }
+      const float Cq = s_cD[q] * v3max + s_cD[a] * ms + s_cD[b] * mt +
+                       basis.K * fabsf(jw.x) * fabsf(uq.hi);
       fxacc s;
       {
         const float2 d = sD[q];
@@ -330,6 +347,7 @@ __global__ void __launch_bounds__(E * NQ * NQ, MB)
         fx_fma(s, c0h[m], c0l[m], ls[m].hi, ls[m].lo);
         fx_fma(s, c1h[m], c1l[m], lt[m].hi, lt[m].lo);
       }
+      if (MASS) fx_fma(s, jw.x, jw.y, uq.hi, uq.lo);
       const df tq = fx_finish(s, Cq);
       W0[q * Q2 + ab] = tq;  // the own column; W0's last readers (the gradient) were before barrier C
       tmax = fmaxf(tmax, fabsf(tq.hi));

@@ -27,6 +27,7 @@ struct mfgb_operator {
   double *d_Bq = nullptr, *d_DGq = nullptr;  // BP3: the two matrices below on the device
   double *d_JxW = nullptr;        // Gauss form with a mass term (Helmholtz): [n_cells][n^3]
   float2 *d_JxWdf = nullptr;      // same, double-float pairs
+  float2 *d_JxWfx = nullptr;      // same, times 2^-gexp[cell] of d_Gfx as float pairs
   double DG[100] = {0};           // Gauss forms: collocation derivative on the Gauss points
   double Bq[100] = {0};           // Gauss forms: GLL basis at the Gauss points, Bq[q*n + i]
   bool is_box = false;
@@ -81,8 +82,10 @@ cudaError_t bk5_fx_g64(int N, int64_t n_cells, const uint32_t *map, const double
 // contiguous src / dst (dst overwritten)
 cudaError_t bk5_fx_evec(int N, int64_t nelmt, const double *G, const double *src, double *dst,
                         const double *D, cudaStream_t s);
+// per-cell scaled float pairs of G (and of JxW, with the same per-cell offset)
 cudaError_t g_to_fx(int64_t n_cells, int per_cell, const double *G, float2 *Gfx, int *gexp,
-                    cudaStream_t s);
+                    cudaStream_t s, int per_cell_j = 0, const double *J = nullptr,
+                    float2 *Jfx = nullptr);
 cudaError_t bk5_df_g64(int N, int64_t n_cells, const uint32_t *map, const double *G,
                        const double *src, double *dst, const double *D, cudaStream_t s,
                        const int *done = nullptr);
@@ -141,10 +144,18 @@ cudaError_t dot_to_device(int64_t n, const double *a, const double *b, double *p
 // with offset double-float accumulation (mfgb_bp3_fx.cu): dst += A src over
 // n_cells cells, scaled G pairs Gfx[cell][6][nq^3] with per-cell exponent
 // offsets gexp, host copies of the basis hB[q*nm+i] and the Gauss-point
-// derivative hDG[q*nq+m]; done (may be null): skip when *done is set
+// derivative hDG[q*nq+m]; done (may be null): skip when *done is set; jxw
+// (may be null): the mass term's JxW[cell][nq^3] pairs on the scale of Gfx
 cudaError_t bp3_fx(int degree, int nq, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
                    const int *gexp, const double *src, double *dst, const double *hB,
-                   const double *hDG, cudaStream_t s, const int *done);
+                   const double *hDG, cudaStream_t s, const int *done,
+                   const float2 *jxw = nullptr);
+// the Helmholtz form of bp3_fx (nq = degree + 1, mfgb_helmholtz_fx.cu): the
+// Gauss p+1 Laplacian plus the mass term from jxw, JxW pairs [cell][nq^3] on
+// the scale of Gfx
+cudaError_t helmholtz_fx(int degree, int64_t n_cells, const uint32_t *map, const float2 *Gfx,
+                         const int *gexp, const float2 *jxw, const double *src, double *dst,
+                         const double *hB, const double *hDG, cudaStream_t s, const int *done);
 // CEED BK1 mass operator on E-vectors with offset double-float accumulation and
 // per-element scaling (mfgb_bp3_fx.cu): out = B^T (JxW o B in) per element,
 // host copy of the basis hB[q*nm+i], nq = degree + 2

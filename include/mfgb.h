@@ -41,10 +41,10 @@ enum {
    significant bits; 1e-12 relative against FP64 on the operator).  On GLL
    collocation operators (shapes 5 / 6 of the kernel shape table, the default
    at every degree), their BK6 vector form (every component on its own), the
-   Gauss p+1 Laplacian and the BP3 operator every cell is scaled by a power of
-   two, so any FP64 input range is carried (so are the kernel seams, per
-   element, given a 16-byte aligned G).  Elsewhere (the Helmholtz form,
-   shapes 0-4, seams given an unaligned G) inputs must lie
+   Gauss p+1 Laplacian, its Helmholtz form and the BP3 operator every cell is
+   scaled by a power of two, so any FP64 input range is carried (so are the
+   kernel seams, per element, given a 16-byte aligned G).  Elsewhere (shapes
+   0-4, seams given an unaligned G) inputs must lie
    in the window of MFGB_ERR_RANGE: the operator's own
    geometric factors are checked when their pairs are built (the call returns
    MFGB_ERR_RANGE), caller-supplied G and vectors of the seams on every call,

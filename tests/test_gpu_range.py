@@ -1,11 +1,11 @@
 """Range of the FP64-accurate double-float arithmetic (MFGB_ARITH_FP64_DF).
 
-* GLL collocation (BK5, and BK6 per component), Gauss p+1 and BP3 Laplacians
-  scale every cell by a power of two: source vectors and geometric factors
-  scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled oracle result to the
-  operator's 1e-12 bar.
-* The double-float kernels without per-cell scaling (the Helmholtz form, a
-  seam given an unaligned G) take inputs whose largest magnitude lies in [2^-40, 2^55]:
+* GLL collocation (BK5, and BK6 per component), the Gauss p+1 Laplacian and its
+  Helmholtz form, and BP3 scale every cell by a power of two: source vectors and
+  geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
+  oracle result to the operator's 1e-12 bar.
+* The double-float kernels without per-cell scaling (a seam given an unaligned
+  G) take inputs whose largest magnitude lies in [2^-40, 2^55]:
   inside it they meet 1e-12, outside it they report MFGB_ERR_RANGE (the seam on
   the call, an operator application through the device error word).
 * A NaN in the right-hand side ends conjugate gradients with MFGB_ERR_NONFINITE.
@@ -101,28 +101,35 @@ def test_gll_df_carries_any_geometry_scale(mf, box, gscale):
         assert rel(y.cpu().numpy(), want_s) <= TOL
 
 
-def test_helmholtz_df_range_window(mf, orc):
-    """The Helmholtz form (mass + stiffness at QGauss(p+1)) keeps the TwoSum
-    kernel without per-cell scaling: inside the window 1e-12, outside it the
-    device range word reports MFGB_ERR_RANGE; native FP64 has no window."""
-    from benchmarks_gb300 import MfgbError, _abi
+@pytest.mark.parametrize("scale", [2.0 ** -100, 1e-30, 2.0 ** 300, 1e-280])
+def test_helmholtz_df_carries_any_source_scale(mf, orc, scale):
+    """The Helmholtz form (mass + stiffness at QGauss(p+1)) runs the scaled
+    offset-accumulation kernel with JxW on each cell's G scale: any source
+    scale meets the bar, as native FP64 does."""
     ref = orc.HelmholtzProblem(3, 3, 2, 3, amplitude=0.05)
     H = mf.HelmholtzOperator(mf.BoxMesh(3, 3, 2, degree=3, amplitude=0.05))
     src = np.random.default_rng(5).uniform(-1, 1, ref.n_dofs)
+    want = ref.apply(src) * scale
     y = H.initialize_dof_vector()
-    for scale in (2.0 ** -30, 2.0 ** 40):  # inside the window
-        H.vmult(y, cuda(src * scale), arith="df")
+    for arith in ("df", "fp64"):
+        H.vmult(y, cuda(src * scale), arith=arith)
         mf.check_device_errors()
-        assert rel(y.cpu().numpy(), ref.apply(src) * scale) <= TOL
-    for scale in (2.0 ** -100, 1e-30, 2.0 ** 300):  # outside: reported, not silent
-        H.vmult(y, cuda(src * scale), arith="df")
-        with pytest.raises(MfgbError) as e:
-            mf.check_device_errors()
-        assert e.value.status == _abi.ERR_RANGE
-    mf.check_device_errors()  # the word was cleared
-    H.vmult(y, cuda(src * 1e-30), arith="fp64")  # native FP64 has no window
+        assert rel(y.cpu().numpy(), want) <= TOL
+
+
+@pytest.mark.parametrize("side", [2.0 ** -30, 2.0 ** 30])
+def test_helmholtz_df_carries_any_domain_scale(mf, orc, side):
+    """A box of side L scales G by L and JxW by L^3: the per-cell offset
+    covers both, and the mass and stiffness terms, 2^120 apart in relative
+    size across these cases, meet the bar together."""
+    hi = (side, side, side)
+    ref = orc.HelmholtzProblem(3, 3, 2, 3, amplitude=0.0, hi=hi)
+    H = mf.HelmholtzOperator(mf.BoxMesh(3, 3, 2, degree=3, amplitude=0.0, hi=hi))
+    src = np.random.default_rng(6).uniform(-1, 1, ref.n_dofs)
+    y = H.initialize_dof_vector()
+    H.vmult(y, cuda(src), arith="df")
     mf.check_device_errors()
-    assert rel(y.cpu().numpy(), ref.apply(src) * 1e-30) <= TOL
+    assert rel(y.cpu().numpy(), ref.apply(src)) <= TOL
 
 
 @pytest.mark.parametrize("scale", [2.0 ** -100, 1e-30, 2.0 ** 300])
