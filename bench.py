@@ -294,14 +294,20 @@ def run_ours(args, rank, world):
     for _ in range(3):
         A.vmult_host(h_dst, h_src)
     torch.cuda.synchronize()
+    # three timed blocks, the median reported (the host link is shared with the
+    # machine's other GPUs: one block under a neighbour's transfer stays visible
+    # in e2e_runs_ms without setting the figure)
     e_steps = max(3, min(args.steps, 20))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e_steps):
-        A.vmult_host(h_dst, h_src)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e_steps, world)
+    e2e_runs = []
+    for _ in range(3):
+        e0.record(stream)
+        for _ in range(e_steps):
+            A.vmult_host(h_dst, h_src)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_runs.append(max_over_ranks(e0.elapsed_time(e1) / e_steps, world))
+    e2e_ms = sorted(e2e_runs)[1]
     # correctness guard on the timed result: the device apply of the same src
     A.vmult(dst, src)
     torch.cuda.synchronize()
@@ -311,7 +317,8 @@ def run_ours(args, rank, world):
     # copy rate with both directions busy
     from benchmarks_gb300.rates import link_rates
     link = link_rates(8 * n, 3)
-    return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk, link)
+    return finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk, link,
+                  e2e_runs)
 
 
 def operator_kernel_ms(L, op, d_dst, d_src, arith, sp, stream, steps):
@@ -380,7 +387,8 @@ def degree_sweep(args, degrees=(3, 4, 5, 6, 7, 8), target_dofs=4.0e7):
     return out
 
 
-def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk, link=None):
+def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms, clk, link=None,
+           e2e_runs=None):
     w = WORKLOAD
     if rank != 0:
         return
@@ -420,7 +428,8 @@ def finish(args, rank, world, A, n, n_cells, arith, total_ms, kernel_ms, e2e_ms,
                      "fp64_equiv_tflops": flops / (kernel_ms * 1e-3) / 1e12},
         "e2e": {"value": world * n / (e2e_ms * 1e-3) / 1e9, "unit": "GDoF/s",
                 "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
-                "ms_per_step": e2e_ms, "call": "mfgb_vmult_host (pinned host vectors)"},
+                "ms_per_step": e2e_ms, "e2e_runs_ms": e2e_runs, "timing": "median of 3 blocks",
+                "call": "mfgb_vmult_host (pinned host vectors)"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
