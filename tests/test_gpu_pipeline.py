@@ -102,10 +102,10 @@ def test_gauss_tma_pipelined(mf, orc, p, arith):
 
 
 @pytest.mark.parametrize("arith", ["df", "fp64"])
-def test_helmholtz_tma_pipelined(mf, orc, arith):
+@pytest.mark.parametrize("p", [2, 4, 7])
+def test_helmholtz_tma_pipelined(mf, orc, p, arith):
     import torch
     from benchmarks_gb300 import _abi
-    p = 4
     cells = MESH[p]
     H = mf.HelmholtzOperator(mf.BoxMesh(*cells, degree=p, amplitude=0.06), arith=arith)
     ref = orc.HelmholtzProblem(*cells, p, amplitude=0.06)
