@@ -138,6 +138,11 @@ class LaplaceOperatorBK35 {
     if (ghost_exchange_on)
       check(mfgb_copy_constrained(op_.get(), dst.get_values(), src.get_values(), nullptr));
   }
+  // BK6: the operator on 3 interleaved components (vec[3 dof + c]; dst and src
+  // hold 3 m() entries); GLL operators only
+  void vmult_vector(DeviceVector &dst, const DeviceVector &src) const {
+    check(mfgb_vmult_vector(op_.get(), dst.get_values(), src.get_values(), 3, arith_, nullptr));
+  }
   // host vectors (pinned for overlap): copies pipelined with the apply; returns
   // after the result is in dst
   void vmult_host(double *dst, const double *src) const {
