@@ -4,8 +4,9 @@
   Helmholtz form, and BP3 scale every cell by a power of two: source vectors and
   geometric factors scaled by 2^-100, 1e-30, 1e30 and 2^300 give the scaled
   oracle result to the operator's 1e-12 bar.
-* The double-float kernels without per-cell scaling (a seam given an unaligned
-  G) take inputs whose largest magnitude lies in [2^-40, 2^55]:
+* The double-float kernels without per-cell scaling (the TwoSum collocation
+  shapes 0-4, a seam given an unaligned G) take inputs whose largest magnitude
+  lies in [2^-40, 2^55]:
   inside it they meet 1e-12, outside it they report MFGB_ERR_RANGE (the seam on
   the call, an operator application through the device error word).
 * A NaN in the right-hand side ends conjugate gradients with MFGB_ERR_NONFINITE.
@@ -99,6 +100,38 @@ def test_gll_df_carries_any_geometry_scale(mf, box, gscale):
         want_s = want * gscale * sscale
         want_s[ref.constrained] = src[ref.constrained] * sscale  # identity rows are not scaled by G
         assert rel(y.cpu().numpy(), want_s) <= TOL
+
+
+def test_twosum_shape_df_range_window(mf, box):
+    """The TwoSum collocation kernels (shapes 0-4, chosen by
+    mfgb_set_kernel_shape) carry no per-cell scaling: inside the window 1e-12,
+    outside it the device range word reports MFGB_ERR_RANGE; the scaled
+    default kernel has no window."""
+    import ctypes
+    from benchmarks_gb300 import MfgbError, _abi
+    ref, src, want = box
+    L = mf.lib()
+    old = ctypes.c_int()
+    _abi.check(L.mfgb_get_kernel_shape(1, 4, ctypes.byref(old)))
+    A = mf.LaplaceOperator(mf.BoxMesh(4, 3, 3, degree=4, amplitude=0.1))
+    y = A.initialize_dof_vector()
+    try:
+        _abi.check(L.mfgb_set_kernel_shape(1, 4, 4))  # double-float, p = 4: TwoSum bulk-TMA
+        for scale in (2.0 ** -30, 2.0 ** 40):  # inside the window
+            A.vmult(y, cuda(src * scale), arith="df")
+            mf.check_device_errors()
+            assert rel(y.cpu().numpy(), want * scale) <= TOL
+        for scale in (2.0 ** -100, 1e-30, 2.0 ** 300):  # outside: reported, not silent
+            A.vmult(y, cuda(src * scale), arith="df")
+            with pytest.raises(MfgbError) as e:
+                mf.check_device_errors()
+            assert e.value.status == _abi.ERR_RANGE
+        mf.check_device_errors()  # the word was cleared
+    finally:
+        _abi.check(L.mfgb_set_kernel_shape(1, 4, old.value))
+    A.vmult(y, cuda(src * 1e-30), arith="df")  # the scaled default kernel
+    mf.check_device_errors()
+    assert rel(y.cpu().numpy(), want * 1e-30) <= TOL
 
 
 @pytest.mark.parametrize("scale", [2.0 ** -100, 1e-30, 2.0 ** 300, 1e-280])
